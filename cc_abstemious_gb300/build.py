@@ -1,0 +1,72 @@
+"""Build recipe for libbem_gb300.so (in-tree, sm_103a only).
+
+Each translation unit under csrc/ is compiled by nvcc in parallel, then linked
+into cc_abstemious_gb300/libbem_gb300.so.  Object files go to
+cc_abstemious_gb300/_build/.  No cmake: one -gencode, a few translation units.
+"""
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libbem_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC = os.environ.get("NVCC", "nvcc")
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+          "-I", os.path.join(ROOT, "include")]
+
+
+def sources():
+    return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+
+
+def _headers_mtime():
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    hs.append(os.path.join(ROOT, "include", "bem.h"))
+    return max(os.path.getmtime(h) for h in hs)
+
+
+def _compile(src, verbose, extra):
+    out = os.path.join(OBJ, src + ".o")
+    path = os.path.join(CSRC, src)
+    if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(path), _headers_mtime()):
+        return out
+    cmd = [NVCC] + ARCH + COMMON + extra + ["-c", path, "-o", out]
+    if src.endswith(".cu"):
+        cmd += ["-Xptxas", "-v"] if os.environ.get("BEM_PTXAS_V") else []
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))
+    if r.stderr and (verbose or os.environ.get("BEM_PTXAS_V")):
+        sys.stderr.write(r.stderr)
+    return out
+
+
+def build(force=False, verbose=False, extra=()):
+    os.makedirs(OBJ, exist_ok=True)
+    srcs = sources()
+    if force:
+        for s in srcs:
+            o = os.path.join(OBJ, s + ".o")
+            if os.path.exists(o):
+                os.remove(o)
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose, list(extra)), srcs))
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
+        return LIB
+    cmd = [NVCC] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcuda"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,222 @@
+// Internal definitions shared by the translation units of libbem_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/bem.h"
+
+namespace bem {
+
+// ---------------------------------------------------------------------------
+// Errors: C-ABI functions catch bem::Error and return its status.
+struct Error : std::runtime_error {
+    bem_status status;
+    Error(bem_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define BEM_CUDA(call)                                                                      \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            throw ::bem::Error(e_ == cudaErrorMemoryAllocation ? BEM_ERR_OOM : BEM_ERR_CUDA, \
+                               std::string(#call) + ": " + cudaGetErrorString(e_));         \
+    } while (0)
+
+#define BEM_CHECK_LAUNCH(ctx) \
+    do { (ctx)->launches++; BEM_CUDA(cudaGetLastError()); } while (0)
+
+inline void require(bool ok, const std::string& msg, bem_status s = BEM_ERR_BAD_INPUT) {
+    if (!ok) throw Error(s, msg);
+}
+
+// ---------------------------------------------------------------------------
+// Input model: UserInput of input_data.rs:80-92.
+struct UserInput {
+    std::string mesh_file;
+    int64_t body_index = 0;
+    int freq_kind = 0;  // 0 List, 1 LinearSpaced, 2 LogSpaced
+    std::vector<double> freq_values;
+    double freq_start = 0, freq_end = 0;
+    int64_t freq_number = 0;
+    double sound_speed = 0, mass_density = 0;
+    int problem_type = 1, method_type = 0, solver = 0;
+    double tolerance = 0;
+    int64_t max_iterations = 0;
+    int64_t hm_leaf = 32;      // solve.rs:91-92, :119-120
+    double hm_eta = 4.0;       // h_matrix.rs:136
+    double hm_aca_tol = 1e-4;  // solve.rs:92, :120
+    int incident_type = 0;
+    double incident_vec[3] = {0, 0, 0};
+    double incident_amp[2] = {0, 0};
+    int bc_type = 1;
+    double bc_value[2] = {0, 0};
+    int output_total = 0, output_pressure = 1;
+    std::string output_file;
+    std::vector<double> field_points;  // nfp x 3
+};
+
+struct Mesh {
+    std::vector<double> nodes;  // 3 * nnodes
+    std::vector<int64_t> body;
+    std::vector<int32_t> etype;
+    std::vector<int64_t> conn_off;
+    std::vector<int64_t> conn;
+    int64_t nbodies = 0;
+    int64_t nelem() const { return (int64_t)body.size(); }
+    int64_t nnodes() const { return (int64_t)nodes.size() / 3; }
+};
+
+UserInput parse_user_input(const std::string& json_text);
+Mesh read_vtk(const std::string& path);
+std::vector<double> frequency_list(const UserInput& in);
+
+// ---------------------------------------------------------------------------
+// Device buffer with grow-only capacity.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void ensure(size_t n) {
+        if (n <= bytes) return;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        BEM_CUDA(cudaMalloc(&p, n));
+        bytes = n;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    ~DevBuf() { release(); }
+};
+
+// Collocation geometry, structure of arrays on the device.  Every array is
+// padded to `npad` (a multiple of 64) so that 64-point tiles can be copied into
+// shared memory with 16-byte aligned bulk copies.
+struct DevGeometry {
+    int64_t n = 0, npad = 0;
+    DevBuf buf;  // GEO_NARR arrays of npad doubles (see GeoArr)
+    DevBuf buf32;  // GEO32_NARR arrays of npad floats (float-float coordinates, see Geo32Arr)
+    double* arr(int k) const { return buf.as<double>() + (size_t)k * npad; }
+    float* arr32(int k) const { return buf32.as<float>() + (size_t)k * npad; }
+};
+
+// x y z: collocation point; nx ny nz: unit normal as stored by the reference;
+// ex ey ez: that normal normalised again (influence_matrix.rs:14-15 normalises
+// per pair; the result only depends on the point); wa = wt * area.
+enum GeoArr { GX = 0, GY, GZ, GNX, GNY, GNZ, GAREA, GWT, GWA, GEX, GEY, GEZ, GEO_NARR };
+// Single-precision copy for the mixed form: coordinates split hi + lo.
+enum Geo32Arr { FXH = 0, FXL, FYH, FYL, FZH, FZL, FEX, FEY, FEZ, FWA, GEO32_NARR };
+
+struct Problem {
+    UserInput in;
+    Mesh mesh;
+    std::vector<double> freqs;
+    int64_t ifreq = 0;
+    std::vector<double> cpts;  // host copy, n x 8
+    int64_t n = 0, nfp = 0;
+    DevGeometry geo;           // device collocation (computed by the collocation kernel)
+    DevBuf d_fp;               // field points, 3 arrays of nfp_pad
+    int64_t nfp_pad = 0;
+    int device = 0;
+    double frequency() const { return freqs.empty() ? 0.0 : freqs[(size_t)ifreq]; }
+    double omega() const { return 2.0 * 3.14159265358979323846 * frequency(); }
+    double wavenumber() const { return omega() / in.sound_speed; }
+};
+
+// Per-stage timing recorded when profiling is enabled (CUDA events).
+struct Stage {
+    std::string name;
+    double ms = 0;
+    int64_t launches = 0;
+    double bytes = 0;
+};
+
+struct Context {
+    int device = 0;
+    bool profiling = false;
+    std::vector<Stage> stages;
+    void stage_add(const std::string& name, double ms, int64_t launches, double bytes) {
+        for (auto& s : stages)
+            if (s.name == name) {
+                s.ms += ms;
+                s.launches += launches;
+                s.bytes += bytes;
+                return;
+            }
+        stages.push_back({name, ms, launches, bytes});
+    }
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    int64_t launches = 0;
+    // workspaces (grow-only)
+    DevBuf w_mat, w_mat2, w_vec, w_small, w_flags, w_part;
+    // results of the last bem_run
+    std::vector<double> last_phi, last_vn;
+    int64_t last_n = 0, last_nf = 0;
+    void sync() { BEM_CUDA(cudaStreamSynchronize(stream)); }
+};
+
+// ---------------------------------------------------------------------------
+// Host-side complex helpers.
+struct cd { double re, im; };
+
+// Kernel-side launch wrappers (defined in the .cu files).
+void compute_collocation(Context& ctx, Problem& p);
+void upload_field_points(Context& ctx, Problem& p);
+
+// Problem scalars on the device.
+struct KParams {
+    double k;        // wavenumber
+    double beta_im;  // BM coupling i/k -> imaginary part 1/k (0 for classical)
+    int bm;          // Burton-Miller
+    double hdiag;    // -0.5 exterior, 0 interior
+    double gdiag_im; // BM: 0.5/k
+};
+KParams kparams(const Problem& p);
+void lhs_factors(const Problem& p, cd& a, cd& b);
+void rhs_factors(const Problem& p, cd& a, cd& b);
+
+// Assembly (assembly.cu)
+void assemble_surface_fp64(Context& ctx, const Problem& p, double2* H, double2* G, int64_t ld);
+// A = alpha H + beta G and rowsum(gamma H + delta G) partials (fused solve path)
+void assemble_system_fp64(Context& ctx, const Problem& p, double2* A, int64_t ld, cd alpha, cd beta,
+                          cd gamma, cd delta, double2* rowsum /* n, may be null */);
+void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
+                               const cd* betas, const cd* gammas, const cd* deltas, int nsys, float2* A,
+                               int64_t ld, size_t mat_stride, double2* rowsum, size_t vec_stride);
+void field_matrices_fp64(Context& ctx, const Problem& p, double2* M, double2* L, int64_t ld);
+void evaluate_field(Context& ctx, const Problem& p, const double2* phi, const double2* vn,
+                    const double2* inc, double2* out);
+void row_or_column(Context& ctx, const Problem& p, const int64_t* dI, int64_t ni, const int64_t* dJ,
+                   int64_t nj, int side, double2* out, int64_t diag_pos);
+void incident_surface(Context& ctx, const Problem& p, double2* out);
+void incident_field(Context& ctx, const Problem& p, double2* out);
+
+// Dense linear algebra (dense.cu)
+void lu_factor_fp64(Context& ctx, int64_t n, double2* A, int64_t lda, int32_t* d_piv, int* d_info);
+void lu_solve_fp64(Context& ctx, int64_t n, const double2* A, int64_t lda, const int32_t* d_piv,
+                   double2* b);
+void gemv_fp64(Context& ctx, int64_t m, int64_t n, const double2* A, int64_t lda, const double2* x,
+               double2* y, cd alpha, cd beta);
+double frob_norm_fp64(Context& ctx, int64_t m, int64_t n, const double2* A, int64_t lda);
+
+// GMRES (gmres.cu)
+struct GmresResult {
+    int64_t num_mv = 0, restarts = 0, iterations = 0;
+    double error = 0;
+    int flag = 0;
+};
+// Reference-faithful GMRES over a dense FP64 matrix (device), x in/out (device).
+GmresResult gmres_dense_fp64(Context& ctx, int64_t n, const double2* A, int64_t lda, int64_t max_it,
+                             double tol, double2* x);
+
+}  // namespace bem

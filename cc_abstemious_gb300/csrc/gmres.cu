@@ -1,0 +1,597 @@
+// Restarted GMRES (gmres.rs:35-202) as a device-side state machine over a
+// batch of independent systems of equal size n.
+//
+// One iteration is the fixed launch sequence
+//   apply(START) -> start -> apply(Q) -> arnoldi -> apply(CHECK) -> check
+// where every kernel reads the per-system state and returns immediately when
+// it has nothing to do.  The sequence can therefore be issued step by step
+// (plain form, host reads the state after each step) or captured into a CUDA
+// graph covering several iterations of every system (batched form).
+//
+// Operator: FP64 matrix (plain form, bit-for-bit the reference arithmetic up
+// to summation order) or FP32 matrix with FP64 vectors and compensated
+// products/sums (mixed form).  Arnoldi (modified Gram-Schmidt), Givens
+// rotations, the small triangular solve and the stopping test are FP64.
+#include "common.cuh"
+#include "complex.cuh"
+#include "gmres.cuh"
+
+namespace bem {
+
+constexpr int MV_ROWS_PER_THREAD = 2;
+constexpr int MV_THREADS = 256;
+constexpr int MV_ROWS = MV_ROWS_PER_THREAD * MV_THREADS;  // 512
+constexpr int MV_COLS = 512;
+constexpr int AR_THREADS = 1024;
+
+__device__ __forceinline__ bool mv_active(const GmState& s, int mode) {
+    if (s.done) return false;
+    if (mode == MV_START) return s.need_start != 0;
+    if (mode == MV_Q) return s.need_start == 0 && s.check == 0;
+    return s.check != 0;  // MV_CHECK
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// acc (hi, lo) += a * b with a*b = p + e exactly (FMA) and a small extra term.
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float a, float b) {
+    float p = a * b;
+    float e = fmaf(a, b, -p);
+    float s, err;
+    two_sum(hi, p, s, err);
+    hi = s;
+    lo += err + e;
+}
+
+// Batched operator application W_s = A_s v_s, v_s = x_s (START/CHECK) or
+// Q_s[:, k] (Q).  Grid (row blocks, column chunks, systems); partial sums of
+// the column chunks are reduced in a fixed order by the last CTA of each row
+// block (ticket counter, no waiting).
+template <typename T>
+__global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mode) {
+    const int s = blockIdx.z;
+    GmState& st = bt.st[s];
+    if (!mv_active(st, mode)) return;
+    const int64_t n = bt.n;
+    const double2* v = (mode == MV_Q) ? bt.Q + (size_t)s * bt.qstride + (size_t)st.k * n : bt.X + (size_t)s * n;
+    __shared__ float2 xh[MV_COLS], xl[MV_COLS];
+    __shared__ double2 xd[MV_COLS];
+    __shared__ int last;
+    const int64_t j0 = (int64_t)blockIdx.y * MV_COLS;
+    const int jn = (int)min((int64_t)MV_COLS, n - j0);
+    for (int t = threadIdx.x; t < jn; t += MV_THREADS) {
+        double2 x = v[j0 + t];
+        if (sizeof(T) == sizeof(float2)) {
+            float hx = (float)x.x, hy = (float)x.y;
+            xh[t] = make_float2(hx, hy);
+            xl[t] = make_float2((float)(x.x - (double)hx), (float)(x.y - (double)hy));
+        } else {
+            xd[t] = x;
+        }
+    }
+    __syncthreads();
+    const int64_t i0 = (int64_t)blockIdx.x * MV_ROWS + MV_ROWS_PER_THREAD * threadIdx.x;
+    double2 r0 = make_double2(0, 0), r1 = make_double2(0, 0);
+    if (i0 < n) {
+        if (sizeof(T) == sizeof(float2)) {
+            const float2* A = reinterpret_cast<const float2*>(bt.A) + (size_t)s * bt.mat_stride;
+            // float-float accumulators for (re0, im0, re1, im1)
+            float h0 = 0, l0 = 0, h1 = 0, l1 = 0, h2 = 0, l2 = 0, h3 = 0, l3 = 0;
+            const bool pair = (i0 + 1 < n);
+            for (int q = 0; q < jn; ++q) {
+                const float2* col = A + (j0 + q) * bt.lda + i0;
+                float4 a;
+                if (pair) a = *reinterpret_cast<const float4*>(col);
+                else { float2 t = col[0]; a = make_float4(t.x, t.y, 0.f, 0.f); }
+                float2 H = xh[q], L = xl[q];
+                ff_acc(h0, l0, a.x, H.x); ff_acc(h0, l0, -a.y, H.y);
+                ff_acc(h1, l1, a.x, H.y); ff_acc(h1, l1, a.y, H.x);
+                ff_acc(h2, l2, a.z, H.x); ff_acc(h2, l2, -a.w, H.y);
+                ff_acc(h3, l3, a.z, H.y); ff_acc(h3, l3, a.w, H.x);
+                l0 = fmaf(a.x, L.x, fmaf(-a.y, L.y, l0));
+                l1 = fmaf(a.x, L.y, fmaf(a.y, L.x, l1));
+                l2 = fmaf(a.z, L.x, fmaf(-a.w, L.y, l2));
+                l3 = fmaf(a.z, L.y, fmaf(a.w, L.x, l3));
+            }
+            r0 = make_double2((double)h0 + (double)l0, (double)h1 + (double)l1);
+            r1 = make_double2((double)h2 + (double)l2, (double)h3 + (double)l3);
+        } else {
+            const double2* A = reinterpret_cast<const double2*>(bt.A) + (size_t)s * bt.mat_stride;
+            const bool pair = (i0 + 1 < n);
+            for (int q = 0; q < jn; ++q) {
+                const double2* col = A + (j0 + q) * bt.lda + i0;
+                double2 xv = xd[q];
+                cfma(r0, col[0], xv);
+                if (pair) cfma(r1, col[1], xv);
+            }
+        }
+        double2* part = bt.part + ((size_t)s * gridDim.y + blockIdx.y) * bt.n_pad;
+        part[i0] = r0;
+        if (i0 + 1 < n) part[i0 + 1] = r1;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int* tk = bt.tickets + (size_t)s * gridDim.x + blockIdx.x;
+        last = (atomicAdd(tk, 1) == (int)gridDim.y - 1);
+        if (last) *tk = 0;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double2* W = bt.W + (size_t)s * n;
+    for (int rr = 0; rr < MV_ROWS_PER_THREAD; ++rr) {
+        int64_t i = i0 + rr;
+        if (i >= n) break;
+        double2 acc = make_double2(0, 0);
+        const double2* part = bt.part + (size_t)s * gridDim.y * bt.n_pad;
+        for (int c = 0; c < (int)gridDim.y; ++c) acc = cadd(acc, part[(size_t)c * bt.n_pad + i]);
+        W[i] = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Block-wide FP64 reductions (1024 threads).
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = l < (int)(blockDim.x >> 5) ? sh[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (l == 0) sh[32] = v;
+    }
+    __syncthreads();
+    return sh[32];
+}
+
+__device__ __forceinline__ double2 block_sum2(double2 v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) { sh[2 * w] = v.x; sh[2 * w + 1] = v.y; }
+    __syncthreads();
+    if (w == 0) {
+        int nw = blockDim.x >> 5;
+        v.x = l < nw ? sh[2 * l] : 0.0;
+        v.y = l < nw ? sh[2 * l + 1] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+        }
+        if (l == 0) { sh[64] = v.x; sh[65] = v.y; }
+    }
+    __syncthreads();
+    return make_double2(sh[64], sh[65]);
+}
+
+__device__ double vec_norm(const double2* v, int64_t n, double* sh) {
+    double s = 0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += v[i].x * v[i].x + v[i].y * v[i].y;
+    return sqrt(block_sum(s, sh));
+}
+
+// Cycle start (gmres.rs:84-106): r = b - A x, q_0 = r / ||r||, beta_0 = ||r||.
+__global__ void __launch_bounds__(AR_THREADS) gm_start_kernel(GmBatch bt) {
+    const int s = blockIdx.x;
+    GmState& st = bt.st[s];
+    if (st.done || !st.need_start) return;
+    __shared__ double sh[80];
+    const int64_t n = bt.n;
+    const double2* b = bt.B + (size_t)s * n;
+    const double2* W = bt.W + (size_t)s * n;
+    double2* Q = bt.Q + (size_t)s * bt.qstride;
+    double acc = 0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        double2 r = csub(b[i], W[i]);
+        Q[i] = r;
+        acc += r.x * r.x + r.y * r.y;
+    }
+    double rn = sqrt(block_sum(acc, sh));
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        double2 r = Q[i];
+        Q[i] = make_double2(r.x / rn, r.y / rn);
+    }
+    double xn = vec_norm(bt.X + (size_t)s * n, n, sh);
+    if (threadIdx.x == 0) {
+        GmSmall sm = gm_small(bt, s);
+        for (int i = 0; i <= bt.m; ++i) sm.beta[i] = make_double2(0, 0);
+        for (int i = 0; i < bt.m; ++i) { sm.cs[i] = make_double2(0, 0); sm.sn[i] = make_double2(0, 0); }
+        sm.beta[0] = make_double2(rn, 0.0);
+        st.xnorm = xn;
+        st.error = rn / (st.anorm * xn + st.bnorm);
+        st.k = 0;
+        st.need_start = 0;
+        st.check = 0;
+        st.num_mv += 1;
+    }
+}
+
+// Arnoldi step k with modified Gram-Schmidt (gmres.rs:158-176), Givens
+// update (gmres.rs:178-202), residual estimate and, when the estimate passes
+// or the cycle ends, the solution update x += Q_k H_k^{-1} beta_k
+// (gmres.rs:146-157).  The Krylov vector w lives in shared memory when it
+// fits (`w_in_smem`), else in the W buffer.
+__global__ void __launch_bounds__(AR_THREADS) gm_arnoldi_kernel(GmBatch bt, int w_in_smem) {
+    const int s = blockIdx.x;
+    GmState& st = bt.st[s];
+    if (st.done || st.need_start || st.check) return;
+    extern __shared__ double2 wsh[];
+    __shared__ double sh[80];
+    __shared__ double2 hsh;
+    const int64_t n = bt.n;
+    const int k = st.k;
+    const int m = bt.m;
+    double2* Q = bt.Q + (size_t)s * bt.qstride;
+    double2* Wg = bt.W + (size_t)s * n;
+    double2* w = w_in_smem ? wsh : Wg;
+    if (w_in_smem)
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) w[i] = Wg[i];
+    __syncthreads();
+    GmSmall sm = gm_small(bt, s);
+    // modified Gram-Schmidt
+    for (int i = 0; i <= k; ++i) {
+        const double2* qi = Q + (size_t)i * n;
+        double2 acc = make_double2(0, 0);
+        for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
+            double2 a = w[l], q = qi[l];
+            if (bt.ref_dotc) cfma(acc, cconj(a), q);  // nalgebra dotc(qk1, q_i) = sum conj(qk1) q_i
+            else cfma(acc, cconj(q), a);             // q_i^H w
+        }
+        double2 h = block_sum2(acc, sh);
+        for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
+            double2 a = w[l];
+            cfma(a, cneg(h), qi[l]);
+            w[l] = a;
+        }
+        if (threadIdx.x == 0) sm.hk1[i] = h;
+        __syncthreads();
+    }
+    double hn = vec_norm(w, n, sh);
+    double2* qk1 = Q + (size_t)(k + 1) * n;
+    // scale = 1 / hk1[k+1] as a complex division (gmres.rs:172)
+    double2 scale = cdiv(make_double2(1.0, 0.0), make_double2(hn, 0.0));
+    for (int64_t l = threadIdx.x; l < n; l += blockDim.x) qk1[l] = cmul(w[l], scale);
+    if (threadIdx.x == 0) {
+        sm.hk1[k + 1] = make_double2(hn, 0.0);
+        // apply previous rotations
+        for (int i = 0; i < k; ++i) {
+            double2 t = cadd(cmul(sm.cs[i], sm.hk1[i]), cmul(sm.sn[i], sm.hk1[i + 1]));
+            sm.hk1[i + 1] = cadd(cmul(cneg(cconj(sm.sn[i])), sm.hk1[i]), cmul(sm.cs[i], sm.hk1[i + 1]));
+            sm.hk1[i] = t;
+        }
+        // new rotation (LAWN 148)
+        double2 v1 = sm.hk1[k], v2 = sm.hk1[k + 1];
+        double a1 = cabs_(v1);
+        double2 signf = (v1.x == 0.0 && v1.y == 0.0) ? make_double2(1.0, 0.0) : make_double2(v1.x / a1, v1.y / a1);
+        double r = sqrt(cnorm2(v1) + cnorm2(v2));
+        double2 cs = make_double2(a1 / r, 0.0);
+        double2 sn = cmul(signf, cconj(v2));
+        sn = make_double2(sn.x / r, sn.y / r);
+        sm.cs[k] = cs;
+        sm.sn[k] = sn;
+        sm.hk1[k] = cadd(cmul(cs, sm.hk1[k]), cmul(sn, sm.hk1[k + 1]));
+        sm.hk1[k + 1] = make_double2(0, 0);
+        for (int i = 0; i < k + 2; ++i) sm.H[(size_t)k * (m + 1) + i] = sm.hk1[i];
+        sm.beta[k + 1] = cmul(cneg(cconj(sn)), sm.beta[k]);
+        sm.beta[k] = cmul(sm.beta[k], cs);
+        st.error = cabs_(sm.beta[k + 1]) / (st.anorm * st.xnorm + st.bnorm);
+        st.num_mv += 1;
+        st.iterations += 1;
+        int chk = (st.error < st.tol) || (k == m - 1);
+        st.check = chk;
+        if (chk) {
+            // y = H_k^{-1} beta_k: H_k is upper triangular after the rotations
+            for (int i = k; i >= 0; --i) {
+                double2 v = sm.beta[i];
+                for (int q = i + 1; q <= k; ++q) v = csub(v, cmul(sm.H[(size_t)q * (m + 1) + i], sm.y[q]));
+                sm.y[i] = cdiv(v, sm.H[(size_t)i * (m + 1) + i]);
+            }
+        } else {
+            st.k = k + 1;
+        }
+        hsh.x = chk;
+    }
+    __syncthreads();
+    if (hsh.x != 0.0) {
+        double2* x = bt.X + (size_t)s * n;
+        for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
+            double2 a = x[l];
+            for (int j = 0; j <= k; ++j) cfma(a, Q[(size_t)j * n + l], sm.y[j]);
+            x[l] = a;
+        }
+    }
+}
+
+// True residual check (gmres.rs:122-138).
+__global__ void __launch_bounds__(AR_THREADS) gm_check_kernel(GmBatch bt) {
+    const int s = blockIdx.x;
+    GmState& st = bt.st[s];
+    if (st.done || !st.check) return;
+    __shared__ double sh[80];
+    const int64_t n = bt.n;
+    const double2* b = bt.B + (size_t)s * n;
+    const double2* W = bt.W + (size_t)s * n;
+    double acc = 0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        double2 r = csub(b[i], W[i]);
+        acc += r.x * r.x + r.y * r.y;
+    }
+    double rn = sqrt(block_sum(acc, sh));
+    double xn = vec_norm(bt.X + (size_t)s * n, n, sh);
+    if (threadIdx.x == 0) {
+        st.num_mv += 1;
+        st.xnorm = xn;
+        st.error = rn / (st.anorm * xn + st.bnorm);
+        st.check = 0;
+        if (st.error < st.tol) {
+            st.done = 1;
+            st.converged = 1;
+        } else if (st.k == bt.m - 1) {
+            st.restarts += 1;
+            if (st.restarts >= st.max_restarts) st.done = 1;
+            else st.need_start = 1;
+        } else {
+            st.k += 1;
+        }
+    }
+}
+
+// Zero initial guess and the per-system constants.
+__global__ void gm_init_kernel(GmBatch bt, const double* anorm, double tol, int64_t max_restarts) {
+    const int s = blockIdx.x;
+    __shared__ double sh[80];
+    const int64_t n = bt.n;
+    double2* x = bt.X + (size_t)s * n;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) x[i] = make_double2(0, 0);
+    double bn = vec_norm(bt.B + (size_t)s * n, n, sh);
+    if (threadIdx.x == 0) {
+        GmState& st = bt.st[s];
+        st.anorm = anorm[s];
+        st.bnorm = bn;
+        st.tol = tol;
+        st.xnorm = 0;
+        st.error = 1.0;
+        st.k = 0;
+        st.need_start = 1;
+        st.check = 0;
+        st.done = 0;
+        st.converged = 0;
+        st.num_mv = 0;
+        st.iterations = 0;
+        st.restarts = 0;
+        st.max_restarts = max_restarts;
+        if (bn == 0.0) {  // zero right-hand side: x = 0 is exact
+            st.done = 1;
+            st.converged = 1;
+            st.error = 0;
+        }
+    }
+}
+
+// Frobenius norms of a batch of matrices (FP64 or FP32 entries).
+template <typename T>
+__global__ void batch_frob_kernel(const void* A, int64_t n, int64_t lda, size_t mat_stride, double* part, int nb) {
+    __shared__ double sh[80];
+    int s = blockIdx.y;
+    const T* M = reinterpret_cast<const T*>(A) + (size_t)s * mat_stride;
+    double acc = 0;
+    int64_t total = n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t j = t / n, i = t - j * n;
+        T v = M[j * lda + i];
+        acc += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+    }
+    double r = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[(size_t)s * nb + blockIdx.x] = r;
+}
+
+__global__ void finish_norms_kernel(const double* part, int nb, int nsys, double* out) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    double acc = 0;
+    for (int b = 0; b < nb; ++b) acc += part[(size_t)s * nb + b];
+    out[s] = sqrt(acc);
+}
+
+// ---------------------------------------------------------------------------
+GmWorkspace::~GmWorkspace() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+}
+
+void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const void* A, int64_t lda,
+                size_t mat_stride, bool fp32, bool ref_dotc) {
+    GmBatch& bt = ws.bt;
+    bt.nsys = nsys;
+    bt.n = n;
+    bt.n_pad = (n + MV_ROWS - 1) / MV_ROWS * MV_ROWS;
+    bt.m = m;
+    bt.A = A;
+    bt.lda = lda;
+    bt.mat_stride = mat_stride;
+    bt.ref_dotc = ref_dotc ? 1 : 0;
+    bt.qstride = (size_t)n * (m + 1);
+    ws.fp32 = fp32;
+    int rb = (int)((n + MV_ROWS - 1) / MV_ROWS), cb = (int)((n + MV_COLS - 1) / MV_COLS);
+    ws.rb = rb;
+    ws.cb = cb;
+    size_t small = gm_small_size(m);
+    size_t bytes = 0;
+    auto carve = [&](size_t b) { size_t o = bytes; bytes += (b + 255) / 256 * 256; return o; };
+    size_t oX = carve(sizeof(double2) * nsys * n), oB = carve(sizeof(double2) * nsys * n);
+    size_t oQ = carve(sizeof(double2) * nsys * bt.qstride), oW = carve(sizeof(double2) * nsys * n);
+    size_t oP = carve(sizeof(double2) * nsys * cb * bt.n_pad), oT = carve(sizeof(int) * nsys * rb);
+    size_t oS = carve(sizeof(double2) * nsys * small), oSt = carve(sizeof(GmState) * nsys);
+    size_t oN = carve(sizeof(double) * nsys * 1024 + sizeof(double) * nsys);
+    ws.mem.ensure(bytes);
+    char* base = ws.mem.as<char>();
+    bt.X = reinterpret_cast<double2*>(base + oX);
+    bt.B = reinterpret_cast<double2*>(base + oB);
+    bt.Q = reinterpret_cast<double2*>(base + oQ);
+    bt.W = reinterpret_cast<double2*>(base + oW);
+    bt.part = reinterpret_cast<double2*>(base + oP);
+    bt.tickets = reinterpret_cast<int*>(base + oT);
+    bt.small = reinterpret_cast<double2*>(base + oS);
+    bt.small_stride = small;
+    bt.st = reinterpret_cast<GmState*>(base + oSt);
+    ws.norm_part = reinterpret_cast<double*>(base + oN);
+    ws.anorm = ws.norm_part + (size_t)nsys * 1024;
+    BEM_CUDA(cudaMemsetAsync(bt.tickets, 0, sizeof(int) * nsys * rb, ctx.stream));
+    ws.w_in_smem = (n * sizeof(double2) <= 200 * 1024);
+    if (ws.w_in_smem) {
+        BEM_CUDA(cudaFuncSetAttribute(gm_arnoldi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(n * sizeof(double2))));
+    }
+    if (ws.graph_exec) {
+        cudaGraphExecDestroy(ws.graph_exec);
+        ws.graph_exec = nullptr;
+    }
+}
+
+void gm_matrix_norms(Context& ctx, GmWorkspace& ws) {
+    const int nb = 512;
+    dim3 grid(nb, ws.bt.nsys);
+    if (ws.fp32)
+        batch_frob_kernel<float2><<<grid, 256, 0, ctx.stream>>>(ws.bt.A, ws.bt.n, ws.bt.lda, ws.bt.mat_stride,
+                                                                ws.norm_part, nb);
+    else
+        batch_frob_kernel<double2><<<grid, 256, 0, ctx.stream>>>(ws.bt.A, ws.bt.n, ws.bt.lda, ws.bt.mat_stride,
+                                                                 ws.norm_part, nb);
+    BEM_CHECK_LAUNCH(&ctx);
+    finish_norms_kernel<<<(ws.bt.nsys + 127) / 128, 128, 0, ctx.stream>>>(ws.norm_part, nb, ws.bt.nsys, ws.anorm);
+    BEM_CHECK_LAUNCH(&ctx);
+}
+
+void gm_init(Context& ctx, GmWorkspace& ws, double tol, int64_t max_restarts) {
+    gm_init_kernel<<<ws.bt.nsys, AR_THREADS, 0, ctx.stream>>>(ws.bt, ws.anorm, tol, max_restarts);
+    BEM_CHECK_LAUNCH(&ctx);
+}
+
+static void launch_apply(Context& ctx, GmWorkspace& ws, int mode) {
+    dim3 grid((unsigned)ws.rb, (unsigned)ws.cb, (unsigned)ws.bt.nsys);
+    if (ws.fp32) gm_apply_kernel<float2><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+    else gm_apply_kernel<double2><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+    BEM_CHECK_LAUNCH(&ctx);
+}
+
+void gm_launch_iteration(Context& ctx, GmWorkspace& ws, cudaEvent_t ev_q0, cudaEvent_t ev_q1) {
+    int nsys = ws.bt.nsys;
+    launch_apply(ctx, ws, MV_START);
+    gm_start_kernel<<<nsys, AR_THREADS, 0, ctx.stream>>>(ws.bt);
+    BEM_CHECK_LAUNCH(&ctx);
+    if (ev_q0) BEM_CUDA(cudaEventRecord(ev_q0, ctx.stream));
+    launch_apply(ctx, ws, MV_Q);
+    if (ev_q1) BEM_CUDA(cudaEventRecord(ev_q1, ctx.stream));
+    size_t dyn = ws.w_in_smem ? (size_t)ws.bt.n * sizeof(double2) : 0;
+    gm_arnoldi_kernel<<<nsys, AR_THREADS, dyn, ctx.stream>>>(ws.bt, ws.w_in_smem ? 1 : 0);
+    BEM_CHECK_LAUNCH(&ctx);
+    launch_apply(ctx, ws, MV_CHECK);
+    gm_check_kernel<<<nsys, AR_THREADS, 0, ctx.stream>>>(ws.bt);
+    BEM_CHECK_LAUNCH(&ctx);
+}
+
+void gm_read_states(Context& ctx, GmWorkspace& ws, std::vector<GmState>& out) {
+    out.resize(ws.bt.nsys);
+    BEM_CUDA(cudaMemcpyAsync(out.data(), ws.bt.st, sizeof(GmState) * ws.bt.nsys, cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+}
+
+// Run to completion.  chunk == 0: one iteration at a time with a state read
+// after each; chunk > 0: a CUDA graph of `chunk` iterations, state read after
+// each graph launch.
+void gm_run(Context& ctx, GmWorkspace& ws, int chunk, int64_t max_total_iterations) {
+    std::vector<GmState> st, prev;
+    int64_t issued = 0;
+    if (chunk <= 0) {
+        // one iteration at a time; with profiling, time the Krylov mat-vec of
+        // every iteration with events on the launching stream
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (ctx.profiling) {
+            BEM_CUDA(cudaEventCreate(&e0));
+            BEM_CUDA(cudaEventCreate(&e1));
+        }
+        gm_read_states(ctx, ws, prev);
+        for (;;) {
+            gm_launch_iteration(ctx, ws, e0, e1);
+            ++issued;
+            gm_read_states(ctx, ws, st);
+            if (ctx.profiling) {
+                float ms = 0;
+                BEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                int64_t active = 0;
+                for (size_t s = 0; s < st.size(); ++s) active += st[s].iterations - prev[s].iterations;
+                if (active > 0)
+                    ctx.stage_add(ws.fp32 ? "gmres_matvec_fp32" : "gmres_matvec_fp64", ms, 1,
+                                  (double)active * ws.bt.n * ws.bt.n * (ws.fp32 ? 8.0 : 16.0));
+            }
+            prev = st;
+            bool all = true;
+            for (auto& s : st) all = all && s.done;
+            if (all || issued >= max_total_iterations) break;
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        return;
+    }
+    if (!ws.graph_exec || ws.graph_chunk != chunk) {
+        if (ws.graph_exec) cudaGraphExecDestroy(ws.graph_exec);
+        ws.graph_exec = nullptr;
+        cudaGraph_t g;
+        int64_t before = ctx.launches;
+        BEM_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
+        for (int c = 0; c < chunk; ++c) gm_launch_iteration(ctx, ws, nullptr, nullptr);
+        BEM_CUDA(cudaStreamEndCapture(ctx.stream, &g));
+        ws.launches_per_graph = ctx.launches - before;
+        ctx.launches = before;
+        BEM_CUDA(cudaGraphInstantiate(&ws.graph_exec, g, 0));
+        cudaGraphDestroy(g);
+        ws.graph_chunk = chunk;
+    }
+    for (;;) {
+        BEM_CUDA(cudaGraphLaunch(ws.graph_exec, ctx.stream));
+        ctx.launches += ws.launches_per_graph;
+        issued += chunk;
+        gm_read_states(ctx, ws, st);
+        bool all = true;
+        for (auto& s : st) all = all && s.done;
+        if (all || issued >= max_total_iterations) break;
+    }
+}
+
+// gmres.rs:35-59 GMRES::solve over one dense FP64 matrix on the device.
+GmresResult gmres_dense_fp64(Context& ctx, int64_t n, const double2* A, int64_t lda, int64_t max_it, double tol,
+                             double2* x) {
+    if (max_it <= 0) max_it = 1000;
+    if (max_it > n) max_it = n;
+    if (tol <= 0.0) tol = 1e-5;
+    int m = (int)std::ceil(std::sqrt((double)max_it));
+    int64_t restarts = max_it / m;
+    GmWorkspace ws;
+    gm_prepare(ctx, ws, 1, n, m, A, lda, 0, false, true);
+    BEM_CUDA(cudaMemcpyAsync(ws.bt.B, x, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+    gm_matrix_norms(ctx, ws);
+    gm_init(ctx, ws, tol, restarts);
+    gm_run(ctx, ws, 0, restarts * (int64_t)m + 1);
+    std::vector<GmState> st;
+    gm_read_states(ctx, ws, st);
+    BEM_CUDA(cudaMemcpyAsync(x, ws.bt.X, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+    ctx.sync();
+    GmresResult r;
+    r.num_mv = st[0].num_mv;
+    r.restarts = st[0].restarts + (st[0].converged ? 1 : 0);
+    r.iterations = st[0].iterations;
+    r.error = st[0].error;
+    r.flag = st[0].converged ? 1 : 2;
+    return r;
+}
+
+}  // namespace bem

@@ -1,0 +1,73 @@
+// Batched restarted GMRES state (see gmres.cu).
+#pragma once
+#include "common.cuh"
+
+namespace bem {
+
+enum { MV_START = 0, MV_Q = 1, MV_CHECK = 2 };
+
+struct GmState {
+    double anorm, bnorm, tol, xnorm, error;
+    int k, need_start, check, done, converged, pad;
+    long long num_mv, iterations, restarts, max_restarts;
+};
+
+struct GmBatch {
+    int nsys, m, ref_dotc, pad;
+    int64_t n, n_pad, lda;
+    size_t mat_stride, qstride, small_stride;
+    const void* A;      // nsys matrices (double2 or float2), column-major, leading dim lda
+    double2* X;         // nsys x n solutions
+    double2* B;         // nsys x n right-hand sides
+    double2* Q;         // nsys x n x (m+1) Krylov bases
+    double2* W;         // nsys x n operator outputs
+    double2* part;      // column-chunk partial sums
+    int* tickets;       // last-CTA counters
+    double2* small;     // per-system Hessenberg / rotations
+    GmState* st;
+};
+
+struct GmSmall {
+    double2 *hk1, *cs, *sn, *beta, *H, *y;
+};
+
+__host__ __device__ inline size_t gm_small_size(int m) {
+    return (size_t)(m + 1) + m + m + (m + 1) + (size_t)(m + 1) * m + (m + 1);
+}
+
+__device__ inline GmSmall gm_small(const GmBatch& bt, int s) {
+    double2* b = bt.small + (size_t)s * bt.small_stride;
+    GmSmall g;
+    int m = bt.m;
+    g.hk1 = b;
+    g.cs = g.hk1 + (m + 1);
+    g.sn = g.cs + m;
+    g.beta = g.sn + m;
+    g.H = g.beta + (m + 1);
+    g.y = g.H + (size_t)(m + 1) * m;
+    return g;
+}
+
+struct GmWorkspace {
+    GmBatch bt{};
+    DevBuf mem;
+    bool fp32 = false;
+    bool w_in_smem = false;
+    int rb = 0, cb = 0;
+    double* norm_part = nullptr;
+    double* anorm = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_chunk = 0;
+    int64_t launches_per_graph = 0;
+    ~GmWorkspace();
+};
+
+void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const void* A, int64_t lda,
+                size_t mat_stride, bool fp32, bool ref_dotc);
+void gm_matrix_norms(Context& ctx, GmWorkspace& ws);
+void gm_init(Context& ctx, GmWorkspace& ws, double tol, int64_t max_restarts);
+void gm_launch_iteration(Context& ctx, GmWorkspace& ws, cudaEvent_t ev_q0, cudaEvent_t ev_q1);
+void gm_read_states(Context& ctx, GmWorkspace& ws, std::vector<GmState>& out);
+void gm_run(Context& ctx, GmWorkspace& ws, int chunk, int64_t max_total_iterations);
+
+}  // namespace bem

@@ -1,0 +1,394 @@
+// Input layer: the JSON UserInput (input_data.rs:9-108, serde_json with
+// externally tagged enums), the VTK legacy ASCII reader in the reference
+// dialect (mesh_data.rs:96-175) and the frequency lists (preprocess.rs:155-167,
+// tools.rs:1-24).  Host C++; no JSON library is available, so a small
+// recursive-descent parser is included.
+#include <cctype>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <sstream>
+
+#include "common.cuh"
+
+namespace bem {
+namespace {
+
+struct JValue {
+    enum Kind { Null, Bool, Number, String, Array, Object } kind = Null;
+    bool b = false;
+    double num = 0;
+    bool is_integer = false;  // literal without fraction or exponent
+    bool negative = false;
+    std::string str;
+    std::vector<JValue> arr;
+    std::vector<std::pair<std::string, JValue>> obj;
+    const JValue* get(const std::string& k) const {
+        for (auto& kv : obj)
+            if (kv.first == k) return &kv.second;
+        return nullptr;
+    }
+};
+
+class JParser {
+  public:
+    explicit JParser(const std::string& s) : s_(s) {}
+    JValue parse() {
+        JValue v = value(0);
+        ws();
+        if (i_ != s_.size()) fail("trailing characters");
+        return v;
+    }
+
+  private:
+    const std::string& s_;
+    size_t i_ = 0;
+    [[noreturn]] void fail(const std::string& m) {
+        throw Error(BEM_ERR_BAD_INPUT, "JSON parse error at offset " + std::to_string(i_) + ": " + m);
+    }
+    void ws() {
+        while (i_ < s_.size() && std::isspace((unsigned char)s_[i_])) ++i_;
+    }
+    JValue value(int depth) {
+        if (depth > 64) fail("nesting too deep");
+        ws();
+        if (i_ >= s_.size()) fail("unexpected end");
+        char c = s_[i_];
+        JValue v;
+        if (c == '{') {
+            v.kind = JValue::Object;
+            ++i_;
+            ws();
+            if (i_ < s_.size() && s_[i_] == '}') { ++i_; return v; }
+            for (;;) {
+                ws();
+                if (i_ >= s_.size() || s_[i_] != '"') fail("expected key");
+                std::string k = string();
+                ws();
+                if (i_ >= s_.size() || s_[i_] != ':') fail("expected ':'");
+                ++i_;
+                JValue e = value(depth + 1);
+                v.obj.emplace_back(k, std::move(e));
+                ws();
+                if (i_ < s_.size() && s_[i_] == ',') { ++i_; continue; }
+                if (i_ < s_.size() && s_[i_] == '}') { ++i_; break; }
+                fail("expected ',' or '}'");
+            }
+        } else if (c == '[') {
+            v.kind = JValue::Array;
+            ++i_;
+            ws();
+            if (i_ < s_.size() && s_[i_] == ']') { ++i_; return v; }
+            for (;;) {
+                v.arr.push_back(value(depth + 1));
+                ws();
+                if (i_ < s_.size() && s_[i_] == ',') { ++i_; continue; }
+                if (i_ < s_.size() && s_[i_] == ']') { ++i_; break; }
+                fail("expected ',' or ']'");
+            }
+        } else if (c == '"') {
+            v.kind = JValue::String;
+            v.str = string();
+        } else if (s_.compare(i_, 4, "true") == 0) {
+            v.kind = JValue::Bool; v.b = true; i_ += 4;
+        } else if (s_.compare(i_, 5, "false") == 0) {
+            v.kind = JValue::Bool; v.b = false; i_ += 5;
+        } else if (s_.compare(i_, 4, "null") == 0) {
+            v.kind = JValue::Null; i_ += 4;
+        } else if (c == '-' || std::isdigit((unsigned char)c)) {
+            size_t st = i_;
+            if (s_[i_] == '-') { v.negative = true; ++i_; }
+            if (i_ >= s_.size() || !std::isdigit((unsigned char)s_[i_])) fail("bad number");
+            while (i_ < s_.size() && std::isdigit((unsigned char)s_[i_])) ++i_;
+            bool integer = true;
+            if (i_ < s_.size() && s_[i_] == '.') {
+                integer = false;
+                ++i_;
+                if (i_ >= s_.size() || !std::isdigit((unsigned char)s_[i_])) fail("bad number");
+                while (i_ < s_.size() && std::isdigit((unsigned char)s_[i_])) ++i_;
+            }
+            if (i_ < s_.size() && (s_[i_] == 'e' || s_[i_] == 'E')) {
+                integer = false;
+                ++i_;
+                if (i_ < s_.size() && (s_[i_] == '+' || s_[i_] == '-')) ++i_;
+                if (i_ >= s_.size() || !std::isdigit((unsigned char)s_[i_])) fail("bad number");
+                while (i_ < s_.size() && std::isdigit((unsigned char)s_[i_])) ++i_;
+            }
+            v.kind = JValue::Number;
+            v.is_integer = integer;
+            v.num = std::strtod(s_.c_str() + st, nullptr);
+        } else {
+            fail("unexpected character");
+        }
+        return v;
+    }
+    std::string string() {
+        ++i_;  // opening quote
+        std::string out;
+        while (i_ < s_.size() && s_[i_] != '"') {
+            char c = s_[i_++];
+            if (c == '\\') {
+                if (i_ >= s_.size()) fail("bad escape");
+                char e = s_[i_++];
+                switch (e) {
+                case '"': out += '"'; break;
+                case '\\': out += '\\'; break;
+                case '/': out += '/'; break;
+                case 'b': out += '\b'; break;
+                case 'f': out += '\f'; break;
+                case 'n': out += '\n'; break;
+                case 'r': out += '\r'; break;
+                case 't': out += '\t'; break;
+                case 'u': {
+                    if (i_ + 4 > s_.size()) fail("bad \\u escape");
+                    unsigned cp = (unsigned)std::strtoul(s_.substr(i_, 4).c_str(), nullptr, 16);
+                    i_ += 4;
+                    if (cp < 0x80) out += (char)cp;
+                    else if (cp < 0x800) { out += (char)(0xC0 | (cp >> 6)); out += (char)(0x80 | (cp & 0x3F)); }
+                    else { out += (char)(0xE0 | (cp >> 12)); out += (char)(0x80 | ((cp >> 6) & 0x3F)); out += (char)(0x80 | (cp & 0x3F)); }
+                    break;
+                }
+                default: fail("bad escape");
+                }
+            } else {
+                out += c;
+            }
+        }
+        if (i_ >= s_.size()) fail("unterminated string");
+        ++i_;
+        return out;
+    }
+};
+
+// serde_json typing rules: f64 accepts any number; usize only non-negative
+// integer literals.
+double as_f64(const JValue* v, const char* what) {
+    require(v != nullptr, std::string("missing field `") + what + "`");
+    require(v->kind == JValue::Number, std::string("invalid type for `") + what + "`, expected f64");
+    return v->num;
+}
+int64_t as_usize(const JValue* v, const char* what) {
+    require(v != nullptr, std::string("missing field `") + what + "`");
+    require(v->kind == JValue::Number && v->is_integer && !v->negative,
+            std::string("invalid type for `") + what + "`, expected usize");
+    return (int64_t)v->num;
+}
+const JValue& field(const JValue& o, const char* name) {
+    require(o.kind == JValue::Object, std::string("expected struct containing `") + name + "`");
+    const JValue* v = o.get(name);
+    require(v != nullptr, std::string("missing field `") + name + "`");
+    return *v;
+}
+void fixed_array(const JValue& a, double* out, size_t n, const char* what) {
+    require(a.kind == JValue::Array && a.arr.size() == n,
+            std::string("invalid length for `") + what + "`, expected an array of length " + std::to_string(n));
+    for (size_t i = 0; i < n; ++i) out[i] = as_f64(&a.arr[i], what);
+}
+
+// Externally tagged enum: unit variants are strings, struct variants are
+// single-key objects.
+std::pair<std::string, const JValue*> tagged(const JValue& v, const char* what) {
+    if (v.kind == JValue::String) return {v.str, nullptr};
+    require(v.kind == JValue::Object && v.obj.size() == 1,
+            std::string("invalid type for enum `") + what + "`");
+    return {v.obj[0].first, &v.obj[0].second};
+}
+
+int unit_variant(const JValue& v, const char* what, std::initializer_list<const char*> names) {
+    auto t = tagged(v, what);
+    int idx = 0;
+    for (const char* n : names) {
+        if (t.first == n) return idx;
+        ++idx;
+    }
+    throw Error(BEM_ERR_BAD_INPUT, std::string("unknown variant `") + t.first + "` for `" + what + "`");
+}
+
+}  // namespace
+
+UserInput parse_user_input(const std::string& text) {
+    JValue root = JParser(text).parse();
+    require(root.kind == JValue::Object, "input must be a JSON object");
+    UserInput u;
+    const JValue& mf = field(root, "mesh_file");
+    require(mf.kind == JValue::String, "invalid type for `mesh_file`, expected a string");
+    u.mesh_file = mf.str;
+    u.body_index = as_usize(&field(root, "body_index"), "body_index");
+    {   // FrequencyInput (input_data.rs:9-14)
+        auto t = tagged(field(root, "frequency"), "frequency");
+        require(t.second != nullptr, "frequency must be a struct variant");
+        if (t.first == "List") {
+            u.freq_kind = 0;
+            const JValue& vals = field(*t.second, "values");
+            require(vals.kind == JValue::Array, "invalid type for `values`");
+            for (auto& x : vals.arr) u.freq_values.push_back(as_f64(&x, "values"));
+        } else if (t.first == "LinearSpaced" || t.first == "LogSpaced") {
+            u.freq_kind = t.first == "LinearSpaced" ? 1 : 2;
+            u.freq_start = as_f64(t.second->get("start"), "start");
+            u.freq_end = as_f64(t.second->get("end"), "end");
+            u.freq_number = as_usize(t.second->get("number"), "number");
+        } else {
+            throw Error(BEM_ERR_BAD_INPUT, "unknown variant `" + t.first + "` for `frequency`");
+        }
+    }
+    u.sound_speed = as_f64(root.get("sound_speed"), "sound_speed");
+    u.mass_density = as_f64(root.get("mass_density"), "mass_density");
+    u.problem_type = unit_variant(field(root, "problem_type"), "problem_type", {"Interior", "Exterior"});
+    u.method_type = unit_variant(field(root, "method_type"), "method_type", {"Classical", "BurtonMiller"});
+    {   // Solver (input_data.rs:29-34) + additive optional H-matrix keys
+        auto t = tagged(field(root, "solver"), "solver");
+        require(t.second != nullptr && t.second->kind == JValue::Object, "solver must be a struct variant");
+        if (t.first == "Direct") {
+            u.solver = 0;
+        } else if (t.first == "Iterative" || t.first == "Hierarchical") {
+            u.solver = t.first == "Iterative" ? 1 : 2;
+            u.tolerance = as_f64(t.second->get("tolerance"), "tolerance");
+            u.max_iterations = as_usize(t.second->get("max_iterations"), "max_iterations");
+            if (const JValue* l = t.second->get("leaf_size")) u.hm_leaf = as_usize(l, "leaf_size");
+            if (const JValue* e = t.second->get("eta")) u.hm_eta = as_f64(e, "eta");
+            if (const JValue* a = t.second->get("aca_tolerance")) u.hm_aca_tol = as_f64(a, "aca_tolerance");
+        } else {
+            throw Error(BEM_ERR_BAD_INPUT, "unknown variant `" + t.first + "` for `solver`");
+        }
+    }
+    {   // IncidentWaveInput (input_data.rs:36-46)
+        auto t = tagged(field(root, "incident_wave"), "incident_wave");
+        require(t.second != nullptr, "incident_wave must be a struct variant");
+        if (t.first == "PlaneWave") {
+            u.incident_type = 0;
+            fixed_array(field(*t.second, "direction"), u.incident_vec, 3, "direction");
+        } else if (t.first == "SphericalWave") {
+            u.incident_type = 1;
+            fixed_array(field(*t.second, "origin"), u.incident_vec, 3, "origin");
+        } else {
+            throw Error(BEM_ERR_BAD_INPUT, "unknown variant `" + t.first + "` for `incident_wave`");
+        }
+        fixed_array(field(*t.second, "amplitude"), u.incident_amp, 2, "amplitude");
+    }
+    {   // SurfaceBoundaryCondition (input_data.rs:48-59)
+        const JValue& bc = field(root, "surface_bc");
+        u.bc_type = unit_variant(field(bc, "bc_type"), "bc_type", {"Pressure", "NormalVelocity", "Impedance"});
+        fixed_array(field(bc, "value"), u.bc_value, 2, "value");
+    }
+    {   // Output (input_data.rs:61-78)
+        const JValue& o = field(root, "output");
+        u.output_total = unit_variant(field(o, "o_type"), "o_type", {"Scattered", "Total"});
+        u.output_pressure = unit_variant(field(o, "field"), "field", {"VelocityPotential", "Pressure"});
+        const JValue& f = field(o, "file");
+        require(f.kind == JValue::String, "invalid type for `file`");
+        u.output_file = f.str;
+        const JValue& fps = field(o, "field_points");
+        require(fps.kind == JValue::Array, "invalid type for `field_points`");
+        for (auto& p : fps.arr) {
+            double xyz[3];
+            fixed_array(p, xyz, 3, "field_points");
+            u.field_points.insert(u.field_points.end(), xyz, xyz + 3);
+        }
+    }
+    return u;
+}
+
+// mesh_data.rs:96-175: line-oriented reader; POINTS rows carry 3 coordinates,
+// CELLS rows carry the body id then the node ids, CELL_TYPES one type per row.
+Mesh read_vtk(const std::string& path) {
+    std::ifstream f(path);
+    require(f.good(), "Mesh file not found at specified path: " + path);
+    Mesh m;
+    std::string line;
+    auto first_word = [](const std::string& l) {
+        std::istringstream is(l);
+        std::string w;
+        is >> w;
+        return w;
+    };
+    auto count_after = [&](const std::string& l) -> int64_t {
+        std::istringstream is(l);
+        std::string w;
+        long long n = -1;
+        is >> w >> n;
+        require(is && n >= 0, "VTK: bad block header: " + l);
+        return (int64_t)n;
+    };
+    while (std::getline(f, line)) {
+        std::string w = first_word(line);
+        if (w == "POINTS") {
+            int64_t n = count_after(line);
+            m.nodes.assign((size_t)(3 * n), 0.0);
+            for (int64_t i = 0; i < n; ++i) {
+                require((bool)std::getline(f, line), "VTK: unexpected end of POINTS");
+                const char* s = line.c_str();
+                char* e;
+                for (int c = 0; c < 3; ++c) {
+                    double v = std::strtod(s, &e);
+                    require(e != s, "VTK: bad point row: " + line);
+                    m.nodes[(size_t)(3 * i + c)] = v;
+                    s = e;
+                }
+            }
+        } else if (w == "CELLS") {
+            int64_t n = count_after(line);
+            m.body.assign((size_t)n, 0);
+            m.etype.assign((size_t)n, 0);
+            m.conn_off.assign((size_t)n + 1, 0);
+            m.conn.clear();
+            for (int64_t i = 0; i < n; ++i) {
+                require((bool)std::getline(f, line), "VTK: unexpected end of CELLS");
+                const char* s = line.c_str();
+                char* e;
+                long long b = std::strtoll(s, &e, 10);
+                require(e != s, "VTK: bad cell row: " + line);
+                m.body[(size_t)i] = b;
+                s = e;
+                for (;;) {
+                    long long v = std::strtoll(s, &e, 10);
+                    if (e == s) break;
+                    m.conn.push_back(v);
+                    s = e;
+                }
+                m.conn_off[(size_t)i + 1] = (int64_t)m.conn.size();
+            }
+        } else if (w == "CELL_TYPES") {
+            int64_t n = count_after(line);
+            require(n <= m.nelem(), "VTK: CELL_TYPES longer than CELLS");
+            for (int64_t i = 0; i < n; ++i) {
+                require((bool)std::getline(f, line), "VTK: unexpected end of CELL_TYPES");
+                m.etype[(size_t)i] = (int32_t)std::strtol(line.c_str(), nullptr, 10);
+            }
+        }
+    }
+    // bodies in order of first appearance (mesh_data.rs:163-171)
+    for (int64_t e = 0; e < m.nelem(); ++e) {
+        int64_t b = m.body[(size_t)e];
+        require(b >= 1, "VTK: body ids start at 1");
+        if (b > m.nbodies) {
+            require(b == m.nbodies + 1, "VTK: body ids must appear in increasing order without gaps");
+            m.nbodies++;
+        }
+    }
+    return m;
+}
+
+// tools.rs:1-24 linspace / logspace with exact endpoints.
+static std::vector<double> linspace(double start, double end, int64_t n) {
+    std::vector<double> x((size_t)n, start);
+    double dx = (end - start) / (double)(n - 1);
+    for (int64_t i = 1; i < n - 1; ++i) x[(size_t)i] = start + dx * (double)i;
+    x[(size_t)n - 1] = end;
+    return x;
+}
+
+std::vector<double> frequency_list(const UserInput& in) {
+    if (in.freq_kind == 0) return in.freq_values;
+    require(in.freq_number >= 1, "frequency: number must be at least 1");
+    if (in.freq_kind == 1) return linspace(in.freq_start, in.freq_end, in.freq_number);
+    std::vector<double> xl = linspace(std::log10(in.freq_start), std::log10(in.freq_end), in.freq_number);
+    std::vector<double> x((size_t)in.freq_number, in.freq_start);
+    x[(size_t)in.freq_number - 1] = in.freq_end;
+    for (int64_t i = 1; i < in.freq_number - 1; ++i) x[(size_t)i] = std::pow(10.0, xl[(size_t)i]);
+    return x;
+}
+
+}  // namespace bem

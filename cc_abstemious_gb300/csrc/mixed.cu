@@ -1,0 +1,215 @@
+// Mixed-precision batched form: every frequency of a body is assembled in one
+// single-precision pass (float-float geometry and phase, FP64 singular self
+// term), then all systems are solved together by the batched FP64 restarted
+// GMRES over the FP32 operators (compensated mat-vecs), and the field points
+// are evaluated in FP64.  The error against an FP64 LU of the same operator is
+// measured on request, outside any timed region.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+#include "complex.cuh"
+#include "gmres.cuh"
+#include "mixed.cuh"
+#include "precond.cuh"
+
+namespace bem {
+
+namespace {
+struct EventTimer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    Context& c;
+    bool on;
+    explicit EventTimer(Context& ctx) : c(ctx), on(ctx.profiling) {
+        if (on) {
+            BEM_CUDA(cudaEventCreate(&a));
+            BEM_CUDA(cudaEventCreate(&b));
+            BEM_CUDA(cudaEventRecord(a, c.stream));
+        }
+    }
+    void stop(const std::string& name, int64_t launches, double bytes) {
+        if (!on) return;
+        BEM_CUDA(cudaEventRecord(b, c.stream));
+        BEM_CUDA(cudaEventSynchronize(b));
+        float ms = 0;
+        BEM_CUDA(cudaEventElapsedTime(&ms, a, b));
+        c.stage_add(name, ms, launches, bytes);
+    }
+    ~EventTimer() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
+}  // namespace
+
+double lu_reference_error(Context& c, const Problem& p, const double* phi_host, const double* vn_host) {
+    int64_t n = p.n;
+    DevBuf b, A;
+    b.ensure(sizeof(double2) * 3 * n);
+    A.ensure(sizeof(double2) * (size_t)n * n);
+    double2* inc = b.as<double2>();
+    double2* phi = inc + n;
+    double2* vn = phi + n;
+    incident_surface(c, p, inc);
+    Problem q;  // same operator, solved with the direct FP64 LU
+    Problem& pp = const_cast<Problem&>(p);
+    int saved = pp.in.solver;
+    pp.in.solver = 0;
+    try {
+        solve_surface_dense_fp64(c, pp, inc, phi, vn, nullptr, A.as<double2>());
+    } catch (...) {
+        pp.in.solver = saved;
+        throw;
+    }
+    pp.in.solver = saved;
+    std::vector<double> ref(2 * n);
+    const double* mine = p.in.bc_type == 0 ? vn_host : phi_host;
+    BEM_CUDA(cudaMemcpyAsync(ref.data(), p.in.bc_type == 0 ? (void*)vn : (void*)phi, sizeof(double2) * n,
+                             cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    double num = 0, den = 0;
+    for (int64_t i = 0; i < 2 * n; ++i) {
+        double d = mine[i] - ref[i];
+        num += d * d;
+        den += ref[i] * ref[i];
+    }
+    (void)q;
+    return std::sqrt(num / den);
+}
+
+void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered, bem_cplx* incident,
+               bem_solve_report* reports, bool check_vs_lu) {
+    require(p.in.solver != 2 || true, "");
+    c.stages.clear();
+    const int64_t nf = (int64_t)p.freqs.size(), n = p.n, nfp = p.nfp;
+    require(nf >= 1, "no frequencies");
+    const int64_t ld = p.geo.npad;  // multiple of 64: aligned float4 loads
+    const size_t mstride = (size_t)ld * n;
+    const int64_t saved_ifreq = p.ifreq;
+    auto t_start = std::chrono::steady_clock::now();
+
+    // per-frequency factors (influence_matrix.rs:130-162)
+    std::vector<double> ks(nf);
+    std::vector<cd> al(nf), be(nf), ga(nf), de(nf);
+    for (int64_t f = 0; f < nf; ++f) {
+        p.ifreq = f;
+        ks[f] = p.wavenumber();
+        lhs_factors(p, al[f], be[f]);
+        rhs_factors(p, ga[f], de[f]);
+    }
+    const bool need_rowsum = !(p.in.bc_value[0] == 0.0 && p.in.bc_value[1] == 0.0) && p.in.bc_type != 2;
+
+    c.w_mat.ensure(sizeof(float2) * mstride * nf);
+    float2* A32 = c.w_mat.as<float2>();
+    c.w_vec.ensure(sizeof(double2) * (size_t)nf * (4 * n + 2 * nfp + 2));
+    double2* inc = c.w_vec.as<double2>();
+    double2* rowsum = inc + nf * n;
+    double2* phi = rowsum + nf * n;
+    double2* vn = phi + nf * n;
+    double2* finc = vn + nf * n;
+    double2* fps = finc + nf * nfp;
+
+    {
+        EventTimer t(c);
+        assemble_system_fp32_body(c, p, ks.data(), al.data(), be.data(), ga.data(), de.data(), (int)nf, A32, ld,
+                                  mstride, need_rowsum ? rowsum : nullptr, (size_t)n);
+        t.stop("assemble_fp32", (nf + 15) / 16, 8.0 * (double)n * n * nf);
+    }
+    {
+        EventTimer t(c);
+        for (int64_t f = 0; f < nf; ++f) {
+            p.ifreq = f;
+            incident_surface(c, p, inc + f * n);
+        }
+        t.stop("incident", nf, 0);
+    }
+
+    // solver parameters: the problem's GMRES settings, or for the direct
+    // solver a tight tolerance (the mixed form always iterates)
+    int64_t max_it = p.in.solver == 0 ? 1000 : p.in.max_iterations;
+    double tol = p.in.solver == 0 ? 1e-10 : p.in.tolerance;
+    if (max_it <= 0) max_it = 1000;
+    if (max_it > n) max_it = n;
+    if (tol <= 0) tol = 1e-5;
+    int m = (int)std::ceil(std::sqrt((double)max_it));
+    int64_t restarts = max_it / m;
+
+    GmWorkspace ws;
+    gm_prepare(c, ws, (int)nf, n, m, A32, ld, mstride, true, false);
+    const double s = p.in.bc_type == 0 ? 1.0 : -1.0;
+    for (int64_t f = 0; f < nf; ++f)
+        launch_rhs_combine(c, n, s, inc + f * n, {p.in.bc_value[0], p.in.bc_value[1]},
+                           need_rowsum ? rowsum + f * n : nullptr, ws.bt.B + f * n);
+    std::vector<GmState> st;
+    {
+        EventTimer t(c);
+        gm_matrix_norms(c, ws);
+        gm_init(c, ws, tol, restarts);
+        if (precond != BEM_PRECOND_NONE)
+            precond_setup(c, p, ws, precond, ks.data());
+        gm_run(c, ws, c.profiling ? 0 : 4, restarts * (int64_t)m + 1);
+        gm_read_states(c, ws, st);
+        int64_t mv = 0;
+        for (auto& x : st) mv += x.num_mv;
+        t.stop("gmres", mv, 8.0 * (double)n * n * mv);
+    }
+    {
+        EventTimer t(c);
+        for (int64_t f = 0; f < nf; ++f) {
+            p.ifreq = f;
+            unpack_solution(c, p, ws.bt.X + f * n, phi + f * n, vn + f * n);
+            incident_field(c, p, finc + f * nfp);
+            evaluate_field(c, p, phi + f * n, vn + f * n, p.in.output_total ? finc + f * nfp : nullptr,
+                           fps + f * nfp);
+        }
+        t.stop("field", nf, 0);
+    }
+    std::vector<double2> hs((size_t)(nf * nfp)), hi((size_t)(nf * nfp));
+    c.last_phi.assign((size_t)(2 * n * nf), 0.0);
+    c.last_vn.assign((size_t)(2 * n * nf), 0.0);
+    c.last_n = n;
+    c.last_nf = nf;
+    if (nfp) {
+        BEM_CUDA(cudaMemcpyAsync(hs.data(), fps, sizeof(double2) * nf * nfp, cudaMemcpyDeviceToHost, c.stream));
+        BEM_CUDA(cudaMemcpyAsync(hi.data(), finc, sizeof(double2) * nf * nfp, cudaMemcpyDeviceToHost, c.stream));
+    }
+    BEM_CUDA(cudaMemcpyAsync(c.last_phi.data(), phi, sizeof(double2) * nf * n, cudaMemcpyDeviceToHost, c.stream));
+    BEM_CUDA(cudaMemcpyAsync(c.last_vn.data(), vn, sizeof(double2) * nf * n, cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    for (int64_t f = 0; f < nf; ++f) {
+        p.ifreq = f;
+        double w = p.in.output_pressure ? p.omega() * p.in.mass_density : 0.0;
+        for (int64_t i = 0; i < nfp; ++i) {
+            double2 a = hs[(size_t)(f * nfp + i)], q = hi[(size_t)(f * nfp + i)];
+            if (p.in.output_pressure) {
+                a = make_double2(-a.y * w, a.x * w);
+                q = make_double2(-q.y * w, q.x * w);
+            }
+            if (scattered) { scattered[f * nfp + i].re = a.x; scattered[f * nfp + i].im = a.y; }
+            if (incident) { incident[f * nfp + i].re = q.x; incident[f * nfp + i].im = q.y; }
+        }
+        if (reports) {
+            bem_solve_report& r = reports[f];
+            r.num_mv = st[(size_t)f].num_mv;
+            r.restarts = st[(size_t)f].restarts + (st[(size_t)f].converged ? 1 : 0);
+            r.iterations = st[(size_t)f].iterations;
+            r.backward_error = st[(size_t)f].error;
+            r.flag = st[(size_t)f].converged ? 1 : 2;
+            r.precond = (int32_t)precond;
+            r.seconds = secs / (double)nf;
+            r.rel_err_vs_lu = -1;
+        }
+    }
+    if (check_vs_lu && reports) {
+        for (int64_t f = 0; f < nf; ++f) {
+            p.ifreq = f;
+            reports[f].rel_err_vs_lu =
+                lu_reference_error(c, p, c.last_phi.data() + 2 * n * f, c.last_vn.data() + 2 * n * f);
+        }
+    }
+    p.ifreq = saved_ifreq;
+}
+
+}  // namespace bem

@@ -1,0 +1,21 @@
+// Mixed-precision batched form and FP64-LU error reference.
+#pragma once
+#include "common.cuh"
+
+namespace bem {
+
+void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered, bem_cplx* incident,
+               bem_solve_report* reports, bool check_vs_lu);
+// ||x - x_LU64|| / ||x_LU64|| for the unknown solved at the problem's current
+// frequency (phi for velocity/impedance conditions, vn for pressure).
+double lu_reference_error(Context& c, const Problem& p, const double* phi_host, const double* vn_host);
+
+// shared helpers (api.cu)
+cd impedance_factor(const Problem& p);
+void unpack_solution(Context& c, const Problem& p, const double2* x, double2* phi, double2* vn);
+void launch_rhs_combine(Context& c, int64_t n, double s, const double2* inc, cd bc, const double2* rowsum,
+                        double2* out);
+void solve_surface_dense_fp64(Context& c, const Problem& p, const double2* d_rhs_inc, double2* d_phi,
+                              double2* d_vn, bem_solve_report* rep, double2* d_A_keep);
+
+}  // namespace bem

@@ -1,0 +1,219 @@
+/*
+ * bem.h -- C ABI of libbem_gb300.so, the GB300 (sm_103a) implementation of the
+ * cc_abstemious BEM hot path.
+ *
+ * The reference is a pure-Rust crate whose hot-path boundary is its module API
+ * (influence_matrix / solve / postprocess, driven by analysis.rs).  Every entry
+ * point below replaces one of those functions; the comment gives the reference
+ * file:line.  A Rust crate would bind these with `extern "C"` declarations
+ * (see INTEGRATION.md).
+ *
+ * Conventions
+ *  - Complex values are interleaved {re, im} doubles (bem_cplx), matching
+ *    num_complex::Complex<f64>.  Matrices are column-major with a leading
+ *    dimension, matching nalgebra DMatrix<Complex<f64>>.
+ *  - The caller owns every buffer.  `mem` says whether matrix/vector pointers
+ *    are host (BEM_MEM_HOST) or CUDA device (BEM_MEM_DEVICE) memory of the
+ *    context's device.
+ *  - Calls are synchronous: results are ready when the call returns.  One
+ *    context per host thread.
+ *  - Errors never abort: every call returns a bem_status and the context keeps
+ *    a message for bem_last_error().  The reference panics (unwrap) or logs
+ *    and continues instead.
+ */
+#ifndef BEM_GB300_H
+#define BEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BEM_API __attribute__((visibility("default")))
+
+typedef struct { double re, im; } bem_cplx;
+
+typedef enum {
+    BEM_OK = 0,
+    BEM_ERR_BAD_INPUT = 1,     /* malformed JSON/VTK, bad sizes or indices */
+    BEM_ERR_SINGULAR = 2,      /* zero pivot in an LU factorisation */
+    BEM_ERR_NOT_CONVERGED = 3, /* iterative solver ran out of iterations */
+    BEM_ERR_NAN = 4,           /* NaN produced (e.g. zero spherical-wave origin) */
+    BEM_ERR_OOM = 5,           /* device allocation failed */
+    BEM_ERR_CUDA = 6,          /* CUDA runtime error */
+    BEM_ERR_TIMEOUT = 7        /* a bounded device-side wait gave up */
+} bem_status;
+
+typedef enum { BEM_MEM_HOST = 0, BEM_MEM_DEVICE = 1 } bem_mem;
+
+/* influence_matrix.rs:164-167 EqnSide */
+typedef enum { BEM_SIDE_RHS = 0, BEM_SIDE_LHS = 1 } bem_side;
+
+/* Execution form of bem_run / bem_solve_for_surface.
+ *  PLAIN_FP64: drop-in form; every stage in FP64 following the reference
+ *              algorithms (LU, restarted GMRES, ACA H-matrix).
+ *  MIXED:      all frequencies batched; FP32 assembly with accurate phase
+ *              reduction, FP64 restarted GMRES over the FP32 operator with
+ *              compensated mat-vecs, optional preconditioner; each result
+ *              reports its error against an FP64 LU when requested. */
+typedef enum { BEM_FORM_PLAIN_FP64 = 0, BEM_FORM_MIXED = 1 } bem_form;
+
+typedef enum {
+    BEM_PRECOND_NONE = 0,
+    BEM_PRECOND_BLOCK_JACOBI = 1,
+    BEM_PRECOND_LEARNED = 2
+} bem_precond;
+
+typedef struct {
+    int64_t num_mv;         /* matrix-vector products (gmres.rs:66) */
+    int64_t restarts;       /* restart cycles started */
+    int64_t iterations;     /* Arnoldi steps */
+    double backward_error;  /* final ||r|| / (||A|| ||x|| + ||b||) */
+    double rel_err_vs_lu;   /* ||x - x_LU64|| / ||x_LU64||, -1 if not computed */
+    double seconds;         /* wall time of the call */
+    int32_t flag;           /* 0 error, 1 tolerance reached, 2 iterations exhausted, 3 direct */
+    int32_t precond;        /* bem_precond used */
+} bem_solve_report;
+
+typedef struct bem_ctx bem_ctx;
+typedef struct bem_problem bem_problem;
+typedef struct bem_hmatrix bem_hmatrix;
+
+/* Parsed UserInput (input_data.rs:80-92), for inspection. */
+typedef struct {
+    double sound_speed, mass_density;
+    int32_t problem_type;    /* 0 Interior, 1 Exterior */
+    int32_t method_type;     /* 0 Classical, 1 BurtonMiller */
+    int32_t solver;          /* 0 Direct, 1 Iterative, 2 Hierarchical */
+    int32_t incident_type;   /* 0 PlaneWave, 1 SphericalWave */
+    int32_t bc_type;         /* 0 Pressure, 1 NormalVelocity, 2 Impedance */
+    int32_t output_total;    /* OutputType::Total */
+    int32_t output_pressure; /* OutputField::Pressure */
+    int32_t body_index;
+    double tolerance;
+    int64_t max_iterations;
+    double incident_vec[3];
+    double incident_amp[2];
+    double bc_value[2];
+    int64_t hm_leaf;         /* additive extension keys, defaults 32 / 4.0 / 1e-4 */
+    double hm_eta;
+    double hm_aca_tol;
+    int64_t num_eqn;
+    int64_t num_field_points;
+    int64_t num_frequencies;
+    int64_t mesh_elements;
+    int64_t mesh_nodes;
+    int64_t mesh_bodies;
+} bem_problem_info;
+
+/* ---- context ---------------------------------------------------------- */
+BEM_API bem_status bem_ctx_create(int device, bem_ctx** out);
+BEM_API void bem_ctx_destroy(bem_ctx* ctx);
+BEM_API const char* bem_last_error(const bem_ctx* ctx);
+/* Number of kernels this context has launched (instrumentation). */
+BEM_API int64_t bem_ctx_kernel_launches(const bem_ctx* ctx);
+BEM_API const char* bem_version(void);
+/* Per-stage CUDA-event timing of bem_run (instrumentation; no reference
+ * counterpart).  Profiling runs the GMRES iteration by iteration so that every
+ * Krylov mat-vec launch is bracketed by events on the context's stream. */
+BEM_API bem_status bem_ctx_set_profiling(bem_ctx* ctx, int on);
+BEM_API int64_t bem_ctx_profile_count(const bem_ctx* ctx);
+BEM_API bem_status bem_ctx_profile_get(const bem_ctx* ctx, int64_t i, char* name, int64_t name_len,
+                                       double* ms, int64_t* launches, double* bytes);
+
+/* ---- input and preprocessing ------------------------------------------ */
+/* analysis.rs:50-53 input_from_string + preprocess.rs:104-124 preprocess.
+ * base_dir (may be NULL) resolves a relative mesh_file; the reference resolves
+ * it against the working directory. */
+BEM_API bem_status bem_problem_from_json(bem_ctx* ctx, const char* json, const char* base_dir,
+                                         bem_problem** out);
+/* analysis.rs:42-48 input_from_file (input_data.rs:94-103). */
+BEM_API bem_status bem_problem_from_file(bem_ctx* ctx, const char* path, bem_problem** out);
+BEM_API void bem_problem_destroy(bem_problem* p);
+BEM_API bem_status bem_problem_get_info(const bem_problem* p, bem_problem_info* out);
+/* preprocess.rs:155-167 frequency list (tools.rs:1-24). */
+BEM_API bem_status bem_problem_frequencies(const bem_problem* p, double* out);
+/* preprocess.rs:34 PreData::set_frequency_index */
+BEM_API bem_status bem_problem_set_frequency_index(bem_problem* p, int64_t index);
+/* Collocation points x y z nx ny nz area wt (n x 8, row-major), computed on the
+ * device by the collocation kernel: elements.rs:172-180 via
+ * preprocess.rs:126-153. */
+BEM_API bem_status bem_collocation(bem_ctx* ctx, const bem_problem* p, double* out);
+
+/* ---- influence matrices (influence_matrix.rs) ------------------------- */
+/* influence_matrix.rs:64-98 get_dense_surface_matrices -> (H, G), n x n. */
+BEM_API bem_status bem_get_dense_surface_matrices(bem_ctx* ctx, const bem_problem* p,
+                                                  bem_cplx* H, bem_cplx* G, int64_t ld, bem_mem mem);
+/* influence_matrix.rs:101-127 get_dense_field_matrices -> (M, L), nfp x n. */
+BEM_API bem_status bem_get_dense_field_matrices(bem_ctx* ctx, const bem_problem* p,
+                                                bem_cplx* M, bem_cplx* L, int64_t ld, bem_mem mem);
+/* influence_matrix.rs:170-193 get_surface_row_or_column: exactly one of ni, nj
+ * must be 1; out has max(ni, nj) entries.  Index arrays are host memory. */
+BEM_API bem_status bem_get_surface_row_or_column(bem_ctx* ctx, const bem_problem* p,
+                                                 const int64_t* I, int64_t ni,
+                                                 const int64_t* J, int64_t nj,
+                                                 bem_side side, bem_cplx* out);
+
+/* ---- incident wave (incident_wave.rs) --------------------------------- */
+/* incident_wave.rs:7-63 get_incident_surface (n entries, host memory). */
+BEM_API bem_status bem_get_incident_surface(bem_ctx* ctx, const bem_problem* p, bem_cplx* rhs_inc);
+/* incident_wave.rs:66-99 get_incident_field (nfp entries, host memory). */
+BEM_API bem_status bem_get_incident_field(bem_ctx* ctx, const bem_problem* p, bem_cplx* phi_inc_fp);
+
+/* ---- solvers (solve.rs, gmres.rs) ------------------------------------- */
+/* solve.rs:11-22 solve_for_surface (dense direct / iterative / hierarchical
+ * per the problem's solver), plain FP64 form.  Host vectors of length n. */
+BEM_API bem_status bem_solve_for_surface(bem_ctx* ctx, const bem_problem* p, const bem_cplx* rhs_inc,
+                                         bem_cplx* phi, bem_cplx* vn, bem_solve_report* report);
+/* solve.rs:166-171 solve_lu: x (length n) is overwritten by A^-1 x. */
+BEM_API bem_status bem_solve_lu(bem_ctx* ctx, int64_t n, const bem_cplx* A, int64_t lda,
+                                bem_cplx* x, bem_mem mem);
+/* gmres.rs:35-59 GMRES::solve on a dense matrix (zero initial guess). */
+BEM_API bem_status bem_gmres_solve(bem_ctx* ctx, int64_t n, const bem_cplx* A, int64_t lda,
+                                   int64_t max_it, double tol, bem_cplx* x,
+                                   bem_solve_report* report, bem_mem mem);
+/* solve.rs:173-185 get_field: out = [phi_inc if Total] - M phi + L vn. */
+BEM_API bem_status bem_get_field(bem_ctx* ctx, const bem_problem* p, const bem_cplx* M,
+                                 const bem_cplx* L, int64_t ld, const bem_cplx* phi,
+                                 const bem_cplx* vn, const bem_cplx* phi_inc_fp,
+                                 bem_cplx* out, bem_mem mem);
+/* Fused field evaluation: influence_matrix.rs:101-127 + solve.rs:173-185
+ * evaluated without storing M and L.  Host vectors. */
+BEM_API bem_status bem_evaluate_field(bem_ctx* ctx, const bem_problem* p, const bem_cplx* phi,
+                                      const bem_cplx* vn, const bem_cplx* phi_inc_fp, bem_cplx* out);
+/* postprocess.rs:83-87 convert_phi_to_pressure_vec: v *= i omega rho. */
+BEM_API bem_status bem_convert_to_pressure(const bem_problem* p, double frequency, bem_cplx* v, int64_t n);
+
+/* ---- driver (analysis.rs:57-118) --------------------------------------- */
+/* Runs every frequency of the problem.  scattered and incident are
+ * (num_frequencies x nfp) row-major host arrays (field point fastest) and
+ * receive the pressure (or velocity potential) as postprocess.rs:70-79
+ * leaves them.  reports: num_frequencies entries or NULL.  With
+ * check_vs_lu != 0 each report carries its error against an FP64 LU solve of
+ * the same operator (costly; outside any timed region). */
+BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* p, bem_form form, bem_precond precond,
+                           bem_cplx* scattered, bem_cplx* incident, bem_solve_report* reports,
+                           int check_vs_lu);
+/* Surface solutions of the last bem_run (n per frequency, frequency-major). */
+BEM_API bem_status bem_last_surface(bem_ctx* ctx, const bem_problem* p, bem_cplx* phi, bem_cplx* vn);
+
+/* ---- H-matrix (h_matrix.rs, aca.rs, cluster.rs, block.rs) -------------- */
+/* h_matrix.rs:127-148 HMatrix::new_from over the problem's collocation points
+ * for the given side (leaf, eta and ACA tolerance from the problem). */
+BEM_API bem_status bem_hmatrix_build(bem_ctx* ctx, const bem_problem* p, bem_side side, bem_hmatrix** out);
+BEM_API void bem_hmatrix_destroy(bem_hmatrix* h);
+/* h_matrix.rs:218-234 gemv: b = alpha H x + beta b (host vectors). */
+BEM_API bem_status bem_hmatrix_gemv(bem_ctx* ctx, const bem_hmatrix* h, bem_cplx alpha, const bem_cplx* x,
+                                    bem_cplx beta, bem_cplx* b);
+/* h_matrix.rs:150 get_norm (sum of leaf Frobenius norms / ACA estimates). */
+BEM_API double bem_hmatrix_norm(const bem_hmatrix* h);
+/* [0] admissible leaves, [1] inadmissible leaves, [2] stored entries, [3] sum of ranks */
+BEM_API bem_status bem_hmatrix_stats(const bem_hmatrix* h, int64_t* stats4);
+/* h_matrix.rs:236-246 to_full (n x n column-major, host). */
+BEM_API bem_status bem_hmatrix_to_full(bem_ctx* ctx, const bem_hmatrix* h, bem_cplx* A, int64_t lda);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
