@@ -1,0 +1,359 @@
+#!/usr/bin/env python
+"""Benchmark: solves/s of the cc_abstemious hot path on one GB300.
+
+Workload (rigid_sphere_bm): rigid sphere r = 1 m meshed as a cube-sphere of
+6144 bilinear quads, exterior Burton-Miller, unit plane wave along +z, 16
+frequencies with ka evenly spaced 1..10, GMRES restart 50 (max_iterations 2500)
+tolerance 1e-8, 100 field points on r = 5 m.  Synthetic, seeded geometry (no
+dataset).  One step = one pass of the whole hot path over the 16 frequencies:
+assembly, surface solve and field evaluation -> 16 solves.
+
+Arms:
+  default        the batched mixed-precision form (FP32 operators with float-float
+                 phase, FP64 GMRES), problem resident on the device; the plain FP64
+                 form is timed beside it ("plain_fp64"), and the error of every
+                 reported frequency against an FP64 LU of the same operator is
+                 measured after the timed region.
+  --impl reference  the CPU restatement of the reference algorithm (oracle/),
+                 host cores only, a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/s at ≤1e-6 rel err vs FP64 LU: learned+mixed vs plain FP64, 1 GB300"
+UNIT = "solves/s"
+WORKLOAD = "rigid_sphere_bm"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--lu-check", type=int, default=4,
+                    help="frequencies checked against an FP64 LU (evenly spread; 0 = all)")
+    ap.add_argument("--cpu-sample", type=int, default=1, help="frequencies solved by the CPU baseline")
+    ap.add_argument("--precond", default="none", choices=["none", "block_jacobi", "learned"])
+    ap.add_argument("--mesh-m", type=int, default=32, help="cube-sphere subdivisions (6 m^2 quads)")
+    ap.add_argument("--nfreq", type=int, default=16)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="one mixed run (for ncu launch lists)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_matrix():
+    """DRAM bytes per matrix-row-block pass of the FP32 batched mat-vec from the
+    committed ncu summary (profiles/), or None."""
+    p = os.path.join(ROOT, "profiles", "gm_apply_fp32_rigid_sphere_bm.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_matrix:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_reference(inp, nfreq_sample, threads):
+    """The oracle (C restatement of the reference algorithm) on `nfreq_sample`
+    frequencies of the workload; returns (solves/s, seconds, sample text)."""
+    from oracle import oracle as O
+    import numpy as np
+    freqs = inp["frequency"]["List"]["values"]
+    idx = np.linspace(0, len(freqs) - 1, nfreq_sample).round().astype(int)
+    sample = dict(inp, frequency={"List": {"values": [freqs[i] for i in idx]}})
+    P = O.Problem(sample)
+    t0 = time.perf_counter()
+    P.run(nthreads=threads)
+    dt = time.perf_counter() - t0
+    return nfreq_sample / dt, dt, "%d of the %d frequencies (ka %s), N=%d" % (
+        nfreq_sample, len(freqs), ",".join("%.2f" % (1.0 + 9.0 * i / max(len(freqs) - 1, 1)) for i in idx), P.n)
+
+
+def run_reference_arm(args, inp):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    threads = max((os.cpu_count() or 2) // 2, 2)  # preprocess.rs:12-17
+    vals = []
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        pass
+    t_total = 0.0
+    for _ in range(max(args.steps, 1)):
+        v, dt, sample = cpu_reference(inp, args.cpu_sample, threads)
+        vals.append(v)
+        t_total += dt
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 complex",
+            "data": "synthetic (seeded cube-sphere mesh)",
+            "config": {"workload": WORKLOAD, "n_unknowns": 6 * args.mesh_m ** 2, "frequencies": args.nfreq,
+                       "parallelism": "replicas only"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample + " per step; oracle/ C restatement of the reference "
+                                                "(reference Rust toolchain absent)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    from cc_abstemious_gb300 import workloads
+    workdir = tempfile.mkdtemp(prefix="bem_bench_")
+    inp = workloads.rigid_sphere_bm(workdir, m=args.mesh_m, nfreq=args.nfreq)
+    if args.impl == "reference":
+        run_reference_arm(args, inp)
+        return
+
+    import numpy as np
+    import torch
+    import cc_abstemious_gb300 as bem
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    text = json.dumps(inp)
+    ctx = bem.Context(local)
+    pd = bem.PreData.from_json(text, ctx=ctx)
+    nf = len(pd.frequencies)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    precond = {"none": 0, "block_jacobi": 1, "learned": 2}[args.precond]
+    sc = np.zeros((nf, pd.nfp), dtype=np.complex128)
+    inc = np.zeros((nf, pd.nfp), dtype=np.complex128)
+    reps = (bem.SolveReport * nf)()
+
+    def run_mixed(check=0):
+        ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_MIXED, precond, bem._ptr(sc), bem._ptr(inc), reps, check))
+
+    if args.profile_only:
+        run_mixed()
+        torch.cuda.synchronize()
+        return
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(args.warmup, 3)):
+        run_mixed()
+    iters = [r.iterations for r in reps]
+
+    # ---- timed region: device-resident problem, CUDA events on the library stream
+    launches0 = ctx.kernel_launches
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)  # sampler running before the timed region starts
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        run_mixed()
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    gpu_launches = ctx.kernel_launches - launches0
+    ms_all = ms
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_all = float(t.item())
+    value = world * nf * 1000.0 / ms_all
+
+    # ---- end to end through the public API: JSON text + mesh file on the host ->
+    # preprocessing on the device -> every frequency -> results in host memory
+    mesh_bytes = os.path.getsize(inp["mesh_file"])
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        a = bem.Analysis(ctx)
+        a.input_from_string(text)
+        a.run(form="mixed", precond=None if args.precond == "none" else args.precond)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_ms = e2e_s * 1000.0
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * nf * 1000.0 / e2e_ms
+    info = pd.info
+    h2d = 8 * 3 * info["mesh_nodes"] + 8 * 5 * pd.n + 8 * 3 * pd.nfp  # nodes, element table, field points
+    d2h = 16 * 2 * nf * pd.nfp + 16 * 2 * nf * pd.n + 8 * 9 * pd.n  # results, surface solution, collocation
+
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        return
+
+    # ---- plain FP64 drop-in form on the same workload (one step)
+    plain = None
+    if not args.no_plain:
+        reps_p = (bem.SolveReport * nf)()
+        ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_PLAIN_FP64, 0, bem._ptr(sc), bem._ptr(inc), reps_p, 0))
+        ep0, ep1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ep0.record(stream)
+        ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_PLAIN_FP64, 0, bem._ptr(sc), bem._ptr(inc), reps_p, 0))
+        ep1.record(stream)
+        ep1.synchronize()
+        pms = ep0.elapsed_time(ep1)
+        plain = {"value": nf * 1000.0 / pms, "unit": UNIT, "ms_per_step": pms,
+                 "iterations": [r.iterations for r in reps_p]}
+        sc_plain = sc.copy()
+
+    # ---- accuracy: mixed vs an FP64 LU of the same operator, sampled frequencies
+    run_mixed(check=0)
+    sc_mixed = sc.copy()
+    errs = {}
+    idx = list(range(nf)) if args.lu_check == 0 else sorted(set(
+        int(round(x)) for x in np.linspace(0, nf - 1, min(args.lu_check, nf))))
+    for i in idx:
+        one = dict(inp, frequency={"List": {"values": [inp["frequency"]["List"]["values"][i]]}})
+        p1 = bem.PreData.from_json(json.dumps(one), ctx=ctx)
+        r1 = (bem.SolveReport * 1)()
+        s1 = np.zeros((1, pd.nfp), dtype=np.complex128)
+        i1 = np.zeros((1, pd.nfp), dtype=np.complex128)
+        ctx.check(ctx.lib.bem_run(ctx.h, p1.h, bem.FORM_MIXED, precond, bem._ptr(s1), bem._ptr(i1), r1, 1))
+        errs["%.3f" % (1.0 + 9.0 * i / max(nf - 1, 1))] = r1[0].rel_err_vs_lu
+        del p1
+    field_err_vs_plain = None
+    if plain is not None:
+        field_err_vs_plain = float(np.max(np.abs(sc_mixed - sc_plain)) / np.max(np.abs(sc_plain)))
+
+    # ---- per-kernel timing pass (CUDA events around every Krylov mat-vec)
+    ctx.set_profiling(True)
+    run_mixed()
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    hbm_peak, peak_kind = measured_peaks()
+    mv = prof.get("gmres_matvec_fp32", {})
+    achieved = mv["bytes"] / (mv["ms"] * 1e-3) / 1e9 if mv.get("ms") else None
+    per_matrix = ncu_traffic_per_matrix()
+    matrices_per_launch = mv["bytes"] / (8.0 * pd.n * pd.n) / max(mv.get("launches", 1), 1) if mv else None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak if achieved else None,
+                "traffic": per_matrix * matrices_per_launch if (per_matrix and matrices_per_launch) else None,
+                "kernel": "gm_apply_kernel<float2> (batched FP32-operator mat-vec, compensated)",
+                "algorithmic_bytes_per_launch": mv["bytes"] / max(mv["launches"], 1) if mv else None,
+                "peak_kind": peak_kind + " (burst copy)"}
+
+    # ---- CPU baseline: the oracle on a bounded sample, host cores of this machine
+    threads = max((os.cpu_count() or 2) // 2, 2)
+    cv, cdt, sample = cpu_reference(inp, args.cpu_sample, threads)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_all, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 operator / fp64 vectors (complex)",
+        "data": "synthetic (cube-sphere mesh, no dataset)",
+        "config": {"workload": WORKLOAD, "n_unknowns": pd.n, "frequencies": nf, "ka": [1.0, 10.0],
+                   "solver": "GMRES restart 50 tol 1e-8", "field_points": pd.nfp,
+                   "form": "batched mixed (FP32 assembly + FP64 GMRES)",
+                   "precond": args.precond, "l2": "operators 8 B x N^2 x 16 = %.1f GB > L2 (no flush needed)"
+                   % (8.0 * pd.n * pd.n * nf / 1e9), "parallelism": "replicas only"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "mesh_file_bytes": mesh_bytes, "note": "JSON text + VTK file on host -> results on host"},
+        "gpu_launches": gpu_launches,
+        "roofline": roofline,
+        "cpu_baseline": {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample + "; oracle/ C restatement, reference thread count max(nproc/2,2)"},
+        "clocks": clk,
+        "plain_fp64": plain,
+        "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
+        "rel_err_vs_fp64_lu": errs,
+        "max_rel_err_vs_fp64_lu": max(errs.values()) if errs else None,
+        "field_rel_diff_vs_plain": field_err_vs_plain,
+        "gmres_iterations": iters,
+        "stages_ms": {k: v["ms"] for k, v in prof.items()},
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+if __name__ == "__main__":
+    main()

@@ -71,6 +71,11 @@ class Context:
     def kernel_launches(self):
         return self.lib.bem_ctx_kernel_launches(self.h)
 
+    @property
+    def stream(self):
+        """Raw cudaStream_t of the context (for torch.cuda.ExternalStream)."""
+        return self.lib.bem_ctx_stream(self.h)
+
     def set_profiling(self, on):
         self.check(self.lib.bem_ctx_set_profiling(self.h, 1 if on else 0))
 
@@ -179,6 +184,14 @@ def get_dense_surface_matrices(pd, out=None):
     H, G = _c(pd.n, pd.n), _c(pd.n, pd.n)
     ctx.check(ctx.lib.bem_get_dense_surface_matrices(ctx.h, pd.h, _ptr(H), _ptr(G), pd.n, MEM_HOST))
     return H, G
+
+
+def get_system_matrix_fp32(pd):
+    """The mixed form's single-precision alpha H + beta G at the current
+    frequency (n x n complex64, column-major)."""
+    A = np.zeros((pd.n, pd.n), dtype=np.complex64, order="F")
+    pd.ctx.check(pd.ctx.lib.bem_get_system_matrix_fp32(pd.ctx.h, pd.h, _ptr(A), pd.n))
+    return A
 
 
 def get_dense_field_matrices(pd):

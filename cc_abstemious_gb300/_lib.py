@@ -70,6 +70,7 @@ SIGNATURES = {
     "bem_get_dense_surface_matrices": (_i, [_vp, _vp, _vp, _vp, _i64, _i]),
     "bem_get_dense_field_matrices": (_i, [_vp, _vp, _vp, _vp, _i64, _i]),
     "bem_get_surface_row_or_column": (_i, [_vp, _vp, _vp, _i64, _vp, _i64, _i, _vp]),
+    "bem_get_system_matrix_fp32": (_i, [_vp, _vp, _vp, _i64]),
     "bem_get_incident_surface": (_i, [_vp, _vp, _vp]),
     "bem_get_incident_field": (_i, [_vp, _vp, _vp]),
     "bem_solve_for_surface": (_i, [_vp, _vp, _vp, _vp, _vp, C.POINTER(SolveReport)]),
@@ -87,6 +88,7 @@ SIGNATURES = {
     "bem_hmatrix_stats": (_i, [_vp, _vp]),
     "bem_hmatrix_to_full": (_i, [_vp, _vp, _vp, _i64]),
     "bem_ctx_set_profiling": (_i, [_vp, _i]),
+    "bem_ctx_stream": (_vp, [_vp]),
     "bem_ctx_profile_count": (_i64, [_vp]),
     "bem_ctx_profile_get": (_i, [_vp, _i64, C.c_char_p, _i64, C.POINTER(C.c_double), C.POINTER(C.c_int64),
                                  C.POINTER(C.c_double)]),

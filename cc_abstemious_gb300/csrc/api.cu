@@ -228,6 +228,8 @@ BEM_API bem_status bem_ctx_set_profiling(bem_ctx* ctx, int on) {
     return BEM_OK;
 }
 
+BEM_API void* bem_ctx_stream(const bem_ctx* ctx) { return ctx ? (void*)ctx->c.stream : nullptr; }
+
 BEM_API int64_t bem_ctx_profile_count(const bem_ctx* ctx) { return ctx ? (int64_t)ctx->c.stages.size() : 0; }
 
 BEM_API bem_status bem_ctx_profile_get(const bem_ctx* ctx, int64_t i, char* name, int64_t name_len, double* ms,
@@ -399,6 +401,29 @@ BEM_API bem_status bem_get_surface_row_or_column(bem_ctx* ctx, const bem_problem
         row_or_column(c, p, dI.as<int64_t>(), ni, dJ.as<int64_t>(), nj, side == BEM_SIDE_LHS ? 1 : 0,
                       dout.as<double2>(), diag);
         to_host(c, out, dout.p, sizeof(double2) * len);
+    });
+}
+
+BEM_API bem_status bem_get_system_matrix_fp32(bem_ctx* ctx, const bem_problem* pp, float* A, int64_t ld) {
+    if (!ctx || !pp || !A) return BEM_ERR_BAD_INPUT;
+    return guard(ctx, [&] {
+        Context& c = ctx->c;
+        const Problem& p = pp->p;
+        set_device(c);
+        require(ld >= p.n, "ld < n");
+        cd a, b, g, d;
+        lhs_factors(p, a, b);
+        rhs_factors(p, g, d);
+        double k = p.wavenumber();
+        const int64_t ldd = p.geo.npad;
+        DevBuf m, nrm;
+        m.ensure(sizeof(float2) * (size_t)ldd * p.n);
+        nrm.ensure(sizeof(double));
+        assemble_system_fp32_body(c, p, &k, &a, &b, &g, &d, 1, m.as<float2>(), ldd, (size_t)ldd * p.n, nullptr, 0,
+                                  nrm.as<double>());
+        BEM_CUDA(cudaMemcpy2DAsync(A, sizeof(float2) * ld, m.p, sizeof(float2) * ldd, sizeof(float2) * p.n, p.n,
+                                   cudaMemcpyDeviceToHost, c.stream));
+        c.sync();
     });
 }
 

@@ -10,12 +10,9 @@
 #include "common.cuh"
 #include "complex.cuh"
 #include "tma.cuh"
+#include "kernels.cuh"
 
 namespace bem {
-
-constexpr int TILE = 64;
-constexpr int ASM_THREADS = 256;
-constexpr double PI_D = 3.14159265358979323846;
 
 // influence_matrix.rs:12-37.  (x, e_x): source point and its normal; (y, e_y):
 // observation point and its normal.  Returns g and h without the wt*area scale.
@@ -45,19 +42,6 @@ __device__ __forceinline__ void greens64(double k, int bm, double beta_im, doubl
         g = cadd(g, make_double2(-beta_im * dg.y, beta_im * dg.x));
         h = cadd(h, make_double2(-beta_im * dh.y, beta_im * dh.x));
     }
-}
-
-// influence_matrix.rs:42-50: static flat-disc self term (k independent), scaled
-// by wt*area, plus the hdiag / gdiag diagonal of preprocess.rs:60-74.
-__device__ __forceinline__ void self_term64(double area, double wt, int bm, double beta_im, double hdiag,
-                                            double gdiag_im, z2& g, z2& h) {
-    double b = sqrt(area / PI_D);
-    double g0 = 1.0 / (2.0 * PI_D * b);
-    double h0im = bm ? beta_im * (-1.0 / (2.0 * PI_D * (b * b * b))) : 0.0;
-    g = make_double2(g0 * wt * area, 0.0);
-    h = make_double2(0.0, h0im * wt * area);
-    h.x += hdiag;
-    g.y += gdiag_im;
 }
 
 struct TileGeo64 {
@@ -159,12 +143,12 @@ __global__ void reduce_parts_kernel(int64_t n, int64_t npad, int ntiles, const d
     out[i] = s;
 }
 
-static int* device_err(Context& ctx) {
+int* device_err(Context& ctx) {
     ctx.w_flags.ensure(256);
     return ctx.w_flags.as<int>();
 }
 
-static void check_device_err(Context& ctx) {
+void check_device_err(Context& ctx) {
     int h = 0;
     BEM_CUDA(cudaMemcpyAsync(&h, ctx.w_flags.p, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
     ctx.sync();
@@ -172,6 +156,11 @@ static void check_device_err(Context& ctx) {
         BEM_CUDA(cudaMemsetAsync(ctx.w_flags.p, 0, sizeof(int), ctx.stream));
         throw Error(BEM_ERR_TIMEOUT, "a bounded device-side wait gave up (code " + std::to_string(h) + ")");
     }
+}
+
+void launch_reduce_parts(Context& ctx, int64_t n, int64_t npad, int ntiles, const double2* part, double2* out) {
+    reduce_parts_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx.stream>>>(n, npad, ntiles, part, out);
+    BEM_CHECK_LAUNCH(&ctx);
 }
 
 void assemble_surface_fp64(Context& ctx, const Problem& p, double2* H, double2* G, int64_t ld) {
@@ -310,245 +299,6 @@ void evaluate_field(Context& ctx, const Problem& p, const double2* phi, const do
     evaluate_field_kernel<<<(unsigned)p.nfp, FIELD_THREADS, 0, ctx.stream>>>(
         p.nfp, p.nfp_pad, p.d_fp.as<double>(), p.n, p.geo.npad, p.geo.arr(0), p.wavenumber(), phi, vn, inc, out);
     BEM_CHECK_LAUNCH(&ctx);
-}
-
-// ---------------------------------------------------------------------------
-// Mixed form: single-precision assembly of A_s = alpha_s H_s + beta_s G_s for
-// several frequencies s of one body in one pass.  Geometry-only terms are
-// evaluated once per pair; coordinates are float-float so the separation r is
-// accurate to ~1e-14 relative, and the phase k r is formed in float-float and
-// reduced modulo pi/2 (Cody-Waite with an exact FMA product) before a
-// single-precision sincos on |x| <= pi/4.  The singular self term is FP64.
-struct Sys32 {
-    float kh, kl;       // wavenumber hi + lo
-    float beta_im;      // 1/k (Burton-Miller) or 0
-    float k2;           // k^2
-    float2 alpha, beta; // LHS factors
-    float2 gamma, delta;// RHS factors
-    double kd, gdiag_im;
-};
-constexpr int MAX_SYS32 = 16;
-struct Asm32Params {
-    int nsys, bm;
-    double hdiag;
-    float P1, P2, P3, two_over_pi;
-    Sys32 s[MAX_SYS32];
-};
-
-struct TileGeo32 {
-    float cxh[TILE], cxl[TILE], cyh[TILE], cyl[TILE], czh[TILE], czl[TILE], cex[TILE], cey[TILE], cez[TILE], cwa[TILE];
-    float rxh[TILE], rxl[TILE], ryh[TILE], ryl[TILE], rzh[TILE], rzl[TILE], rex[TILE], rey[TILE], rez[TILE];
-};
-
-// a - b as float-float (hi, lo) given float-float inputs.
-__device__ __forceinline__ void ff_diff(float ah, float al, float bh, float bl, float& h, float& l) {
-    float s = ah - bh;
-    float bb = s - ah;
-    float e = (ah - (s - bb)) - (bh + bb);
-    h = s;
-    l = e + (al - bl);
-}
-
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = a + b;
-    float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
-template <int WITH_RHS>
-__global__ void __launch_bounds__(ASM_THREADS) assemble32_kernel(
-    int64_t n, int64_t npad, const float* __restrict__ g32, const double* __restrict__ geo, Asm32Params prm,
-    float2* __restrict__ A, int64_t ld, size_t mat_stride, double2* __restrict__ part, size_t part_stride,
-    int* __restrict__ err) {
-    __shared__ __align__(128) TileGeo32 t;
-    __shared__ __align__(8) uint64_t bar;
-    const int64_t I0 = (int64_t)blockIdx.y * TILE, J0 = (int64_t)blockIdx.x * TILE;
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    const uint32_t B = TILE * sizeof(float);
-    if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(&bar, 19 * B);
-        float* cdst[10] = {t.cxh, t.cxl, t.cyh, t.cyl, t.czh, t.czl, t.cex, t.cey, t.cez, t.cwa};
-        for (int a = 0; a < 10; ++a) bulk_g2s(cdst[a], g32 + a * npad + J0, B, &bar);
-        float* rdst[9] = {t.rxh, t.rxl, t.ryh, t.ryl, t.rzh, t.rzl, t.rex, t.rey, t.rez};
-        for (int a = 0; a < 9; ++a) bulk_g2s(rdst[a], g32 + a * npad + I0, B, &bar);
-    }
-    if (!mbar_wait_bounded(&bar, 0)) {
-        if (threadIdx.x == 0) atomicOr(err, DEVERR_MBAR_TIMEOUT);
-        mbar_wait_bounded(&bar, 0);
-        return;
-    }
-    const int tx = threadIdx.x & (TILE - 1), ty = threadIdx.x >> 6;
-    const int64_t i = I0 + tx;
-    const float yxh = t.rxh[tx], yxl = t.rxl[tx], yyh = t.ryh[tx], yyl = t.ryl[tx], yzh = t.rzh[tx],
-                yzl = t.rzl[tx];
-    const float eyx = t.rex[tx], eyy = t.rey[tx], eyz = t.rez[tx];
-    const float inv4pi = (float)(1.0 / (4.0 * PI_D));
-    float2 acc[MAX_SYS32];
-    if (WITH_RHS)
-        for (int s = 0; s < MAX_SYS32; ++s) acc[s] = make_float2(0.f, 0.f);
-#pragma unroll 1
-    for (int c = 0; c < TILE / 4; ++c) {
-        const int jj = ty + 4 * c;
-        const int64_t j = J0 + jj;
-        const bool store = i < n && j < n;
-        if (i == j) {
-            if (!store) continue;
-            double area = geo[GAREA * npad + j], wt = geo[GWT * npad + j];
-            for (int s = 0; s < prm.nsys; ++s) {
-                z2 g, h;
-                self_term64(area, wt, prm.bm, prm.bm ? 1.0 / prm.s[s].kd : 0.0, prm.hdiag, prm.s[s].gdiag_im, g, h);
-                z2 al = make_double2(prm.s[s].alpha.x, prm.s[s].alpha.y);
-                z2 be = make_double2(prm.s[s].beta.x, prm.s[s].beta.y);
-                z2 a = cmul(al, h);
-                cfma(a, be, g);
-                A[s * mat_stride + j * ld + i] = make_float2((float)a.x, (float)a.y);
-                if (WITH_RHS) {
-                    z2 ga = make_double2(prm.s[s].gamma.x, prm.s[s].gamma.y);
-                    z2 de = make_double2(prm.s[s].delta.x, prm.s[s].delta.y);
-                    z2 r = cmul(ga, h);
-                    cfma(r, de, g);
-                    acc[s].x += (float)r.x;
-                    acc[s].y += (float)r.y;
-                }
-            }
-            continue;
-        }
-        // separation in float-float
-        float dxh, dxl, dyh, dyl, dzh, dzl;
-        ff_diff(t.cxh[jj], t.cxl[jj], yxh, yxl, dxh, dxl);
-        ff_diff(t.cyh[jj], t.cyl[jj], yyh, yyl, dyh, dyl);
-        ff_diff(t.czh[jj], t.czl[jj], yzh, yzl, dzh, dzl);
-        float px = dxh * dxh, py = dyh * dyh, pz = dzh * dzh;
-        float ex = fmaf(dxh, dxh, -px), ey = fmaf(dyh, dyh, -py), ez = fmaf(dzh, dzh, -pz);
-        float s1, e1, s2, e2;
-        two_sum(px, py, s1, e1);
-        two_sum(s1, pz, s2, e2);
-        float r2l = (e1 + e2) + (ex + ey + ez) + 2.0f * (dxh * dxl + dyh * dyl + dzh * dzl);
-        float r2h = s2;
-        float rh = sqrtf(r2h);
-        float inv = 1.0f / rh;
-        float rl = (fmaf(-rh, rh, r2h) + r2l) * (0.5f * inv);
-        float erx = dxh * inv, ery = dyh * inv, erz = dzh * inv;
-        float rdoty = erx * eyx + ery * eyy + erz * eyz;
-        float rdotx = erx * t.cex[jj] + ery * t.cey[jj] + erz * t.cez[jj];
-        float nxy = eyx * t.cex[jj] + eyy * t.cey[jj] + eyz * t.cez[jj];
-        float q = inv * inv4pi * t.cwa[jj];
-        for (int s = 0; s < prm.nsys; ++s) {
-            const Sys32& S = prm.s[s];
-            // phase = k r in float-float, reduced modulo pi/2
-            float p = S.kh * rh;
-            float pe = fmaf(S.kh, rh, -p) + (S.kh * rl + S.kl * rh);
-            float nq = rintf(p * prm.two_over_pi);
-            float tt = nq * prm.P2;
-            float te = fmaf(nq, prm.P2, -tt);
-            float red = ((fmaf(-nq, prm.P1, p) - tt) + ((pe - te) - nq * prm.P3));
-            float sn, cs;
-            sincosf(red, &sn, &cs);
-            int quad = ((int)nq) & 3;
-            float c0 = cs, s0 = sn;
-            if (quad == 1) { c0 = -sn; s0 = cs; }
-            else if (quad == 2) { c0 = -cs; s0 = -sn; }
-            else if (quad == 3) { c0 = sn; s0 = -cs; }
-            float2 g = make_float2(c0 * q, s0 * q);   // g * wt * area
-            float2 f1 = make_float2(-inv, S.kh);
-            float2 gf1 = fmul(g, f1);
-            float2 h = fscale(gf1, -rdoty);
-            if (prm.bm) {
-                float2 dg = fscale(gf1, rdotx);
-                float2 t1 = make_float2(inv * nxy, -S.kh * nxy);  // (-f1) * nxy
-                float2 t2 = fscale(make_float2(S.k2 * rh + 3.0f * f1.x, 3.0f * f1.y), rdotx * rdoty);
-                float2 dh = fmul(fscale(g, inv), make_float2(t1.x - t2.x, t1.y - t2.y));
-                g = make_float2(g.x - S.beta_im * dg.y, g.y + S.beta_im * dg.x);
-                h = make_float2(h.x - S.beta_im * dh.y, h.y + S.beta_im * dh.x);
-            }
-            if (store) {
-                float2 a = fmul(S.alpha, h);
-                float2 b2 = fmul(S.beta, g);
-                A[s * mat_stride + j * ld + i] = make_float2(a.x + b2.x, a.y + b2.y);
-                if (WITH_RHS) {
-                    float2 r1 = fmul(S.gamma, h), r2 = fmul(S.delta, g);
-                    acc[s].x += r1.x + r2.x;
-                    acc[s].y += r1.y + r2.y;
-                }
-            }
-        }
-    }
-    if (WITH_RHS) {
-        __shared__ float2 red[ASM_THREADS];
-        for (int s = 0; s < prm.nsys; ++s) {
-            __syncthreads();
-            red[threadIdx.x] = acc[s];
-            __syncthreads();
-            if (ty == 0 && i < n) {
-                double sx = 0, sy = 0;
-                for (int q2 = 0; q2 < 4; ++q2) {
-                    sx += red[tx + TILE * q2].x;
-                    sy += red[tx + TILE * q2].y;
-                }
-                part[s * part_stride + (int64_t)blockIdx.x * npad + i] = make_double2(sx, sy);
-            }
-        }
-    }
-}
-
-void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks, const cd* alphas, const cd* betas,
-                               const cd* gammas, const cd* deltas, int nsys, float2* A, int64_t ld,
-                               size_t mat_stride, double2* rowsum, size_t vec_stride) {
-    int* err = device_err(ctx);
-    BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx.stream));
-    const float P1 = 1.5703125f;
-    const double rem1 = PI_D / 2 - (double)P1;
-    const float P2 = (float)rem1;
-    const float P3 = (float)(rem1 - (double)P2);
-    int ntiles = (int)(p.geo.npad / TILE);
-    for (int s0 = 0; s0 < nsys; s0 += MAX_SYS32) {
-        Asm32Params prm;
-        prm.nsys = std::min(MAX_SYS32, nsys - s0);
-        prm.bm = p.in.method_type == 1;
-        prm.hdiag = p.in.problem_type == 1 ? -0.5 : 0.0;
-        prm.P1 = P1;
-        prm.P2 = P2;
-        prm.P3 = P3;
-        prm.two_over_pi = (float)(2.0 / PI_D);
-        for (int s = 0; s < prm.nsys; ++s) {
-            double k = ks[s0 + s];
-            Sys32& S = prm.s[s];
-            S.kh = (float)k;
-            S.kl = (float)(k - (double)S.kh);
-            S.kd = k;
-            S.k2 = (float)(k * k);
-            S.beta_im = prm.bm ? (float)(1.0 / k) : 0.f;
-            S.gdiag_im = prm.bm ? 0.5 * (1.0 / k) : 0.0;
-            S.alpha = make_float2((float)alphas[s0 + s].re, (float)alphas[s0 + s].im);
-            S.beta = make_float2((float)betas[s0 + s].re, (float)betas[s0 + s].im);
-            S.gamma = make_float2((float)gammas[s0 + s].re, (float)gammas[s0 + s].im);
-            S.delta = make_float2((float)deltas[s0 + s].re, (float)deltas[s0 + s].im);
-        }
-        dim3 grid((unsigned)ntiles, (unsigned)ntiles);
-        float2* As = A + (size_t)s0 * mat_stride;
-        if (rowsum) {
-            size_t pstride = (size_t)ntiles * p.geo.npad;
-            ctx.w_part.ensure(sizeof(double2) * pstride * prm.nsys);
-            double2* part = ctx.w_part.as<double2>();
-            assemble32_kernel<1><<<grid, ASM_THREADS, 0, ctx.stream>>>(p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0),
-                                                                       prm, As, ld, mat_stride, part, pstride, err);
-            BEM_CHECK_LAUNCH(&ctx);
-            for (int s = 0; s < prm.nsys; ++s) {
-                reduce_parts_kernel<<<(unsigned)((p.n + 255) / 256), 256, 0, ctx.stream>>>(
-                    p.n, p.geo.npad, ntiles, part + s * pstride, rowsum + (size_t)(s0 + s) * vec_stride);
-                BEM_CHECK_LAUNCH(&ctx);
-            }
-        } else {
-            assemble32_kernel<0><<<grid, ASM_THREADS, 0, ctx.stream>>>(
-                p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0), prm, As, ld, mat_stride, nullptr, 0, err);
-            BEM_CHECK_LAUNCH(&ctx);
-        }
-    }
-    check_device_err(ctx);
 }
 
 }  // namespace bem

@@ -1,0 +1,429 @@
+// Mixed form, single-precision assembly and field evaluation.
+//
+// A_s = alpha_s H_s + beta_s G_s is assembled for several frequencies s of one
+// body in one pass: the geometry-only terms of a pair (separation, direction
+// cosines) are evaluated once and reused for every frequency.  Coordinates are
+// float-float (hi + lo) so the separation r is accurate to ~1e-14 relative;
+// the phase k r is formed in float-float and reduced modulo pi/2 (Cody-Waite
+// with an exact FMA product), and sin/cos on |x| <= pi/4 use Taylor
+// polynomials (truncation < 2e-9).  The singular self term stays FP64.  The
+// same kernel accumulates the squared Frobenius norm of every A_s (needed by
+// the GMRES stopping test) so the operators are never re-read for it.
+#include "common.cuh"
+#include "complex.cuh"
+#include "kernels.cuh"
+#include "tma.cuh"
+
+namespace bem {
+
+struct Sys32 {
+    float kh, kl;        // wavenumber hi + lo
+    float beta_im;       // 1/k (Burton-Miller) or 0
+    float k2;            // k^2
+    float2 alpha, beta;  // LHS factors
+    float2 gamma, delta; // RHS factors
+    double kd, gdiag_im;
+};
+constexpr int MAX_SYS32 = 16;
+struct Asm32Params {
+    int nsys, bm;
+    double hdiag;
+    float P1, P2, P3, two_over_pi;
+    Sys32 s[MAX_SYS32];
+};
+
+struct TileGeo32 {
+    float cxh[TILE], cxl[TILE], cyh[TILE], cyl[TILE], czh[TILE], czl[TILE], cex[TILE], cey[TILE], cez[TILE], cwa[TILE];
+    float rxh[TILE], rxl[TILE], ryh[TILE], ryl[TILE], rzh[TILE], rzl[TILE], rex[TILE], rey[TILE], rez[TILE];
+};
+
+// a - b as float-float (hi, lo) given float-float inputs.
+__device__ __forceinline__ void ff_diff(float ah, float al, float bh, float bl, float& h, float& l) {
+    float s = ah - bh;
+    float bb = s - ah;
+    float e = (ah - (s - bb)) - (bh + bb);
+    h = s;
+    l = e + (al - bl);
+}
+
+__device__ __forceinline__ void two_sum32(float a, float b, float& s, float& e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// sin and cos on |x| <= pi/4 + eps from their Taylor series (terms through
+// x^9 and x^10), Horner form.
+__device__ __forceinline__ void poly_sincos(float x, float& s, float& c) {
+    const float x2 = x * x;
+    float ps = fmaf(x2, 2.75573192e-6f, -1.98412698e-4f);   // 1/9!, -1/7!
+    ps = fmaf(x2, ps, 8.33333333e-3f);                       // 1/5!
+    ps = fmaf(x2, ps, -1.66666667e-1f);                      // -1/3!
+    s = fmaf(x * x2, ps, x);
+    float pc = fmaf(x2, -2.75573192e-7f, 2.48015873e-5f);   // -1/10!, 1/8!
+    pc = fmaf(x2, pc, -1.38888889e-3f);                      // -1/6!
+    pc = fmaf(x2, pc, 4.16666667e-2f);                       // 1/4!
+    pc = fmaf(x2, pc, -0.5f);                                // -1/2!
+    c = fmaf(x2, pc, 1.0f);
+}
+
+// e^{i k r} with k = kh + kl and r = rh + rl (float-float).
+__device__ __forceinline__ void phase32(float kh, float kl, float rh, float rl, const Asm32Params& prm, float& c0,
+                                        float& s0) {
+    float p = kh * rh;
+    float pe = fmaf(kh, rh, -p) + (kh * rl + kl * rh);
+    float nq = rintf(p * prm.two_over_pi);
+    float tt = nq * prm.P2;
+    float te = fmaf(nq, prm.P2, -tt);
+    float red = ((fmaf(-nq, prm.P1, p) - tt) + ((pe - te) - nq * prm.P3));
+    float sn, cs;
+    poly_sincos(red, sn, cs);
+    int quad = ((int)nq) & 3;
+    c0 = cs;
+    s0 = sn;
+    if (quad == 1) { c0 = -sn; s0 = cs; }
+    else if (quad == 2) { c0 = -cs; s0 = -sn; }
+    else if (quad == 3) { c0 = sn; s0 = -cs; }
+}
+
+// r = |a - b| for float-float points: returns (d_hi components, r hi/lo, 1/r).
+struct Sep32 {
+    float dx, dy, dz, rh, rl, inv;
+};
+__device__ __forceinline__ Sep32 separation32(float axh, float axl, float ayh, float ayl, float azh, float azl,
+                                              float bxh, float bxl, float byh, float byl, float bzh, float bzl) {
+    float dxh, dxl, dyh, dyl, dzh, dzl;
+    ff_diff(axh, axl, bxh, bxl, dxh, dxl);
+    ff_diff(ayh, ayl, byh, byl, dyh, dyl);
+    ff_diff(azh, azl, bzh, bzl, dzh, dzl);
+    float px = dxh * dxh, py = dyh * dyh, pz = dzh * dzh;
+    float ex = fmaf(dxh, dxh, -px), ey = fmaf(dyh, dyh, -py), ez = fmaf(dzh, dzh, -pz);
+    float s1, e1, s2, e2;
+    two_sum32(px, py, s1, e1);
+    two_sum32(s1, pz, s2, e2);
+    float r2l = (e1 + e2) + (ex + ey + ez) + 2.0f * (dxh * dxl + dyh * dyl + dzh * dzl);
+    Sep32 o;
+    o.rh = sqrtf(s2);
+    o.inv = 1.0f / o.rh;
+    o.rl = (fmaf(-o.rh, o.rh, s2) + r2l) * (0.5f * o.inv);
+    o.dx = dxh;
+    o.dy = dyh;
+    o.dz = dzh;
+    return o;
+}
+
+template <int WITH_RHS>
+__global__ void __launch_bounds__(ASM_THREADS) assemble32_kernel(
+    int64_t n, int64_t npad, const float* __restrict__ g32, const double* __restrict__ geo, Asm32Params prm,
+    float2* __restrict__ A, int64_t ld, size_t mat_stride, double2* __restrict__ part, size_t part_stride,
+    double* __restrict__ norm_part, int* __restrict__ err) {
+    __shared__ __align__(128) TileGeo32 t;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ float red[ASM_THREADS / 32][MAX_SYS32];
+    const int64_t I0 = (int64_t)blockIdx.y * TILE, J0 = (int64_t)blockIdx.x * TILE;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const uint32_t B = TILE * sizeof(float);
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&bar, 19 * B);
+        float* cdst[10] = {t.cxh, t.cxl, t.cyh, t.cyl, t.czh, t.czl, t.cex, t.cey, t.cez, t.cwa};
+        for (int a = 0; a < 10; ++a) bulk_g2s(cdst[a], g32 + a * npad + J0, B, &bar);
+        float* rdst[9] = {t.rxh, t.rxl, t.ryh, t.ryl, t.rzh, t.rzl, t.rex, t.rey, t.rez};
+        for (int a = 0; a < 9; ++a) bulk_g2s(rdst[a], g32 + a * npad + I0, B, &bar);
+    }
+    if (!mbar_wait_bounded(&bar, 0)) {
+        if (threadIdx.x == 0) atomicOr(err, DEVERR_MBAR_TIMEOUT);
+        mbar_wait_bounded(&bar, 0);
+        return;
+    }
+    const int tx = threadIdx.x & (TILE - 1), ty = threadIdx.x >> 6;
+    const int64_t i = I0 + tx;
+    const float yxh = t.rxh[tx], yxl = t.rxl[tx], yyh = t.ryh[tx], yyl = t.ryl[tx], yzh = t.rzh[tx],
+                yzl = t.rzl[tx];
+    const float eyx = t.rex[tx], eyy = t.rey[tx], eyz = t.rez[tx];
+    const float inv4pi = (float)(1.0 / (4.0 * PI_D));
+    float nrm[MAX_SYS32];
+    float2 acc[MAX_SYS32];
+#pragma unroll
+    for (int s = 0; s < MAX_SYS32; ++s) {
+        nrm[s] = 0.f;
+        acc[s] = make_float2(0.f, 0.f);
+    }
+#pragma unroll 1
+    for (int c = 0; c < TILE / 4; ++c) {
+        const int jj = ty + 4 * c;
+        const int64_t j = J0 + jj;
+        const bool store = i < n && j < n;
+        if (i == j) {
+            if (!store) continue;
+            double area = geo[GAREA * npad + j], wt = geo[GWT * npad + j];
+#pragma unroll
+            for (int s = 0; s < MAX_SYS32; ++s) {
+                if (s >= prm.nsys) break;
+                z2 g, h;
+                self_term64(area, wt, prm.bm, prm.bm ? 1.0 / prm.s[s].kd : 0.0, prm.hdiag, prm.s[s].gdiag_im, g, h);
+                z2 al = make_double2(prm.s[s].alpha.x, prm.s[s].alpha.y);
+                z2 be = make_double2(prm.s[s].beta.x, prm.s[s].beta.y);
+                z2 a = cmul(al, h);
+                cfma(a, be, g);
+                float2 af = make_float2((float)a.x, (float)a.y);
+                A[s * mat_stride + j * ld + i] = af;
+                nrm[s] += af.x * af.x + af.y * af.y;
+                if (WITH_RHS) {
+                    z2 ga = make_double2(prm.s[s].gamma.x, prm.s[s].gamma.y);
+                    z2 de = make_double2(prm.s[s].delta.x, prm.s[s].delta.y);
+                    z2 r = cmul(ga, h);
+                    cfma(r, de, g);
+                    acc[s].x += (float)r.x;
+                    acc[s].y += (float)r.y;
+                }
+            }
+            continue;
+        }
+        const Sep32 sp = separation32(t.cxh[jj], t.cxl[jj], t.cyh[jj], t.cyl[jj], t.czh[jj], t.czl[jj], yxh, yxl, yyh,
+                                      yyl, yzh, yzl);
+        const float inv = sp.inv;
+        const float erx = sp.dx * inv, ery = sp.dy * inv, erz = sp.dz * inv;
+        const float rdoty = erx * eyx + ery * eyy + erz * eyz;
+        const float rdotx = erx * t.cex[jj] + ery * t.cey[jj] + erz * t.cez[jj];
+        const float nxy = eyx * t.cex[jj] + eyy * t.cey[jj] + eyz * t.cez[jj];
+        const float q = inv * inv4pi * t.cwa[jj];
+#pragma unroll
+        for (int s = 0; s < MAX_SYS32; ++s) {
+            if (s >= prm.nsys) break;
+            const Sys32& S = prm.s[s];
+            float c0, s0;
+            phase32(S.kh, S.kl, sp.rh, sp.rl, prm, c0, s0);
+            float2 g = make_float2(c0 * q, s0 * q);  // g * wt * area
+            float2 f1 = make_float2(-inv, S.kh);
+            float2 gf1 = fmul(g, f1);
+            float2 h = fscale(gf1, -rdoty);
+            if (prm.bm) {
+                float2 dg = fscale(gf1, rdotx);
+                float2 t1 = make_float2(inv * nxy, -S.kh * nxy);  // (-f1) * nxy
+                float2 t2 = fscale(make_float2(S.k2 * sp.rh + 3.0f * f1.x, 3.0f * f1.y), rdotx * rdoty);
+                float2 dh = fmul(fscale(g, inv), make_float2(t1.x - t2.x, t1.y - t2.y));
+                g = make_float2(g.x - S.beta_im * dg.y, g.y + S.beta_im * dg.x);
+                h = make_float2(h.x - S.beta_im * dh.y, h.y + S.beta_im * dh.x);
+            }
+            if (store) {
+                float2 a = fmul(S.alpha, h);
+                float2 b2 = fmul(S.beta, g);
+                float2 af = make_float2(a.x + b2.x, a.y + b2.y);
+                A[s * mat_stride + j * ld + i] = af;
+                nrm[s] += af.x * af.x + af.y * af.y;
+                if (WITH_RHS) {
+                    float2 r1 = fmul(S.gamma, h), r2 = fmul(S.delta, g);
+                    acc[s].x += r1.x + r2.x;
+                    acc[s].y += r1.y + r2.y;
+                }
+            }
+        }
+    }
+    // squared Frobenius norms: warp shuffle, then one partial per CTA
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int s = 0; s < MAX_SYS32; ++s) {
+        if (s >= prm.nsys) break;
+        float v = nrm[s];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][s] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < prm.nsys) {
+        double sum = 0;
+        for (int w = 0; w < ASM_THREADS / 32; ++w) sum += red[w][threadIdx.x];
+        norm_part[(size_t)threadIdx.x * gridDim.x * gridDim.y + (size_t)blockIdx.y * gridDim.x + blockIdx.x] = sum;
+    }
+    if (WITH_RHS) {
+        __shared__ float2 rred[ASM_THREADS];
+#pragma unroll
+        for (int s = 0; s < MAX_SYS32; ++s) {
+            if (s >= prm.nsys) break;
+            __syncthreads();
+            rred[threadIdx.x] = acc[s];
+            __syncthreads();
+            if (ty == 0 && i < n) {
+                double sx = 0, sy = 0;
+                for (int q2 = 0; q2 < 4; ++q2) {
+                    sx += rred[tx + TILE * q2].x;
+                    sy += rred[tx + TILE * q2].y;
+                }
+                part[s * part_stride + (int64_t)blockIdx.x * npad + i] = make_double2(sx, sy);
+            }
+        }
+    }
+}
+
+__global__ void finish_norm_kernel(const double* __restrict__ part, int64_t nparts, double* __restrict__ out) {
+    __shared__ double sh[256];
+    const int s = blockIdx.x;
+    double v = 0;
+    for (int64_t t = threadIdx.x; t < nparts; t += blockDim.x) v += part[(size_t)s * nparts + t];
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[s] = sqrt(sh[0]);
+}
+
+void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks, const cd* alphas, const cd* betas,
+                               const cd* gammas, const cd* deltas, int nsys, float2* A, int64_t ld, size_t mat_stride,
+                               double2* rowsum, size_t vec_stride, double* norms) {
+    int* err = device_err(ctx);
+    BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx.stream));
+    const float P1 = 1.5703125f;  // 201/128: n * P1 exact for n < 2^16
+    const double rem1 = PI_D / 2 - (double)P1;
+    const float P2 = (float)rem1;
+    const float P3 = (float)(rem1 - (double)P2);
+    const int ntiles = (int)(p.geo.npad / TILE);
+    const int64_t nparts = (int64_t)ntiles * ntiles;
+    DevBuf& nbuf = ctx.w_norm;
+    nbuf.ensure(sizeof(double) * (size_t)nparts * MAX_SYS32);
+    for (int s0 = 0; s0 < nsys; s0 += MAX_SYS32) {
+        Asm32Params prm;
+        prm.nsys = std::min(MAX_SYS32, nsys - s0);
+        prm.bm = p.in.method_type == 1;
+        prm.hdiag = p.in.problem_type == 1 ? -0.5 : 0.0;
+        prm.P1 = P1;
+        prm.P2 = P2;
+        prm.P3 = P3;
+        prm.two_over_pi = (float)(2.0 / PI_D);
+        for (int s = 0; s < prm.nsys; ++s) {
+            double k = ks[s0 + s];
+            Sys32& S = prm.s[s];
+            S.kh = (float)k;
+            S.kl = (float)(k - (double)S.kh);
+            S.kd = k;
+            S.k2 = (float)(k * k);
+            S.beta_im = prm.bm ? (float)(1.0 / k) : 0.f;
+            S.gdiag_im = prm.bm ? 0.5 * (1.0 / k) : 0.0;
+            S.alpha = make_float2((float)alphas[s0 + s].re, (float)alphas[s0 + s].im);
+            S.beta = make_float2((float)betas[s0 + s].re, (float)betas[s0 + s].im);
+            S.gamma = make_float2((float)gammas[s0 + s].re, (float)gammas[s0 + s].im);
+            S.delta = make_float2((float)deltas[s0 + s].re, (float)deltas[s0 + s].im);
+        }
+        dim3 grid((unsigned)ntiles, (unsigned)ntiles);
+        float2* As = A + (size_t)s0 * mat_stride;
+        double* np_ = nbuf.as<double>();
+        if (rowsum) {
+            size_t pstride = (size_t)ntiles * p.geo.npad;
+            ctx.w_part.ensure(sizeof(double2) * pstride * prm.nsys);
+            double2* part = ctx.w_part.as<double2>();
+            assemble32_kernel<1><<<grid, ASM_THREADS, 0, ctx.stream>>>(p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0),
+                                                                       prm, As, ld, mat_stride, part, pstride, np_,
+                                                                       err);
+            BEM_CHECK_LAUNCH(&ctx);
+            for (int s = 0; s < prm.nsys; ++s)
+                launch_reduce_parts(ctx, p.n, p.geo.npad, ntiles, part + s * pstride,
+                                    rowsum + (size_t)(s0 + s) * vec_stride);
+        } else {
+            assemble32_kernel<0><<<grid, ASM_THREADS, 0, ctx.stream>>>(
+                p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0), prm, As, ld, mat_stride, nullptr, 0, np_, err);
+            BEM_CHECK_LAUNCH(&ctx);
+        }
+        if (norms) {
+            finish_norm_kernel<<<prm.nsys, 256, 0, ctx.stream>>>(np_, nparts, norms + s0);
+            BEM_CHECK_LAUNCH(&ctx);
+        }
+    }
+    check_device_err(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// Field points for all frequencies in one launch (influence_matrix.rs:101-127
+// + solve.rs:173-185 without storing M and L): one CTA per (field point,
+// frequency), single-precision kernel evaluation with the float-float phase,
+// per-thread sums folded into FP64, fixed-order block reduction.
+constexpr int F32_THREADS = 256;
+__global__ void __launch_bounds__(F32_THREADS) field32_kernel(
+    int64_t nfp, int64_t fpad, const float* __restrict__ fp32, int64_t n, int64_t npad, const float* __restrict__ g32,
+    Asm32Params prm, const double2* __restrict__ phi, const double2* __restrict__ vn, int64_t vstride,
+    const double2* __restrict__ inc, double2* __restrict__ out) {
+    __shared__ double shx[F32_THREADS], shy[F32_THREADS];
+    const int64_t i = blockIdx.x;
+    const int f = blockIdx.y;
+    const Sys32& S = prm.s[f];
+    const float pxh = fp32[i], pxl = fp32[fpad + i], pyh = fp32[2 * fpad + i], pyl = fp32[3 * fpad + i],
+                pzh = fp32[4 * fpad + i], pzl = fp32[5 * fpad + i];
+    const double2* ph = phi + (size_t)f * vstride;
+    const double2* vv = vn + (size_t)f * vstride;
+    const float inv4pi = (float)(1.0 / (4.0 * PI_D));
+    double ax = 0, ay = 0;
+    float bx = 0, by = 0;
+    int cnt = 0;
+    for (int64_t j = threadIdx.x; j < n; j += F32_THREADS) {
+        const Sep32 sp = separation32(pxh, pxl, pyh, pyl, pzh, pzl, g32[FXH * npad + j], g32[FXL * npad + j],
+                                      g32[FYH * npad + j], g32[FYL * npad + j], g32[FZH * npad + j],
+                                      g32[FZL * npad + j]);
+        // r = x - y with x the field point, y the element: e_r . n_y
+        const float rdoty =
+            (sp.dx * g32[FEX * npad + j] + sp.dy * g32[FEY * npad + j] + sp.dz * g32[FEZ * npad + j]) * sp.inv;
+        const float q = sp.inv * inv4pi * g32[FWA * npad + j];
+        float c0, s0;
+        phase32(S.kh, S.kl, sp.rh, sp.rl, prm, c0, s0);
+        float2 g = make_float2(c0 * q, s0 * q);
+        float2 h = fscale(fmul(g, make_float2(-sp.inv, S.kh)), -rdoty);
+        const double2 pj = ph[j], vj = vv[j];
+        const float2 pf = make_float2((float)pj.x, (float)pj.y), vf = make_float2((float)vj.x, (float)vj.y);
+        const float2 t1 = fmul(h, pf), t2 = fmul(g, vf);
+        bx += t2.x - t1.x;
+        by += t2.y - t1.y;
+        if (++cnt == 8) {
+            ax += bx;
+            ay += by;
+            bx = by = 0;
+            cnt = 0;
+        }
+    }
+    shx[threadIdx.x] = ax + bx;
+    shy[threadIdx.x] = ay + by;
+    __syncthreads();
+    for (int o = F32_THREADS / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            shx[threadIdx.x] += shx[threadIdx.x + o];
+            shy[threadIdx.x] += shy[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double2 r = make_double2(shx[0], shy[0]);
+        if (inc) r = cadd(r, inc[(size_t)f * nfp + i]);
+        out[(size_t)f * nfp + i] = r;
+    }
+}
+
+void evaluate_field32_batch(Context& ctx, const Problem& p, const double* ks, int nsys, const double2* phi,
+                            const double2* vn, int64_t vstride, const double2* inc, double2* out) {
+    if (p.nfp == 0) return;
+    const float P1 = 1.5703125f;
+    const double rem1 = PI_D / 2 - (double)P1;
+    for (int s0 = 0; s0 < nsys; s0 += MAX_SYS32) {
+        Asm32Params prm;
+        prm.nsys = std::min(MAX_SYS32, nsys - s0);
+        prm.bm = 0;
+        prm.hdiag = 0;
+        prm.P1 = P1;
+        prm.P2 = (float)rem1;
+        prm.P3 = (float)(rem1 - (double)prm.P2);
+        prm.two_over_pi = (float)(2.0 / PI_D);
+        for (int s = 0; s < prm.nsys; ++s) {
+            double k = ks[s0 + s];
+            prm.s[s].kh = (float)k;
+            prm.s[s].kl = (float)(k - (double)prm.s[s].kh);
+            prm.s[s].kd = k;
+        }
+        dim3 grid((unsigned)p.nfp, (unsigned)prm.nsys);
+        field32_kernel<<<grid, F32_THREADS, 0, ctx.stream>>>(
+            p.nfp, p.nfp_pad, p.d_fp32.as<float>(), p.n, p.geo.npad, p.geo.arr32(0), prm, phi + (size_t)s0 * vstride,
+            vn + (size_t)s0 * vstride, vstride, inc ? inc + (size_t)s0 * p.nfp : nullptr, out + (size_t)s0 * p.nfp);
+        BEM_CHECK_LAUNCH(&ctx);
+    }
+}
+
+}  // namespace bem

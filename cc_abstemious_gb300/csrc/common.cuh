@@ -125,6 +125,7 @@ struct Problem {
     int64_t n = 0, nfp = 0;
     DevGeometry geo;           // device collocation (computed by the collocation kernel)
     DevBuf d_fp;               // field points, 3 arrays of nfp_pad
+    DevBuf d_fp32;             // field points as float-float, 6 arrays of nfp_pad
     int64_t nfp_pad = 0;
     int device = 0;
     double frequency() const { return freqs.empty() ? 0.0 : freqs[(size_t)ifreq]; }
@@ -158,7 +159,7 @@ struct Context {
     std::string last_error;
     int64_t launches = 0;
     // workspaces (grow-only)
-    DevBuf w_mat, w_mat2, w_vec, w_small, w_flags, w_part;
+    DevBuf w_mat, w_mat2, w_vec, w_small, w_flags, w_part, w_norm;
     // results of the last bem_run
     std::vector<double> last_phi, last_vn;
     int64_t last_n = 0, last_nf = 0;
@@ -192,7 +193,9 @@ void assemble_system_fp64(Context& ctx, const Problem& p, double2* A, int64_t ld
                           cd gamma, cd delta, double2* rowsum /* n, may be null */);
 void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
                                const cd* betas, const cd* gammas, const cd* deltas, int nsys, float2* A,
-                               int64_t ld, size_t mat_stride, double2* rowsum, size_t vec_stride);
+                               int64_t ld, size_t mat_stride, double2* rowsum, size_t vec_stride, double* norms);
+void evaluate_field32_batch(Context& ctx, const Problem& p, const double* ks, int nsys, const double2* phi,
+                            const double2* vn, int64_t vstride, const double2* inc, double2* out);
 void field_matrices_fp64(Context& ctx, const Problem& p, double2* M, double2* L, int64_t ld);
 void evaluate_field(Context& ctx, const Problem& p, const double2* phi, const double2* vn,
                     const double2* inc, double2* out);

@@ -158,6 +158,18 @@ void upload_field_points(Context& ctx, Problem& p) {
     p.d_fp.ensure(sizeof(double) * soa.size());
     BEM_CUDA(cudaMemcpyAsync(p.d_fp.p, soa.data(), sizeof(double) * soa.size(), cudaMemcpyHostToDevice,
                              ctx.stream));
+    // float-float copy (hi, lo per coordinate) for the single-precision field kernel
+    std::vector<float> ff((size_t)6 * p.nfp_pad, 0.f);
+    for (int k = 0; k < 3; ++k)
+        for (int64_t i = 0; i < p.nfp_pad; ++i) {
+            double v = soa[(size_t)(k * p.nfp_pad + i)];
+            float hi = (float)v;
+            ff[(size_t)((2 * k) * p.nfp_pad + i)] = hi;
+            ff[(size_t)((2 * k + 1) * p.nfp_pad + i)] = (float)(v - (double)hi);
+        }
+    p.d_fp32.ensure(sizeof(float) * ff.size());
+    BEM_CUDA(cudaMemcpyAsync(p.d_fp32.p, ff.data(), sizeof(float) * ff.size(), cudaMemcpyHostToDevice, ctx.stream));
+    ctx.sync();
 }
 
 KParams kparams(const Problem& p) {

@@ -50,8 +50,18 @@ __device__ __forceinline__ void ff_acc(float& hi, float& lo, float a, float b) {
 // Batched operator application W_s = A_s v_s, v_s = x_s (START/CHECK) or
 // Q_s[:, k] (Q).  Grid (row blocks, column chunks, systems); partial sums of
 // the column chunks are reduced in a fixed order by the last CTA of each row
-// block (ticket counter, no waiting).
-template <typename T>
+// block (ticket counter, no waiting).  Each thread owns two consecutive rows
+// and streams its columns with 16-byte loads, eight columns in flight.
+//
+// FP32 operators, two accumulation schemes:
+//  EXACT (true residuals, START/CHECK): x split into hi + lo floats, every
+//        product split exactly with an FMA and summed in float-float;
+//  FAST  (Krylov vectors, Q): FP32 sums of 8 columns folded into a float-float
+//        accumulator; ~1e-7 relative, which only perturbs the Krylov basis:
+//        the exact residual at each check and restart keeps the answer exact.
+constexpr int MV_UNROLL = 8;
+
+template <typename T, int EXACT>
 __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mode) {
     const int s = blockIdx.z;
     GmState& st = bt.st[s];
@@ -63,8 +73,8 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
     __shared__ int last;
     const int64_t j0 = (int64_t)blockIdx.y * MV_COLS;
     const int jn = (int)min((int64_t)MV_COLS, n - j0);
-    for (int t = threadIdx.x; t < jn; t += MV_THREADS) {
-        double2 x = v[j0 + t];
+    for (int t = threadIdx.x; t < MV_COLS; t += MV_THREADS) {
+        double2 x = t < jn ? v[j0 + t] : make_double2(0, 0);
         if (sizeof(T) == sizeof(float2)) {
             float hx = (float)x.x, hy = (float)x.y;
             xh[t] = make_float2(hx, hy);
@@ -77,41 +87,80 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
     const int64_t i0 = (int64_t)blockIdx.x * MV_ROWS + MV_ROWS_PER_THREAD * threadIdx.x;
     double2 r0 = make_double2(0, 0), r1 = make_double2(0, 0);
     if (i0 < n) {
+        const bool pair = (i0 + 1 < n);
         if (sizeof(T) == sizeof(float2)) {
-            const float2* A = reinterpret_cast<const float2*>(bt.A) + (size_t)s * bt.mat_stride;
+            const float2* A = reinterpret_cast<const float2*>(bt.A) + (size_t)s * bt.mat_stride + i0;
             // float-float accumulators for (re0, im0, re1, im1)
             float h0 = 0, l0 = 0, h1 = 0, l1 = 0, h2 = 0, l2 = 0, h3 = 0, l3 = 0;
-            const bool pair = (i0 + 1 < n);
-            for (int q = 0; q < jn; ++q) {
-                const float2* col = A + (j0 + q) * bt.lda + i0;
-                float4 a;
-                if (pair) a = *reinterpret_cast<const float4*>(col);
-                else { float2 t = col[0]; a = make_float4(t.x, t.y, 0.f, 0.f); }
-                float2 H = xh[q], L = xl[q];
-                ff_acc(h0, l0, a.x, H.x); ff_acc(h0, l0, -a.y, H.y);
-                ff_acc(h1, l1, a.x, H.y); ff_acc(h1, l1, a.y, H.x);
-                ff_acc(h2, l2, a.z, H.x); ff_acc(h2, l2, -a.w, H.y);
-                ff_acc(h3, l3, a.z, H.y); ff_acc(h3, l3, a.w, H.x);
-                l0 = fmaf(a.x, L.x, fmaf(-a.y, L.y, l0));
-                l1 = fmaf(a.x, L.y, fmaf(a.y, L.x, l1));
-                l2 = fmaf(a.z, L.x, fmaf(-a.w, L.y, l2));
-                l3 = fmaf(a.z, L.y, fmaf(a.w, L.x, l3));
+            for (int q0 = 0; q0 < jn; q0 += MV_UNROLL) {
+                float4 a[MV_UNROLL];
+#pragma unroll
+                for (int u = 0; u < MV_UNROLL; ++u) {
+                    const int q = q0 + u;
+                    if (q < jn) {
+                        const float2* col = A + (j0 + q) * bt.lda;
+                        if (pair) a[u] = __ldcs(reinterpret_cast<const float4*>(col));
+                        else { float2 t = col[0]; a[u] = make_float4(t.x, t.y, 0.f, 0.f); }
+                    } else {
+                        a[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                }
+                if (EXACT) {
+#pragma unroll
+                    for (int u = 0; u < MV_UNROLL; ++u) {
+                        const float2 H = xh[q0 + u], L = xl[q0 + u];
+                        const float4 w = a[u];
+                        ff_acc(h0, l0, w.x, H.x); ff_acc(h0, l0, -w.y, H.y);
+                        ff_acc(h1, l1, w.x, H.y); ff_acc(h1, l1, w.y, H.x);
+                        ff_acc(h2, l2, w.z, H.x); ff_acc(h2, l2, -w.w, H.y);
+                        ff_acc(h3, l3, w.z, H.y); ff_acc(h3, l3, w.w, H.x);
+                        l0 = fmaf(w.x, L.x, fmaf(-w.y, L.y, l0));
+                        l1 = fmaf(w.x, L.y, fmaf(w.y, L.x, l1));
+                        l2 = fmaf(w.z, L.x, fmaf(-w.w, L.y, l2));
+                        l3 = fmaf(w.z, L.y, fmaf(w.w, L.x, l3));
+                    }
+                } else {
+                    float b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+#pragma unroll
+                    for (int u = 0; u < MV_UNROLL; ++u) {
+                        const float2 H = xh[q0 + u];
+                        const float4 w = a[u];
+                        b0 = fmaf(w.x, H.x, fmaf(-w.y, H.y, b0));
+                        b1 = fmaf(w.x, H.y, fmaf(w.y, H.x, b1));
+                        b2 = fmaf(w.z, H.x, fmaf(-w.w, H.y, b2));
+                        b3 = fmaf(w.z, H.y, fmaf(w.w, H.x, b3));
+                    }
+                    float e, t;
+                    two_sum(h0, b0, t, e); h0 = t; l0 += e;
+                    two_sum(h1, b1, t, e); h1 = t; l1 += e;
+                    two_sum(h2, b2, t, e); h2 = t; l2 += e;
+                    two_sum(h3, b3, t, e); h3 = t; l3 += e;
+                }
             }
             r0 = make_double2((double)h0 + (double)l0, (double)h1 + (double)l1);
             r1 = make_double2((double)h2 + (double)l2, (double)h3 + (double)l3);
         } else {
-            const double2* A = reinterpret_cast<const double2*>(bt.A) + (size_t)s * bt.mat_stride;
-            const bool pair = (i0 + 1 < n);
-            for (int q = 0; q < jn; ++q) {
-                const double2* col = A + (j0 + q) * bt.lda + i0;
-                double2 xv = xd[q];
-                cfma(r0, col[0], xv);
-                if (pair) cfma(r1, col[1], xv);
+            const double2* A = reinterpret_cast<const double2*>(bt.A) + (size_t)s * bt.mat_stride + i0;
+            for (int q0 = 0; q0 < jn; q0 += MV_UNROLL) {
+                double2 a0[MV_UNROLL], a1[MV_UNROLL];
+#pragma unroll
+                for (int u = 0; u < MV_UNROLL; ++u) {
+                    const int q = q0 + u;
+                    const double2* col = A + (j0 + (q < jn ? q : 0)) * bt.lda;
+                    a0[u] = q < jn ? col[0] : make_double2(0, 0);
+                    a1[u] = (q < jn && pair) ? col[1] : make_double2(0, 0);
+                }
+#pragma unroll
+                for (int u = 0; u < MV_UNROLL; ++u) {
+                    const double2 xv = xd[q0 + u];
+                    cfma(r0, a0[u], xv);
+                    cfma(r1, a1[u], xv);
+                }
             }
         }
         double2* part = bt.part + ((size_t)s * gridDim.y + blockIdx.y) * bt.n_pad;
         part[i0] = r0;
-        if (i0 + 1 < n) part[i0 + 1] = r1;
+        if (pair) part[i0 + 1] = r1;
     }
     __threadfence();
     __syncthreads();
@@ -336,7 +385,11 @@ __global__ void __launch_bounds__(AR_THREADS) gm_check_kernel(GmBatch bt) {
         if (st.error < st.tol) {
             st.done = 1;
             st.converged = 1;
-        } else if (st.k == bt.m - 1) {
+        } else if (st.k == bt.m - 1 || !bt.ref_dotc) {
+            // End of the cycle.  Outside the reference-faithful mode a failed
+            // check also restarts from the updated x (an iterative-refinement
+            // step), instead of continuing the Arnoldi process and adding the
+            // Krylov correction to x a second time at the next check.
             st.restarts += 1;
             if (st.restarts >= st.max_restarts) st.done = 1;
             else st.need_start = 1;
@@ -378,18 +431,20 @@ __global__ void gm_init_kernel(GmBatch bt, const double* anorm, double tol, int6
     }
 }
 
-// Frobenius norms of a batch of matrices (FP64 or FP32 entries).
+// Frobenius norms of a batch of matrices (FP64 or FP32 entries): CTAs stride
+// over columns, threads over rows (coalesced, no index division).
 template <typename T>
 __global__ void batch_frob_kernel(const void* A, int64_t n, int64_t lda, size_t mat_stride, double* part, int nb) {
     __shared__ double sh[80];
     int s = blockIdx.y;
     const T* M = reinterpret_cast<const T*>(A) + (size_t)s * mat_stride;
     double acc = 0;
-    int64_t total = n * n;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t j = t / n, i = t - j * n;
-        T v = M[j * lda + i];
-        acc += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+    for (int64_t j = blockIdx.x; j < n; j += gridDim.x) {
+        const T* col = M + j * lda;
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+            T v = col[i];
+            acc += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+        }
     }
     double r = block_sum(acc, sh);
     if (threadIdx.x == 0) part[(size_t)s * nb + blockIdx.x] = r;
@@ -478,8 +533,12 @@ void gm_init(Context& ctx, GmWorkspace& ws, double tol, int64_t max_restarts) {
 
 static void launch_apply(Context& ctx, GmWorkspace& ws, int mode) {
     dim3 grid((unsigned)ws.rb, (unsigned)ws.cb, (unsigned)ws.bt.nsys);
-    if (ws.fp32) gm_apply_kernel<float2><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
-    else gm_apply_kernel<double2><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+    if (ws.fp32) {
+        if (mode == MV_Q) gm_apply_kernel<float2, 0><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+        else gm_apply_kernel<float2, 1><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+    } else {
+        gm_apply_kernel<double2, 1><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+    }
     BEM_CHECK_LAUNCH(&ctx);
 }
 

@@ -100,8 +100,13 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     }
     const bool need_rowsum = !(p.in.bc_value[0] == 0.0 && p.in.bc_value[1] == 0.0) && p.in.bc_type != 2;
 
-    c.w_mat.ensure(sizeof(float2) * mstride * nf);
+    // A first-kind operator (classical formulation with a pressure condition:
+    // the single layer G alone) is too ill-conditioned for single-precision
+    // storage at 1e-6; those systems keep an FP64 operator in the same batch.
+    const bool first_kind = p.in.method_type == 0 && p.in.bc_type == 0;
+    c.w_mat.ensure((first_kind ? sizeof(double2) : sizeof(float2)) * mstride * nf);
     float2* A32 = c.w_mat.as<float2>();
+    double2* A64 = c.w_mat.as<double2>();
     c.w_vec.ensure(sizeof(double2) * (size_t)nf * (4 * n + 2 * nfp + 2));
     double2* inc = c.w_vec.as<double2>();
     double2* rowsum = inc + nf * n;
@@ -110,10 +115,33 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     double2* finc = vn + nf * n;
     double2* fps = finc + nf * nfp;
 
-    {
+    // solver parameters: the problem's GMRES settings, or for the direct
+    // solver a tight tolerance (the mixed form always iterates)
+    int64_t max_it = p.in.solver == 0 ? 1000 : p.in.max_iterations;
+    double tol = p.in.solver == 0 ? 1e-10 : p.in.tolerance;
+    if (max_it <= 0) max_it = 1000;
+    if (max_it > n) max_it = n;
+    if (tol <= 0) tol = 1e-5;
+    int m = (int)std::ceil(std::sqrt((double)max_it));
+    int64_t restarts = max_it / m;
+    GmWorkspace ws;
+    gm_prepare(c, ws, (int)nf, n, m, first_kind ? (const void*)A64 : (const void*)A32, ld, mstride, !first_kind,
+               false);
+
+    if (first_kind) {
+        EventTimer t(c);
+        for (int64_t f = 0; f < nf; ++f) {
+            p.ifreq = f;
+            assemble_system_fp64(c, p, A64 + f * mstride, ld, al[f], be[f], ga[f], de[f],
+                                 need_rowsum ? rowsum + f * n : nullptr);
+        }
+        gm_matrix_norms(c, ws);
+        t.stop("assemble_fp64", nf, 16.0 * (double)n * n * nf);
+    } else {
+        // the assembly kernel also writes ||A_f||_F for the stopping test
         EventTimer t(c);
         assemble_system_fp32_body(c, p, ks.data(), al.data(), be.data(), ga.data(), de.data(), (int)nf, A32, ld,
-                                  mstride, need_rowsum ? rowsum : nullptr, (size_t)n);
+                                  mstride, need_rowsum ? rowsum : nullptr, (size_t)n, ws.anorm);
         t.stop("assemble_fp32", (nf + 15) / 16, 8.0 * (double)n * n * nf);
     }
     {
@@ -125,18 +153,6 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
         t.stop("incident", nf, 0);
     }
 
-    // solver parameters: the problem's GMRES settings, or for the direct
-    // solver a tight tolerance (the mixed form always iterates)
-    int64_t max_it = p.in.solver == 0 ? 1000 : p.in.max_iterations;
-    double tol = p.in.solver == 0 ? 1e-10 : p.in.tolerance;
-    if (max_it <= 0) max_it = 1000;
-    if (max_it > n) max_it = n;
-    if (tol <= 0) tol = 1e-5;
-    int m = (int)std::ceil(std::sqrt((double)max_it));
-    int64_t restarts = max_it / m;
-
-    GmWorkspace ws;
-    gm_prepare(c, ws, (int)nf, n, m, A32, ld, mstride, true, false);
     const double s = p.in.bc_type == 0 ? 1.0 : -1.0;
     for (int64_t f = 0; f < nf; ++f)
         launch_rhs_combine(c, n, s, inc + f * n, {p.in.bc_value[0], p.in.bc_value[1]},
@@ -144,7 +160,6 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     std::vector<GmState> st;
     {
         EventTimer t(c);
-        gm_matrix_norms(c, ws);
         gm_init(c, ws, tol, restarts);
         if (precond != BEM_PRECOND_NONE)
             precond_setup(c, p, ws, precond, ks.data());
@@ -152,7 +167,7 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
         gm_read_states(c, ws, st);
         int64_t mv = 0;
         for (auto& x : st) mv += x.num_mv;
-        t.stop("gmres", mv, 8.0 * (double)n * n * mv);
+        t.stop("gmres", mv, (first_kind ? 16.0 : 8.0) * (double)n * n * mv);
     }
     {
         EventTimer t(c);
@@ -160,10 +175,9 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
             p.ifreq = f;
             unpack_solution(c, p, ws.bt.X + f * n, phi + f * n, vn + f * n);
             incident_field(c, p, finc + f * nfp);
-            evaluate_field(c, p, phi + f * n, vn + f * n, p.in.output_total ? finc + f * nfp : nullptr,
-                           fps + f * nfp);
         }
-        t.stop("field", nf, 0);
+        evaluate_field32_batch(c, p, ks.data(), (int)nf, phi, vn, n, p.in.output_total ? finc : nullptr, fps);
+        t.stop("field", 1, 0);
     }
     std::vector<double2> hs((size_t)(nf * nfp)), hi((size_t)(nf * nfp));
     c.last_phi.assign((size_t)(2 * n * nf), 0.0);

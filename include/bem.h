@@ -118,6 +118,9 @@ BEM_API const char* bem_version(void);
  * counterpart).  Profiling runs the GMRES iteration by iteration so that every
  * Krylov mat-vec launch is bracketed by events on the context's stream. */
 BEM_API bem_status bem_ctx_set_profiling(bem_ctx* ctx, int on);
+/* The context's CUDA stream (cudaStream_t), so callers can order their own
+ * work or record CUDA events around library calls. */
+BEM_API void* bem_ctx_stream(const bem_ctx* ctx);
 BEM_API int64_t bem_ctx_profile_count(const bem_ctx* ctx);
 BEM_API bem_status bem_ctx_profile_get(const bem_ctx* ctx, int64_t i, char* name, int64_t name_len,
                                        double* ms, int64_t* launches, double* bytes);
@@ -154,6 +157,11 @@ BEM_API bem_status bem_get_surface_row_or_column(bem_ctx* ctx, const bem_problem
                                                  const int64_t* I, int64_t ni,
                                                  const int64_t* J, int64_t nj,
                                                  bem_side side, bem_cplx* out);
+
+/* The mixed form's single-precision system matrix alpha H + beta G
+ * (influence_matrix.rs:130-146 factors) at the current frequency, as
+ * interleaved {re, im} floats, n x n column-major, host memory. */
+BEM_API bem_status bem_get_system_matrix_fp32(bem_ctx* ctx, const bem_problem* p, float* A, int64_t ld);
 
 /* ---- incident wave (incident_wave.rs) --------------------------------- */
 /* incident_wave.rs:7-63 get_incident_surface (n entries, host memory). */

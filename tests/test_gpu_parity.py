@@ -75,6 +75,23 @@ def test_dense_surface_matrices_device(ctx, name, inp):
     assert rel(Gt.cpu().numpy()[:, :n].T, Go) < 1e-12
 
 
+@pytest.mark.parametrize("name,inp", problems() + [
+    ("tri_bm_kr40", sphere_input(method_type="BurtonMiller", frequency={"List": {"values": [9549.0]}})),
+    ("quad_bm_kr40", sphere_input("sphere_quad.vtk", body_index=2, method_type="BurtonMiller",
+                                  frequency={"List": {"values": [9549.0]}}))])
+def test_system_matrix_fp32(ctx, name, inp):
+    """Single-precision assembly (float-float phase, Taylor sin/cos) against the
+    FP64 oracle: entry errors within a few FP32 ulps of the largest entry."""
+    pd = bem.PreData.from_dict(inp, ctx=ctx)
+    op = O.Problem(inp)
+    H, G = op.dense_surface()
+    a, b = op.lhs_factors()
+    ref = a * H + b * G
+    A = bem.get_system_matrix_fp32(pd).astype(np.complex128)
+    assert rel(A, ref) < 3e-7
+    assert np.linalg.norm(A - ref) / np.linalg.norm(ref) < 1e-7
+
+
 @pytest.mark.parametrize("name,inp", problems()[:3])
 def test_row_or_column(ctx, name, inp):
     pd = bem.PreData.from_dict(inp, ctx=ctx)
