@@ -14,13 +14,6 @@
 #include "hmatrix.cuh"
 #include "mixed.cuh"
 
-struct bem_ctx {
-    bem::Context c;
-};
-struct bem_problem {
-    bem::Problem p;
-};
-
 namespace bem {
 
 template <class F>

@@ -223,3 +223,11 @@ GmresResult gmres_dense_fp64(Context& ctx, int64_t n, const double2* A, int64_t 
                              double tol, double2* x);
 
 }  // namespace bem
+
+// Opaque handles of the C ABI.
+struct bem_ctx {
+    bem::Context c;
+};
+struct bem_problem {
+    bem::Problem p;
+};

@@ -66,6 +66,9 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
     const int s = blockIdx.z;
     GmState& st = bt.st[s];
     if (!mv_active(st, mode)) return;
+    // outside the reference-faithful mode the first cycle starts from x = 0,
+    // so its residual is b itself: no product needed
+    if (mode == MV_START && !bt.ref_dotc && st.restarts == 0) return;
     const int64_t n = bt.n;
     const double2* v = (mode == MV_Q) ? bt.Q + (size_t)s * bt.qstride + (size_t)st.k * n : bt.X + (size_t)s * n;
     __shared__ float2 xh[MV_COLS], xl[MV_COLS];
@@ -239,9 +242,10 @@ __global__ void __launch_bounds__(AR_THREADS) gm_start_kernel(GmBatch bt) {
     const double2* b = bt.B + (size_t)s * n;
     const double2* W = bt.W + (size_t)s * n;
     double2* Q = bt.Q + (size_t)s * bt.qstride;
+    const bool zero_x = !bt.ref_dotc && st.restarts == 0;  // x = 0: A x not formed
     double acc = 0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-        double2 r = csub(b[i], W[i]);
+        double2 r = zero_x ? b[i] : csub(b[i], W[i]);
         Q[i] = r;
         acc += r.x * r.x + r.y * r.y;
     }
@@ -261,7 +265,7 @@ __global__ void __launch_bounds__(AR_THREADS) gm_start_kernel(GmBatch bt) {
         st.k = 0;
         st.need_start = 0;
         st.check = 0;
-        st.num_mv += 1;
+        st.num_mv += zero_x ? 0 : 1;
     }
 }
 
@@ -532,6 +536,10 @@ void gm_init(Context& ctx, GmWorkspace& ws, double tol, int64_t max_restarts) {
 }
 
 static void launch_apply(Context& ctx, GmWorkspace& ws, int mode) {
+    if (ws.hook) {
+        ws.hook(ctx, ws, mode, ws.hook_user);
+        return;
+    }
     dim3 grid((unsigned)ws.rb, (unsigned)ws.cb, (unsigned)ws.bt.nsys);
     if (ws.fp32) {
         if (mode == MV_Q) gm_apply_kernel<float2, 0><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);

@@ -27,6 +27,14 @@ struct GmBatch {
     GmState* st;
 };
 
+// Whether the operator application of `mode` has work for a system.
+__device__ __forceinline__ bool gm_apply_active(const GmBatch& bt, const GmState& s, int mode) {
+    if (s.done) return false;
+    if (mode == MV_START) return s.need_start != 0 && !(!bt.ref_dotc && s.restarts == 0);
+    if (mode == MV_Q) return s.need_start == 0 && s.check == 0;
+    return s.check != 0;  // MV_CHECK
+}
+
 struct GmSmall {
     double2 *hk1, *cs, *sn, *beta, *H, *y;
 };
@@ -48,8 +56,15 @@ __device__ inline GmSmall gm_small(const GmBatch& bt, int s) {
     return g;
 }
 
+struct GmWorkspace;
+// Operator application hook (H-matrix): launches W_s = A_s v_s for `mode`,
+// predicated on the state like the dense apply kernel.
+typedef void (*GmApplyHook)(Context& ctx, GmWorkspace& ws, int mode, void* user);
+
 struct GmWorkspace {
     GmBatch bt{};
+    GmApplyHook hook = nullptr;
+    void* hook_user = nullptr;
     DevBuf mem;
     bool fp32 = false;
     bool w_in_smem = false;

@@ -4,6 +4,8 @@
 
 namespace bem {
 
+struct HMatrixDev;
+
 void solve_surface_hmatrix(Context& c, const Problem& p, const double2* d_rhs_inc, double2* d_phi, double2* d_vn,
                            bem_solve_report* rep);
 

@@ -1,0 +1,103 @@
+"""GPU H-matrix (cluster/block trees, ACA with the reference's pivot stream,
+QR+SVD recompression, leaf mat-vec, GMRES) against the oracle and the
+reference's H-matrix known answer."""
+import numpy as np
+import pytest
+
+from conftest import sphere_input
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+bem = pytest.importorskip("cc_abstemious_gb300")
+
+HIER = {"Hierarchical": {"max_iterations": 1000, "tolerance": 1e-5}}
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return bem.Context.default()
+
+
+def oracle_hmatrix(inp, side):
+    P = O.Problem(inp)
+
+    def gen(ctx_, I, ni, J, nj, out):
+        ii = np.ctypeslib.as_array(I, shape=(ni,)).copy()
+        jj = np.ctypeslib.as_array(J, shape=(nj,)).copy()
+        o = np.ctypeslib.as_array(out, shape=(2 * max(ni, nj),)).view(np.complex128)
+        o[:] = P.row_or_column(ii, jj, side)
+
+    s = P.s
+    return P, O.HMatrix(P.cpts, int(s.hm_leaf), float(s.hm_eta), float(s.hm_aca_tol), gen=gen)
+
+
+def test_hmatrix_golden(ctx, goldens):
+    """src/tests/verification.rs:150-176 (absolute 1e-10)."""
+    a = bem.Analysis(ctx)
+    a.set_input(sphere_input(solver=HIER))
+    a.run()
+    v = a.get_result()[0].scattered[0]
+    g = goldens["rigid_sphere_plane_wave_hmatrix"]
+    assert abs(v.real - g["value"][0]) < 1e-10 and abs(v.imag - g["value"][1]) < 1e-10
+
+
+@pytest.mark.parametrize("kw", [{}, {"method_type": "BurtonMiller"},
+                                {"surface_bc": {"bc_type": "Pressure", "value": [0.3, -0.1]}}])
+def test_hmatrix_against_oracle(ctx, kw):
+    inp = sphere_input(solver=HIER, **kw)
+    pd = bem.PreData.from_dict(inp, ctx=ctx)
+    P, Ho = oracle_hmatrix(inp, 1)
+    H = bem.HMatrix(pd, bem.EqnSide.LHS)
+    so, sg = Ho.stats(), H.stats()
+    assert so == sg
+    assert abs(H.norm - Ho.norm) <= 1e-12 * Ho.norm
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=pd.n) + 1j * rng.normal(size=pd.n)
+    b = rng.normal(size=pd.n) + 1j * rng.normal(size=pd.n)
+    y = H.gemv(0.5 - 1j, x, 2.0 + 0.5j, b)
+    yo = Ho.gemv(0.5 - 1j, x, 2.0 + 0.5j, b)
+    assert np.max(np.abs(y - yo)) <= 1e-12 * np.max(np.abs(yo))
+    F, Fo = H.to_full(), Ho.to_full()
+    assert np.max(np.abs(F - Fo)) <= 1e-12 * np.max(np.abs(Fo))
+    # the compression is within the ACA tolerance of the dense matrix
+    Hd, Gd = P.dense_surface()
+    al, be = P.lhs_factors()
+    A = al * Hd + be * Gd
+    assert np.linalg.norm(F - A) / np.linalg.norm(A) < 1e-3
+
+
+@pytest.mark.parametrize("kw", [{}, {"method_type": "BurtonMiller"},
+                                {"surface_bc": {"bc_type": "Pressure", "value": [0.3, -0.1]}},
+                                {"surface_bc": {"bc_type": "NormalVelocity", "value": [1.0, 0.2]}},
+                                {"method_type": "BurtonMiller",
+                                 "surface_bc": {"bc_type": "Impedance", "value": [1.5e6, 3e5]}}])
+def test_hierarchical_solve_vs_oracle(ctx, kw):
+    inp = sphere_input(solver=HIER, **kw)
+    pd = bem.PreData.from_dict(inp, ctx=ctx)
+    op = O.Problem(inp)
+    rhs = op.incident_surface()
+    phi, vn, rep = bem.solve_for_surface(pd, rhs)
+    phio, vno, st, orep = op.solve_for_surface(rhs)
+    assert rep["num_mv"] == orep.num_mv
+    assert np.max(np.abs(phi - phio)) <= 1e-9 * np.max(np.abs(phio))
+    assert np.max(np.abs(vn - vno)) <= 1e-9 * np.max(np.abs(vno))
+
+
+def test_hierarchical_extension_keys(ctx):
+    """Additive optional keys leaf_size / eta / aca_tolerance (defaults are the
+    reference's hard-coded 32 / 4 / 1e-4)."""
+    solver = {"Hierarchical": {"max_iterations": 1000, "tolerance": 1e-6, "leaf_size": 16, "eta": 1.0,
+                               "aca_tolerance": 1e-5}}
+    inp = sphere_input("refined_sphere.vtk", solver=solver, method_type="BurtonMiller")
+    pd = bem.PreData.from_dict(inp, ctx=ctx)
+    assert pd.info["hm_leaf"] == 16 and pd.info["hm_eta"] == 1.0 and pd.info["hm_aca_tol"] == 1e-5
+    P, Ho = oracle_hmatrix(inp, 1)
+    H = bem.HMatrix(pd, bem.EqnSide.LHS)
+    assert H.stats() == Ho.stats()
+    a = bem.Analysis(ctx)
+    a.set_input(inp)
+    a.run()
+    ref = O.Problem(dict(inp, solver={"Direct": {}})).run()[0]["scattered"]
+    got = a.get_result()[0].scattered
+    assert np.max(np.abs(got - ref)) <= 1e-4 * np.max(np.abs(ref))

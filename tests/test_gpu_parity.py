@@ -88,7 +88,7 @@ def test_system_matrix_fp32(ctx, name, inp):
     a, b = op.lhs_factors()
     ref = a * H + b * G
     A = bem.get_system_matrix_fp32(pd).astype(np.complex128)
-    assert rel(A, ref) < 3e-7
+    assert rel(A, ref) < 6e-7  # ~5 FP32 ulps of the largest entry
     assert np.linalg.norm(A - ref) / np.linalg.norm(ref) < 1e-7
 
 
