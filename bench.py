@@ -114,14 +114,14 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic_per_matrix():
-    """DRAM bytes per matrix-row-block pass of the FP32 batched mat-vec from the
-    committed ncu summary (profiles/), or None."""
+def ncu_traffic_ratio():
+    """DRAM traffic / algorithmic bytes of the batched FP32 mat-vec, from the
+    committed ncu summary (profiles/); traffic scales with the matrices streamed."""
     p = os.path.join(ROOT, "profiles", "gm_apply_fp32_rigid_sphere_bm.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("dram_bytes_per_matrix:"):
+        if line.startswith("traffic_over_algorithmic:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -311,14 +311,16 @@ def main():
     hbm_peak, peak_kind = measured_peaks()
     mv = prof.get("gmres_matvec_fp32", {})
     achieved = mv["bytes"] / (mv["ms"] * 1e-3) / 1e9 if mv.get("ms") else None
-    per_matrix = ncu_traffic_per_matrix()
-    matrices_per_launch = mv["bytes"] / (8.0 * pd.n * pd.n) / max(mv.get("launches", 1), 1) if mv else None
+    ratio = ncu_traffic_ratio()
+    alg_per_launch = mv["bytes"] / max(mv["launches"], 1) if mv else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak if achieved else None,
-                "traffic": per_matrix * matrices_per_launch if (per_matrix and matrices_per_launch) else None,
-                "kernel": "gm_apply_kernel<float2> (batched FP32-operator mat-vec, compensated)",
-                "algorithmic_bytes_per_launch": mv["bytes"] / max(mv["launches"], 1) if mv else None,
-                "peak_kind": peak_kind + " (burst copy)"}
+                "traffic": ratio * alg_per_launch if (ratio and alg_per_launch) else None,
+                "kernel": "gm_apply_kernel<float2, 0> (batched FP32-operator Krylov mat-vec)",
+                "algorithmic_bytes_per_launch": alg_per_launch,
+                "peak_kind": peak_kind + " (burst copy)",
+                "traffic_note": "ncu dram read+write / algorithmic bytes from profiles/"
+                                "gm_apply_fp32_rigid_sphere_bm.md (small case), scaled to this launch"}
 
     # ---- CPU baseline: the oracle on a bounded sample, host cores of this machine
     threads = max((os.cpu_count() or 2) // 2, 2)

@@ -102,6 +102,10 @@ def test_hierarchical_extension_keys(ctx):
     a = bem.Analysis(ctx)
     a.set_input(inp)
     a.run()
-    ref = O.Problem(dict(inp, solver={"Direct": {}})).run()[0]["scattered"]
     got = a.get_result()[0].scattered
-    assert np.max(np.abs(got - ref)) <= 1e-4 * np.max(np.abs(ref))
+    # same algorithm on the CPU (ranks may differ by a truncation near-tie)
+    ref_h = O.Problem(inp).run()[0]["scattered"]
+    assert np.max(np.abs(got - ref_h)) <= 1e-6 * np.max(np.abs(ref_h))
+    # within the compression + GMRES tolerance of the dense direct answer
+    ref = O.Problem(dict(inp, solver={"Direct": {}})).run()[0]["scattered"]
+    assert np.max(np.abs(got - ref)) <= 1e-3 * np.max(np.abs(ref))
