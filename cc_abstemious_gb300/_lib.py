@@ -76,6 +76,7 @@ SIGNATURES = {
     "bem_solve_for_surface": (_i, [_vp, _vp, _vp, _vp, _vp, C.POINTER(SolveReport)]),
     "bem_solve_lu": (_i, [_vp, _i64, _vp, _i64, _vp, _i]),
     "bem_gmres_solve": (_i, [_vp, _i64, _vp, _i64, _i64, _d, _vp, C.POINTER(SolveReport), _i]),
+    "bem_gmres_solve_noalloc": (_i, [_vp, _i64, _vp, _i64, _i64, _d, _vp, C.POINTER(SolveReport)]),
     "bem_get_field": (_i, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i]),
     "bem_evaluate_field": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "bem_convert_to_pressure": (_i, [_vp, _d, _vp, _i64]),

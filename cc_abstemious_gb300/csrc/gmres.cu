@@ -516,6 +516,59 @@ void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const
     }
 }
 
+// Same layout as gm_prepare, carved from caller-provided device memory instead
+// of an allocation.  Returns the bytes the layout needs; when that exceeds
+// `capacity` nothing is written and the workspace is left unset.
+size_t gm_prepare_external(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const void* A, int64_t lda,
+                           size_t mat_stride, bool fp32, bool ref_dotc, void* mem, size_t capacity) {
+    const int64_t n_pad = (n + MV_ROWS - 1) / MV_ROWS * MV_ROWS;
+    const size_t qstride = (size_t)n * (m + 1);
+    const int rb = (int)((n + MV_ROWS - 1) / MV_ROWS), cb = (int)((n + MV_COLS - 1) / MV_COLS);
+    const size_t small = gm_small_size(m);
+    size_t bytes = 0;
+    auto carve = [&](size_t b) { size_t o = bytes; bytes += (b + 255) / 256 * 256; return o; };
+    size_t oX = carve(sizeof(double2) * nsys * n), oB = carve(sizeof(double2) * nsys * n);
+    size_t oQ = carve(sizeof(double2) * nsys * qstride), oW = carve(sizeof(double2) * nsys * n);
+    size_t oP = carve(sizeof(double2) * nsys * cb * n_pad), oT = carve(sizeof(int) * nsys * rb);
+    size_t oS = carve(sizeof(double2) * nsys * small), oSt = carve(sizeof(GmState) * nsys);
+    size_t oN = carve(sizeof(double) * nsys * 1024 + sizeof(double) * nsys);
+    if (bytes > capacity) return bytes;
+    GmBatch& bt = ws.bt;
+    bt.nsys = nsys;
+    bt.n = n;
+    bt.n_pad = n_pad;
+    bt.m = m;
+    bt.A = A;
+    bt.lda = lda;
+    bt.mat_stride = mat_stride;
+    bt.ref_dotc = ref_dotc ? 1 : 0;
+    bt.qstride = qstride;
+    ws.fp32 = fp32;
+    ws.rb = rb;
+    ws.cb = cb;
+    char* base = static_cast<char*>(mem);
+    bt.X = reinterpret_cast<double2*>(base + oX);
+    bt.B = reinterpret_cast<double2*>(base + oB);
+    bt.Q = reinterpret_cast<double2*>(base + oQ);
+    bt.W = reinterpret_cast<double2*>(base + oW);
+    bt.part = reinterpret_cast<double2*>(base + oP);
+    bt.tickets = reinterpret_cast<int*>(base + oT);
+    bt.small = reinterpret_cast<double2*>(base + oS);
+    bt.small_stride = small;
+    bt.st = reinterpret_cast<GmState*>(base + oSt);
+    ws.norm_part = reinterpret_cast<double*>(base + oN);
+    ws.anorm = ws.norm_part + (size_t)nsys * 1024;
+    // the last-CTA tickets must start at zero; every other region is written
+    // before it is read
+    BEM_CUDA(cudaMemsetAsync(bt.tickets, 0, sizeof(int) * nsys * rb, ctx.stream));
+    ws.w_in_smem = (n * sizeof(double2) <= 200 * 1024);
+    if (ws.w_in_smem) {
+        BEM_CUDA(cudaFuncSetAttribute(gm_arnoldi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(n * sizeof(double2))));
+    }
+    return bytes;
+}
+
 void gm_matrix_norms(Context& ctx, GmWorkspace& ws) {
     const int nb = 512;
     dim3 grid(nb, ws.bt.nsys);

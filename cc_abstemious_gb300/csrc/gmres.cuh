@@ -79,6 +79,8 @@ struct GmWorkspace {
 
 void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const void* A, int64_t lda,
                 size_t mat_stride, bool fp32, bool ref_dotc);
+size_t gm_prepare_external(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const void* A, int64_t lda,
+                           size_t mat_stride, bool fp32, bool ref_dotc, void* mem, size_t capacity);
 void gm_matrix_norms(Context& ctx, GmWorkspace& ws);
 void gm_init(Context& ctx, GmWorkspace& ws, double tol, int64_t max_restarts);
 void gm_launch_iteration(Context& ctx, GmWorkspace& ws, cudaEvent_t ev_q0, cudaEvent_t ev_q1);

@@ -181,6 +181,20 @@ BEM_API bem_status bem_solve_lu(bem_ctx* ctx, int64_t n, const bem_cplx* A, int6
 BEM_API bem_status bem_gmres_solve(bem_ctx* ctx, int64_t n, const bem_cplx* A, int64_t lda,
                                    int64_t max_it, double tol, bem_cplx* x,
                                    bem_solve_report* report, bem_mem mem);
+/* No counterpart in the reference.  The dense GMRES of bem_gmres_solve, with A
+ * and x (in: b, out: solution) in device memory, that allocates no device
+ * memory: its working memory is a fixed 8 MiB array in the library's device
+ * image, held by every GPU that loads the library until the process exits.  For
+ * callers that cannot allocate device memory at solve time, such as
+ * applications that give all device memory to their own pool up front or run a
+ * fixed-budget loop, where a cudaMalloc would synchronise the device or fail.
+ * Limit: n up to 4096 at any iteration limit; sizes whose workspace exceeds the
+ * array are rejected with BEM_ERR_BAD_INPUT before any work is issued.  The
+ * first call on each device looks up the array's device address; make that
+ * first call before any stream capture.  Every call uses the same array, so
+ * calls that overlap on the GPU (other threads, other streams) race. */
+BEM_API bem_status bem_gmres_solve_noalloc(bem_ctx* ctx, int64_t n, const bem_cplx* A, int64_t lda,
+                                           int64_t max_it, double tol, bem_cplx* x, bem_solve_report* report);
 /* solve.rs:173-185 get_field: out = [phi_inc if Total] - M phi + L vn. */
 BEM_API bem_status bem_get_field(bem_ctx* ctx, const bem_problem* p, const bem_cplx* M,
                                  const bem_cplx* L, int64_t ld, const bem_cplx* phi,
