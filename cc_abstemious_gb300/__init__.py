@@ -440,3 +440,47 @@ class HMatrix:
                 self.h = None
         except Exception:
             pass
+
+
+# ---- learned preconditioner ------------------------------------------------------
+def learned_num_params():
+    return int(_lib.load().bem_learned_num_params())
+
+
+def learned_train(problems, steps=200, nprobe=8, lr=1e-3, seed=0, ctx=None):
+    """Train the context's preconditioner network on the operators of
+    `problems` (PreData, all their frequencies).  Returns the per-step losses
+    E ||A M z - z||^2 / ||z||^2."""
+    ctx = ctx or problems[0].ctx
+    arr = (C.c_void_p * len(problems))(*[p.h for p in problems])
+    losses = np.zeros(max(steps, 1))
+    ctx.check(ctx.lib.bem_learned_train(ctx.h, arr, len(problems), steps, nprobe, lr, seed, _ptr(losses)))
+    return losses[:steps]
+
+
+def learned_get_weights(ctx=None):
+    ctx = ctx or Context.default()
+    w = np.zeros(learned_num_params(), dtype=np.float32)
+    ctx.check(ctx.lib.bem_learned_get_weights(ctx.h, _ptr(w)))
+    return w
+
+
+def learned_set_weights(w, ctx=None):
+    ctx = ctx or Context.default()
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    ctx.check(ctx.lib.bem_learned_set_weights(ctx.h, _ptr(w)))
+
+
+def learned_mlp_eval(features, dO=None, ctx=None):
+    """Network outputs (P x 2) for P x 16 features and, with dO, the gradient of
+    sum(dO * outputs) with respect to the parameters."""
+    ctx = ctx or Context.default()
+    F = np.ascontiguousarray(features, dtype=np.float32)
+    P = F.shape[0]
+    out = np.zeros((P, 2), dtype=np.float32)
+    grad = None
+    if dO is not None:
+        dO = np.ascontiguousarray(dO, dtype=np.float32)
+        grad = np.zeros(learned_num_params(), dtype=np.float32)
+    ctx.check(ctx.lib.bem_learned_mlp_eval(ctx.h, P, _ptr(F), _ptr(dO), _ptr(out), _ptr(grad)))
+    return (out, grad) if dO is not None else out

@@ -82,6 +82,11 @@ SIGNATURES = {
     "bem_convert_to_pressure": (_i, [_vp, _d, _vp, _i64]),
     "bem_run": (_i, [_vp, _vp, _i, _i, _vp, _vp, C.POINTER(SolveReport), _i]),
     "bem_last_surface": (_i, [_vp, _vp, _vp, _vp]),
+    "bem_learned_train": (_i, [_vp, _vp, _i, _i, _i, _d, C.c_uint64, _vp]),
+    "bem_learned_num_params": (_i64, []),
+    "bem_learned_get_weights": (_i, [_vp, _vp]),
+    "bem_learned_set_weights": (_i, [_vp, _vp]),
+    "bem_learned_mlp_eval": (_i, [_vp, _i64, _vp, _vp, _vp, _vp]),
     "bem_hmatrix_build": (_i, [_vp, _vp, _i, _PP]),
     "bem_hmatrix_destroy": (None, [_vp]),
     "bem_hmatrix_gemv": (_i, [_vp, _vp, Cplx, _vp, Cplx, _vp]),

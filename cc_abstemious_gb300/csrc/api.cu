@@ -13,6 +13,7 @@
 #include "gmres.cuh"
 #include "hmatrix.cuh"
 #include "mixed.cuh"
+#include "precond.cuh"
 
 namespace bem {
 
@@ -681,6 +682,60 @@ BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* pp, bem_form form, bem_pre
             }
         }
         p.ifreq = saved;
+    });
+}
+
+BEM_API bem_status bem_learned_train(bem_ctx* ctx, bem_problem* const* problems, int nproblems, int steps,
+                                     int nprobe, double lr, uint64_t seed, double* losses) {
+    if (!ctx || !problems || nproblems < 1 || steps < 0 || nprobe < 1) return BEM_ERR_BAD_INPUT;
+    return guard(ctx, [&] {
+        set_device(ctx->c);
+        std::vector<Problem*> ps;
+        for (int i = 0; i < nproblems; ++i) {
+            require(problems[i] != nullptr, "null problem");
+            ps.push_back(&problems[i]->p);
+        }
+        std::vector<double> l;
+        learned_train(ctx->c, ps, steps, nprobe, lr, seed, l);
+        if (losses) std::memcpy(losses, l.data(), sizeof(double) * l.size());
+    });
+}
+
+BEM_API int64_t bem_learned_num_params(void) { return learned_num_params(); }
+
+BEM_API bem_status bem_learned_get_weights(bem_ctx* ctx, float* w) {
+    if (!ctx || !w) return BEM_ERR_BAD_INPUT;
+    return guard(ctx, [&] {
+        require(ctx->c.net && ctx->c.net->ready, "no network loaded");
+        set_device(ctx->c);
+        BEM_CUDA(cudaMemcpyAsync(w, ctx->c.net->w.p, sizeof(float) * learned_num_params(), cudaMemcpyDeviceToHost,
+                                 ctx->c.stream));
+        ctx->c.sync();
+    });
+}
+
+BEM_API bem_status bem_learned_set_weights(bem_ctx* ctx, const float* w) {
+    if (!ctx || !w) return BEM_ERR_BAD_INPUT;
+    return guard(ctx, [&] {
+        set_device(ctx->c);
+        if (!ctx->c.net) ctx->c.net = std::make_shared<LearnedNet>();
+        LearnedNet& net = *ctx->c.net;
+        if (!net.ready) net.init(ctx->c, 0);
+        net.w_host.assign(w, w + learned_num_params());
+        net.upload(ctx->c);
+        BEM_CUDA(cudaMemsetAsync(net.m1.p, 0, sizeof(float) * learned_num_params(), ctx->c.stream));
+        BEM_CUDA(cudaMemsetAsync(net.m2.p, 0, sizeof(float) * learned_num_params(), ctx->c.stream));
+        net.step = 0;
+        ctx->c.sync();
+    });
+}
+
+BEM_API bem_status bem_learned_mlp_eval(bem_ctx* ctx, int64_t P, const float* features, const float* dO, float* out,
+                                        float* grad) {
+    if (!ctx || P < 1 || !features) return BEM_ERR_BAD_INPUT;
+    return guard(ctx, [&] {
+        set_device(ctx->c);
+        learned_mlp_eval(ctx->c, P, features, dO, out, grad);
     });
 }
 

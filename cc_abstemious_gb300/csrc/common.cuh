@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <cstdio>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -141,9 +142,12 @@ struct Stage {
     double bytes = 0;
 };
 
+struct LearnedNet;
+
 struct Context {
     int device = 0;
     bool profiling = false;
+    std::shared_ptr<LearnedNet> net;  // preconditioner network (trained or loaded)
     std::vector<Stage> stages;
     void stage_add(const std::string& name, double ms, int64_t launches, double bytes) {
         for (auto& s : stages)

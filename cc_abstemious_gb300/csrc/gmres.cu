@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
     // so its residual is b itself: no product needed
     if (mode == MV_START && !bt.ref_dotc && st.restarts == 0) return;
     const int64_t n = bt.n;
-    const double2* v = (mode == MV_Q) ? bt.Q + (size_t)s * bt.qstride + (size_t)st.k * n : bt.X + (size_t)s * n;
+    const double2* kv = bt.Z ? bt.Z : bt.Q;  // right preconditioning applies A to M q_k
+    const double2* v = (mode == MV_Q) ? kv + (size_t)s * bt.qstride + (size_t)st.k * n : bt.X + (size_t)s * n;
     __shared__ float2 xh[MV_COLS], xl[MV_COLS];
     __shared__ double2 xd[MV_COLS];
     __shared__ int last;
@@ -356,10 +357,12 @@ __global__ void __launch_bounds__(AR_THREADS) gm_arnoldi_kernel(GmBatch bt, int 
     }
     __syncthreads();
     if (hsh.x != 0.0) {
+        // x += Q_k y, or Z_k y with flexible right preconditioning
         double2* x = bt.X + (size_t)s * n;
+        const double2* Zs = bt.Z ? bt.Z + (size_t)s * bt.qstride : Q;
         for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
             double2 a = x[l];
-            for (int j = 0; j <= k; ++j) cfma(a, Q[(size_t)j * n + l], sm.y[j]);
+            for (int j = 0; j <= k; ++j) cfma(a, Zs[(size_t)j * n + l], sm.y[j]);
             x[l] = a;
         }
     }
@@ -609,6 +612,7 @@ void gm_launch_iteration(Context& ctx, GmWorkspace& ws, cudaEvent_t ev_q0, cudaE
     gm_start_kernel<<<nsys, AR_THREADS, 0, ctx.stream>>>(ws.bt);
     BEM_CHECK_LAUNCH(&ctx);
     if (ev_q0) BEM_CUDA(cudaEventRecord(ev_q0, ctx.stream));
+    if (ws.precond) ws.precond(ctx, ws, MV_Q, ws.precond_user);
     launch_apply(ctx, ws, MV_Q);
     if (ev_q1) BEM_CUDA(cudaEventRecord(ev_q1, ctx.stream));
     size_t dyn = ws.w_in_smem ? (size_t)ws.bt.n * sizeof(double2) : 0;

@@ -25,6 +25,7 @@ struct GmBatch {
     int* tickets;       // last-CTA counters
     double2* small;     // per-system Hessenberg / rotations
     GmState* st;
+    double2* Z;         // flexible right preconditioning: Z[:, k] = M Q[:, k] (nullptr: none)
 };
 
 // Whether the operator application of `mode` has work for a system.
@@ -65,6 +66,12 @@ struct GmWorkspace {
     GmBatch bt{};
     GmApplyHook hook = nullptr;
     void* hook_user = nullptr;
+    // Preconditioner hook: launches Z_s[:, k] = M_s Q_s[:, k] for the systems
+    // whose Krylov step is pending (same predicate as the MV_Q apply).
+    GmApplyHook precond = nullptr;
+    void* precond_user = nullptr;
+    std::shared_ptr<void> precond_keep;  // owns the preconditioner data
+    DevBuf zmem;
     DevBuf mem;
     bool fp32 = false;
     bool w_in_smem = false;

@@ -96,6 +96,42 @@ void block_leaves(const ClNode& r, const ClNode& c, double eta,
 }
 }  // namespace
 
+static void collect_leaves(const ClNode& c, std::vector<LeafCluster>& out) {
+    if (c.leaf()) {
+        LeafCluster l;
+        l.idx = c.idx;
+        for (int d = 0; d < 3; ++d) {
+            l.lo[d] = c.lo[d];
+            l.hi[d] = c.hi[d];
+        }
+        l.diam = c.diam;
+        out.push_back(std::move(l));
+        return;
+    }
+    collect_leaves(*c.son[0], out);
+    collect_leaves(*c.son[1], out);
+}
+
+std::vector<LeafCluster> cluster_leaves(const std::vector<double>& pts, int64_t stride, int64_t leaf) {
+    const int64_t n = (int64_t)pts.size() / stride;
+    std::vector<int64_t> idx((size_t)n);
+    for (int64_t i = 0; i < n; ++i) idx[(size_t)i] = i;
+    auto root = build_cluster(pts, stride, idx, leaf, 0);
+    std::vector<LeafCluster> out;
+    collect_leaves(*root, out);
+    return out;
+}
+
+double box_distance(const LeafCluster& a, const LeafCluster& b) {
+    double s = 0;
+    for (int d = 0; d < 3; ++d) {
+        double t1 = std::fmax(0.0, a.lo[d] - b.hi[d]);
+        double t2 = std::fmax(0.0, b.lo[d] - a.hi[d]);
+        s += t1 * t1 + t2 * t2;
+    }
+    return std::sqrt(s);
+}
+
 // Leaf descriptor shared with the kernels.
 struct HLeaf {
     int64_t row_off, m;   // into rows[]

@@ -162,7 +162,7 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
         EventTimer t(c);
         gm_init(c, ws, tol, restarts);
         if (precond != BEM_PRECOND_NONE)
-            precond_setup(c, p, ws, precond, ks.data());
+            precond = precond_setup(c, p, ws, precond, ks.data());
         gm_run(c, ws, c.profiling ? 0 : 4, restarts * (int64_t)m + 1);
         gm_read_states(c, ws, st);
         int64_t mv = 0;

@@ -1,12 +1,842 @@
-// Preconditioners for the batched GMRES.
+// Preconditioners for the batched GMRES (flexible right preconditioning,
+// Z[:, k] = M Q[:, k]).
+//
+// The unknowns are grouped by the leaves of the cluster tree (bounding-box
+// bisection of cluster.rs, leaf size 64).  Two leaves are "near" when the
+// block-tree admissibility test min(diam) <= eta * dist fails for them.
+//
+//  * Block-Jacobi: M = blockdiag(A_cc)^-1, the exact inverse of every diagonal
+//    leaf block (Gauss-Jordan with partial pivoting, one CTA per block).
+//  * Learned: M = blockdiag(A_cc)^-1 + C, where C lives on the near
+//    off-diagonal leaf blocks and every entry C_ij is emitted by a 3-layer MLP
+//    (16 -> 128 -> 128 -> 2, tanh, width 128) from geometry only: the pair's
+//    separation scaled by the element size, both normals, the area ratio, k h
+//    and the phase k r.  C_ij = s_ij (o_1 + i o_2) with s_ij = wa_j / (4 pi r).
+//    Weights and activations are rounded to BF16, products accumulate in
+//    FP32.  The network is trained on the GPU on operators the BEM assembles,
+//    minimising E_z ||A M z - z||^2 / ||z||^2 over random probes z, with
+//    hand-written forward / backward kernels and Adam.  The block-Jacobi part
+//    is always present, so an untrained (zero) correction is block-Jacobi.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <random>
+
 #include "common.cuh"
+#include "complex.cuh"
+#include "gmres.cuh"
+#include "hmatrix.cuh"
 #include "precond.cuh"
 
 namespace bem {
 
-void precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks) {
-    (void)c; (void)p; (void)ws; (void)ks;
-    throw Error(BEM_ERR_BAD_INPUT, "preconditioner " + std::to_string((int)kind) + " is not available");
+constexpr int PC_LEAF = 64;
+constexpr double PC_ETA = 2.0;
+
+// ---------------------------------------------------------------------------
+// Near-field leaf pattern (host).
+void build_pattern(const Problem& p, NearPattern& P) {
+    auto leaves = cluster_leaves(p.cpts, 8, PC_LEAF);
+    P.n = p.n;
+    P.nc = (int)leaves.size();
+    P.cl_off.assign(1, 0);
+    P.cl_idx.clear();
+    for (auto& l : leaves) {
+        P.cl_idx.insert(P.cl_idx.end(), l.idx.begin(), l.idx.end());
+        P.cl_off.push_back((int64_t)P.cl_idx.size());
+    }
+    P.nb_off.assign(1, 0);
+    P.nb_d.clear();
+    P.nb_blk.clear();
+    int64_t entries = 0;
+    P.pair_i.clear();
+    P.pair_j.clear();
+    P.pair_dst.clear();
+    for (int c = 0; c < P.nc; ++c) {
+        std::vector<int> near{c};
+        for (int d = 0; d < P.nc; ++d) {
+            if (d == c) continue;
+            bool adm = std::fmin(leaves[c].diam, leaves[d].diam) <= PC_ETA * box_distance(leaves[c], leaves[d]);
+            if (!adm) near.push_back(d);
+        }
+        const int64_t bc = P.cl_off[c + 1] - P.cl_off[c];
+        for (int d : near) {
+            const int64_t bd = P.cl_off[d + 1] - P.cl_off[d];
+            P.nb_d.push_back(d);
+            P.nb_blk.push_back(entries);
+            if (d != c) {
+                for (int64_t jj = 0; jj < bd; ++jj)
+                    for (int64_t ii = 0; ii < bc; ++ii) {
+                        P.pair_i.push_back((int32_t)P.cl_idx[(size_t)(P.cl_off[c] + ii)]);
+                        P.pair_j.push_back((int32_t)P.cl_idx[(size_t)(P.cl_off[d] + jj)]);
+                        P.pair_dst.push_back(entries + jj * bc + ii);
+                    }
+            }
+            entries += bc * bd;
+        }
+        P.nb_off.push_back((int32_t)P.nb_d.size());
+    }
+    P.entries = entries;
+    P.npairs = (int64_t)P.pair_i.size();
+}
+
+// ---------------------------------------------------------------------------
+// Exact inverse of every diagonal leaf block, [A_cc | I] reduced by
+// Gauss-Jordan with partial pivoting in FP32, one CTA per (block, system).
+template <typename T>
+__global__ void __launch_bounds__(256) pc_diag_inverse_kernel(const T* __restrict__ A, int64_t lda, size_t mstride,
+                                                              const int64_t* __restrict__ cl_off,
+                                                              const int64_t* __restrict__ cl_idx,
+                                                              const int32_t* __restrict__ nb_off,
+                                                              const int64_t* __restrict__ nb_blk,
+                                                              float2* __restrict__ M, size_t Mstride) {
+    extern __shared__ float2 aug[];  // b x 2b, row-major
+    __shared__ int s_piv;
+    __shared__ float2 fcol[PC_LEAF];  // elimination factors of the current column
+    const int c = blockIdx.x, s = blockIdx.y;
+    const int64_t o = cl_off[c];
+    const int b = (int)(cl_off[c + 1] - o);
+    const int w = 2 * b;
+    const T* As = A + (size_t)s * mstride;
+    for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
+        int i = t % b, j = t / b;
+        T v = As[cl_idx[o + j] * lda + cl_idx[o + i]];
+        aug[i * w + j] = make_float2((float)v.x, (float)v.y);
+        aug[i * w + b + j] = make_float2(i == j ? 1.f : 0.f, 0.f);
+    }
+    __syncthreads();
+    for (int col = 0; col < b; ++col) {
+        if (threadIdx.x == 0) {
+            int best = col;
+            float bv = -1.f;
+            for (int r = col; r < b; ++r) {
+                float v = fabsf(aug[r * w + col].x) + fabsf(aug[r * w + col].y);
+                if (v > bv) { bv = v; best = r; }
+            }
+            s_piv = best;
+        }
+        __syncthreads();
+        const int pr = s_piv;
+        if (pr != col)
+            for (int t = threadIdx.x; t < w; t += blockDim.x) {
+                float2 a = aug[col * w + t];
+                aug[col * w + t] = aug[pr * w + t];
+                aug[pr * w + t] = a;
+            }
+        __syncthreads();
+        const float2 d = aug[col * w + col];
+        const float dn = d.x * d.x + d.y * d.y;
+        const float2 inv = dn > 0.f ? make_float2(d.x / dn, -d.y / dn) : make_float2(0.f, 0.f);
+        __syncthreads();
+        for (int t = threadIdx.x; t < w; t += blockDim.x) aug[col * w + t] = fmul(aug[col * w + t], inv);
+        for (int r = threadIdx.x; r < b; r += blockDim.x) fcol[r] = aug[r * w + col];
+        __syncthreads();
+        for (int t = threadIdx.x; t < b * w; t += blockDim.x) {
+            int r = t / w, j = t % w;
+            if (r == col) continue;
+            float2 f = fcol[r];
+            float2 v = aug[r * w + j];
+            float2 u = aug[col * w + j];
+            aug[r * w + j] = make_float2(v.x - (f.x * u.x - f.y * u.y), v.y - (f.x * u.y + f.y * u.x));
+        }
+        __syncthreads();
+        // the pivot column of the other rows was consumed; zero it for clarity
+    }
+    float2* Mo = M + (size_t)s * Mstride + nb_blk[nb_off[c]];  // first neighbour is the block itself
+    for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
+        int i = t % b, j = t / b;
+        Mo[(size_t)j * b + i] = aug[i * w + b + j];
+    }
+}
+
+// z[rows of c] = sum over near d of M_cd q[rows of d]; one CTA per (leaf, system).
+__device__ __forceinline__ void pc_block_apply(int c, const int64_t* cl_off, const int64_t* cl_idx,
+                                               const int32_t* nb_off, const int32_t* nb_d, const int64_t* nb_blk,
+                                               const float2* Ms, const double2* q, double2* z, int use_offdiag) {
+    __shared__ double2 qs[PC_LEAF];
+    const int64_t oc = cl_off[c];
+    const int bc = (int)(cl_off[c + 1] - oc);
+    double2 acc = make_double2(0, 0);
+    const int i = threadIdx.x;
+    const int nend = use_offdiag ? nb_off[c + 1] : nb_off[c] + 1;
+    for (int t = nb_off[c]; t < nend; ++t) {
+        const int d = nb_d[t];
+        const int64_t od = cl_off[d];
+        const int bd = (int)(cl_off[d + 1] - od);
+        __syncthreads();
+        if (i < bd) qs[i] = q[cl_idx[od + i]];
+        __syncthreads();
+        if (i < bc) {
+            const float2* blk = Ms + nb_blk[t];
+            for (int j = 0; j < bd; ++j) {
+                float2 m = blk[(size_t)j * bc + i];
+                cfma(acc, make_double2(m.x, m.y), qs[j]);
+            }
+        }
+    }
+    if (i < bc) z[cl_idx[oc + i]] = acc;
+}
+
+struct PcDev {
+    const int64_t *cl_off, *cl_idx, *nb_blk;
+    const int32_t *nb_off, *nb_d;
+    const float2* M;
+    size_t Mstride;
+    int offdiag;
+};
+
+__global__ void __launch_bounds__(PC_LEAF) pc_apply_gmres_kernel(PcDev pc, GmBatch bt) {
+    const int s = blockIdx.y;
+    const GmState& st = bt.st[s];
+    if (!gm_apply_active(bt, st, MV_Q)) return;
+    const double2* q = bt.Q + (size_t)s * bt.qstride + (size_t)st.k * bt.n;
+    double2* z = bt.Z + (size_t)s * bt.qstride + (size_t)st.k * bt.n;
+    pc_block_apply(blockIdx.x, pc.cl_off, pc.cl_idx, pc.nb_off, pc.nb_d, pc.nb_blk, pc.M + (size_t)s * pc.Mstride, q,
+                   z, pc.offdiag);
+}
+
+// Probe form: Y[:, q] = M_s Z[:, q] for nprobe vectors (training).
+__global__ void __launch_bounds__(PC_LEAF) pc_apply_probes_kernel(PcDev pc, int s, const double2* __restrict__ Zp,
+                                                                  double2* __restrict__ Yp, int64_t n) {
+    const int q = blockIdx.y;
+    pc_block_apply(blockIdx.x, pc.cl_off, pc.cl_idx, pc.nb_off, pc.nb_d, pc.nb_blk, pc.M + (size_t)s * pc.Mstride,
+                   Zp + (size_t)q * n, Yp + (size_t)q * n, pc.offdiag);
+}
+
+// ---------------------------------------------------------------------------
+// MLP.  Parameters (FP32 master copy): W1 [128][16], b1 [128], W2 [128][128],
+// b2 [128], W3 [2][128], b3 [2].
+constexpr int NF = 16, NH = 128, NO = 2;
+constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH * NF, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH,
+              OFF_W3 = OFF_B2 + NH, OFF_B3 = OFF_W3 + NO * NH, NPARAM = OFF_B3 + NO;
+
+__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16(x)); }
+__device__ __forceinline__ float tanh_act(float x) { return tanhf(x); }
+
+// Pair features (geometry and ka only) and the output scale.
+__global__ void pc_features_kernel(int64_t P, const int32_t* __restrict__ pi, const int32_t* __restrict__ pj,
+                                   int64_t npad, const double* __restrict__ geo, double k, float* __restrict__ F,
+                                   float* __restrict__ scale) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int64_t i = pi[p], j = pj[p];
+    double dx = geo[GX * npad + j] - geo[GX * npad + i], dy = geo[GY * npad + j] - geo[GY * npad + i],
+           dz = geo[GZ * npad + j] - geo[GZ * npad + i];
+    double r = sqrt(dx * dx + dy * dy + dz * dz);
+    double ai = geo[GAREA * npad + i], aj = geo[GAREA * npad + j];
+    double h = sqrt(ai);
+    double kr = k * r;
+    float* f = F + p * NF;
+    f[0] = (float)(dx / h);
+    f[1] = (float)(dy / h);
+    f[2] = (float)(dz / h);
+    f[3] = (float)(r / h);
+    f[4] = (float)geo[GNX * npad + i];
+    f[5] = (float)geo[GNY * npad + i];
+    f[6] = (float)geo[GNZ * npad + i];
+    f[7] = (float)geo[GNX * npad + j];
+    f[8] = (float)geo[GNY * npad + j];
+    f[9] = (float)geo[GNZ * npad + j];
+    f[10] = (float)(aj / ai);
+    f[11] = (float)(k * h);
+    f[12] = (float)cos(kr);
+    f[13] = (float)sin(kr);
+    f[14] = (float)(h / r);
+    f[15] = 1.0f;
+    for (int t = 0; t < NF; ++t) f[t] = bf16r(f[t]);
+    scale[p] = (float)(geo[GWA * npad + j] / (4.0 * 3.14159265358979323846 * r));
+}
+
+// C = act(op(A) op(B) + bias) (+ C when accumulate).  Row-major storage;
+// op(A): M x K stored [M][K] (TA = 0) or [K][M] (TA = 1); op(B): K x N stored
+// [K][N] (TB = 0) or [N][K] (TB = 1).  128 x 128 tile, 8 x 8 per thread,
+// FP32 accumulation.  With split > 1 the K range is split over gridDim.z and
+// the results are added atomically (weight gradients).
+constexpr int GB_M = 128, GB_N = 128, GB_K = 8;
+template <int TA, int TB>
+__global__ void __launch_bounds__(256) mlp_gemm_kernel(int64_t M, int64_t N, int64_t K, const float* __restrict__ A,
+                                                       const float* __restrict__ B, float* __restrict__ C,
+                                                       const float* __restrict__ bias, int act, int round_bf16,
+                                                       int atomic) {
+    __shared__ float As[GB_K][GB_M + 4];
+    __shared__ float Bs[GB_K][GB_N + 4];
+    const int64_t m0 = (int64_t)blockIdx.x * GB_M, n0 = (int64_t)blockIdx.y * GB_N;
+    const int64_t kchunk = (K + gridDim.z - 1) / gridDim.z;
+    const int64_t kb = (int64_t)blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+    const int tr = threadIdx.x / 16, tc = threadIdx.x % 16;
+    float acc[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+    for (int64_t k0 = kb; k0 < ke; k0 += GB_K) {
+        for (int t = threadIdx.x; t < GB_K * GB_M; t += 256) {
+            int kk = TA ? t / GB_M : t % GB_K, mm = TA ? t % GB_M : t / GB_K;
+            int64_t gm = m0 + mm, gk = k0 + kk;
+            float v = 0.f;
+            if (gm < M && gk < ke) v = TA ? A[gk * M + gm] : A[gm * K + gk];
+            As[kk][mm] = v;
+        }
+        for (int t = threadIdx.x; t < GB_K * GB_N; t += 256) {
+            int kk = TB ? t % GB_K : t / GB_N, nn = TB ? t / GB_K : t % GB_N;
+            int64_t gn = n0 + nn, gk = k0 + kk;
+            float v = 0.f;
+            if (gn < N && gk < ke) v = TB ? B[gn * K + gk] : B[gk * N + gn];
+            Bs[kk][nn] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GB_K; ++kk) {
+            float av[8], bv[8];
+#pragma unroll
+            for (int a = 0; a < 8; ++a) av[a] = As[kk][tr + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) bv[b] = Bs[kk][tc + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        const int64_t gm = m0 + tr + 16 * a;
+        if (gm >= M) continue;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            const int64_t gn = n0 + tc + 16 * b;
+            if (gn >= N) continue;
+            float v = acc[a][b];
+            if (atomic) {
+                atomicAdd(&C[gm * N + gn], v);
+                continue;
+            }
+            if (bias) v += bias[gn];
+            if (act == 1) v = tanh_act(v);
+            if (round_bf16) v = bf16r(v);
+            C[gm * N + gn] = v;
+        }
+    }
+}
+
+template <int TA, int TB>
+static void gemm(Context& c, int64_t M, int64_t N, int64_t K, const float* A, const float* B, float* C,
+                 const float* bias, int act, int round_bf16, int split = 1) {
+    dim3 grid((unsigned)((M + GB_M - 1) / GB_M), (unsigned)((N + GB_N - 1) / GB_N), (unsigned)split);
+    mlp_gemm_kernel<TA, TB><<<grid, 256, 0, c.stream>>>(M, N, K, A, B, C, bias, act, round_bf16, split > 1 ? 1 : 0);
+    BEM_CHECK_LAUNCH(&c);
+}
+
+// BF16 copy of the weights (kept as FP32 values) used by the forward pass.
+__global__ void round_params_kernel(int n, const float* __restrict__ w, float* __restrict__ wb) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) wb[t] = bf16r(w[t]);
+}
+
+// Learned entries into the block storage of one system.
+__global__ void pc_write_learned_kernel(int64_t P, const float* __restrict__ O, const float* __restrict__ scale,
+                                        const int64_t* __restrict__ dst, float2* __restrict__ M) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    M[dst[p]] = make_float2(scale[p] * O[2 * p], scale[p] * O[2 * p + 1]);
+}
+
+void mlp_forward(Context& c, const LearnedNet& net, int64_t P, const float* F, float* H1, float* H2, float* O) {
+    const float* wb = net.wbf.as<float>();
+    gemm<0, 1>(c, P, NH, NF, F, wb + OFF_W1, H1, wb + OFF_B1, 1, 1);
+    gemm<0, 1>(c, P, NH, NH, H1, wb + OFF_W2, H2, wb + OFF_B2, 1, 1);
+    gemm<0, 1>(c, P, NO, NH, H2, wb + OFF_W3, O, wb + OFF_B3, 0, 0);
+}
+
+// ---------------------------------------------------------------------------
+// Training kernels.
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return x;
+}
+
+// Complex Gaussian probes (Box-Muller on a counter hash).
+__global__ void probes_kernel(int64_t total, uint64_t seed, double2* __restrict__ Z) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    uint64_t a = mix64(seed ^ (2 * (uint64_t)t + 1)), b = mix64(seed + 0x9E3779B97F4A7C15ULL * (uint64_t)(t + 7));
+    double u1 = ((a >> 11) + 1) * (1.0 / 9007199254740993.0), u2 = (b >> 11) * (1.0 / 9007199254740992.0);
+    double rr = sqrt(-2.0 * log(u1));
+    Z[t] = make_double2(rr * cos(6.283185307179586 * u2), rr * sin(6.283185307179586 * u2));
+}
+
+// Y[:, q] = A X[:, q] (conj = 0) or A^H X[:, q] (conj = 1), FP32 operator,
+// column-major with leading dimension lda.  One CTA per (row block or column, probe).
+__global__ void probe_matvec_kernel(int64_t n, const float2* __restrict__ A, int64_t lda, const double2* __restrict__ X,
+                                    double2* __restrict__ Y, int conj) {
+    const int q = blockIdx.y;
+    const double2* x = X + (size_t)q * n;
+    double2* y = Y + (size_t)q * n;
+    if (!conj) {
+        int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+        if (i >= n) return;
+        double2 acc = make_double2(0, 0);
+        for (int64_t j = 0; j < n; ++j) {
+            float2 a = A[j * lda + i];
+            cfma(acc, make_double2(a.x, a.y), x[j]);
+        }
+        y[i] = acc;
+    } else {
+        // y_j = sum_i conj(A_ij) x_i: one warp per column j
+        int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32;
+        int lane = threadIdx.x & 31;
+        if (j >= n) return;
+        double ax = 0, ay = 0;
+        for (int64_t i = lane; i < n; i += 32) {
+            float2 a = A[j * lda + i];
+            double2 v = x[i];
+            ax += a.x * v.x + a.y * v.y;
+            ay += a.x * v.y - a.y * v.x;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            ax += __shfl_down_sync(0xffffffffu, ax, o);
+            ay += __shfl_down_sync(0xffffffffu, ay, o);
+        }
+        if (lane == 0) y[j] = make_double2(ax, ay);
+    }
+}
+
+// R = W - Z, per-probe |R|^2 and |Z|^2 partials (loss).
+__global__ void probe_residual_kernel(int64_t total, const double2* __restrict__ W, const double2* __restrict__ Z,
+                                      double2* __restrict__ R, double* __restrict__ acc) {
+    __shared__ double sr[256], sz[256];
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double a = 0, b = 0;
+    if (t < total) {
+        double2 r = csub(W[t], Z[t]);
+        R[t] = r;
+        a = r.x * r.x + r.y * r.y;
+        b = Z[t].x * Z[t].x + Z[t].y * Z[t].y;
+    }
+    sr[threadIdx.x] = a;
+    sz[threadIdx.x] = b;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            sr[threadIdx.x] += sr[threadIdx.x + o];
+            sz[threadIdx.x] += sz[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(&acc[0], sr[0]);
+        atomicAdd(&acc[1], sz[0]);
+    }
+}
+
+// dL/d(o1, o2) of every pair: 2 s (Re, Im) sum_q G_iq conj(Z_jq) / sum |Z|^2.
+__global__ void pair_grad_kernel(int64_t P, int nprobe, int64_t n, const int32_t* __restrict__ pi,
+                                 const int32_t* __restrict__ pj, const float* __restrict__ scale,
+                                 const double2* __restrict__ G, const double2* __restrict__ Z,
+                                 const double* __restrict__ acc, float* __restrict__ dO) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int64_t i = pi[p], j = pj[p];
+    double re = 0, im = 0;
+    for (int q = 0; q < nprobe; ++q) {
+        double2 g = G[(size_t)q * n + i], z = Z[(size_t)q * n + j];
+        re += g.x * z.x + g.y * z.y;
+        im += g.y * z.x - g.x * z.y;
+    }
+    const double f = 2.0 * scale[p] / acc[1];
+    dO[2 * p] = (float)(f * re);
+    dO[2 * p + 1] = (float)(f * im);
+}
+
+// D = D * (1 - H^2) (tanh derivative).
+__global__ void tanh_back_kernel(int64_t total, const float* __restrict__ H, float* __restrict__ D) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < total) D[t] *= 1.f - H[t] * H[t];
+}
+
+// Column sums (bias gradients): out[c] += sum_r D[r][c].
+__global__ void colsum_kernel(int64_t rows, int cols, const float* __restrict__ D, float* __restrict__ out) {
+    __shared__ float sh[256];
+    const int c = blockIdx.x;
+    float s = 0.f;
+    for (int64_t r = blockIdx.y * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.y * blockDim.x)
+        s += D[r * cols + c];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(&out[c], sh[0]);
+}
+
+__global__ void adam_kernel(int n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m1,
+                            float* __restrict__ m2, float lr, float b1, float b2, float c1, float c2, float eps) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    float gg = g[t];
+    float a = b1 * m1[t] + (1.f - b1) * gg;
+    float b = b2 * m2[t] + (1.f - b2) * gg * gg;
+    m1[t] = a;
+    m2[t] = b;
+    w[t] -= lr * (a / c1) / (sqrtf(b / c2) + eps);
+}
+
+// Backward through the MLP from dO (P x 2) to the parameter gradients (added to grad).
+void mlp_backward(Context& c, const LearnedNet& net, int64_t P, const float* F, const float* H1, const float* H2,
+                  const float* dO, float* D2, float* D1, float* grad) {
+    const float* wb = net.wbf.as<float>();
+    const int split = (int)std::min<int64_t>(256, std::max<int64_t>(1, P / 4096));
+    // layer 3
+    gemm<1, 0>(c, NO, NH, P, dO, H2, grad + OFF_W3, nullptr, 0, 0, split);
+    colsum_kernel<<<dim3(NO, 64), 256, 0, c.stream>>>(P, NO, dO, grad + OFF_B3);
+    BEM_CHECK_LAUNCH(&c);
+    gemm<0, 0>(c, P, NH, NO, dO, wb + OFF_W3, D2, nullptr, 0, 0);
+    tanh_back_kernel<<<(unsigned)((P * NH + 255) / 256), 256, 0, c.stream>>>(P * NH, H2, D2);
+    BEM_CHECK_LAUNCH(&c);
+    // layer 2
+    gemm<1, 0>(c, NH, NH, P, D2, H1, grad + OFF_W2, nullptr, 0, 0, split);
+    colsum_kernel<<<dim3(NH, 16), 256, 0, c.stream>>>(P, NH, D2, grad + OFF_B2);
+    BEM_CHECK_LAUNCH(&c);
+    gemm<0, 0>(c, P, NH, NH, D2, wb + OFF_W2, D1, nullptr, 0, 0);
+    tanh_back_kernel<<<(unsigned)((P * NH + 255) / 256), 256, 0, c.stream>>>(P * NH, H1, D1);
+    BEM_CHECK_LAUNCH(&c);
+    // layer 1
+    gemm<1, 0>(c, NH, NF, P, D1, F, grad + OFF_W1, nullptr, 0, 0, split);
+    colsum_kernel<<<dim3(NH, 16), 256, 0, c.stream>>>(P, NH, D1, grad + OFF_B1);
+    BEM_CHECK_LAUNCH(&c);
+}
+
+void LearnedNet::init(Context& c, uint64_t seed) {
+    std::vector<float> w(NPARAM, 0.f);
+    std::mt19937_64 g(seed);
+    auto fill = [&](int off, int fan_out, int fan_in, float gain) {
+        std::normal_distribution<float> nd(0.f, gain / std::sqrt((float)fan_in));
+        for (int t = 0; t < fan_out * fan_in; ++t) w[(size_t)(off + t)] = nd(g);
+    };
+    fill(OFF_W1, NH, NF, 1.0f);
+    fill(OFF_W2, NH, NH, 1.0f);
+    // the output layer starts at zero: an untrained network adds nothing to block-Jacobi
+    w_host = w;
+    upload(c);
+    m1.ensure(sizeof(float) * NPARAM);
+    m2.ensure(sizeof(float) * NPARAM);
+    BEM_CUDA(cudaMemsetAsync(m1.p, 0, sizeof(float) * NPARAM, c.stream));
+    BEM_CUDA(cudaMemsetAsync(m2.p, 0, sizeof(float) * NPARAM, c.stream));
+    step = 0;
+    ready = true;
+}
+
+void LearnedNet::upload(Context& c) {
+    w.ensure(sizeof(float) * NPARAM);
+    wbf.ensure(sizeof(float) * NPARAM);
+    BEM_CUDA(cudaMemcpyAsync(w.p, w_host.data(), sizeof(float) * NPARAM, cudaMemcpyHostToDevice, c.stream));
+    refresh(c);
+}
+
+void LearnedNet::refresh(Context& c) {
+    round_params_kernel<<<(NPARAM + 255) / 256, 256, 0, c.stream>>>(NPARAM, w.as<float>(), wbf.as<float>());
+    BEM_CHECK_LAUNCH(&c);
+}
+
+int learned_num_params() { return NPARAM; }
+
+// ---------------------------------------------------------------------------
+// Preconditioner data of a batch (one body, nsys frequencies).
+struct PcData {
+    NearPattern pat;
+    DevBuf cl_off, cl_idx, nb_off, nb_d, nb_blk, M;
+    bool offdiag = false;
+    PcDev dev(int use_off) const {
+        PcDev d;
+        d.cl_off = cl_off.as<int64_t>();
+        d.cl_idx = cl_idx.as<int64_t>();
+        d.nb_blk = nb_blk.as<int64_t>();
+        d.nb_off = nb_off.as<int32_t>();
+        d.nb_d = nb_d.as<int32_t>();
+        d.M = M.as<float2>();
+        d.Mstride = (size_t)pat.entries;
+        d.offdiag = use_off;
+        return d;
+    }
+};
+
+static void upload_pattern(Context& c, PcData& d) {
+    auto up = [&](DevBuf& b, const void* h, size_t bytes) {
+        b.ensure(bytes ? bytes : 16);
+        if (bytes) BEM_CUDA(cudaMemcpyAsync(b.p, h, bytes, cudaMemcpyHostToDevice, c.stream));
+    };
+    up(d.cl_off, d.pat.cl_off.data(), sizeof(int64_t) * d.pat.cl_off.size());
+    up(d.cl_idx, d.pat.cl_idx.data(), sizeof(int64_t) * d.pat.cl_idx.size());
+    up(d.nb_off, d.pat.nb_off.data(), sizeof(int32_t) * d.pat.nb_off.size());
+    up(d.nb_d, d.pat.nb_d.data(), sizeof(int32_t) * d.pat.nb_d.size());
+    up(d.nb_blk, d.pat.nb_blk.data(), sizeof(int64_t) * d.pat.nb_blk.size());
+}
+
+// Block-Jacobi inverses of every system of a batch into d.M.
+static void diag_inverses(Context& c, PcData& d, int nsys, const void* A, bool fp32, int64_t lda, size_t mstride) {
+    d.M.ensure(sizeof(float2) * (size_t)d.pat.entries * nsys);
+    BEM_CUDA(cudaMemsetAsync(d.M.p, 0, sizeof(float2) * (size_t)d.pat.entries * nsys, c.stream));
+    int bmax = 0;
+    for (int cc = 0; cc < d.pat.nc; ++cc)
+        bmax = std::max(bmax, (int)(d.pat.cl_off[cc + 1] - d.pat.cl_off[cc]));
+    size_t smem = sizeof(float2) * (size_t)bmax * 2 * bmax;
+    dim3 grid((unsigned)d.pat.nc, (unsigned)nsys);
+    if (fp32) {
+        BEM_CUDA(cudaFuncSetAttribute(pc_diag_inverse_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        pc_diag_inverse_kernel<float2><<<grid, 256, smem, c.stream>>>(
+            static_cast<const float2*>(A), lda, mstride, d.cl_off.as<int64_t>(), d.cl_idx.as<int64_t>(),
+            d.nb_off.as<int32_t>(), d.nb_blk.as<int64_t>(), d.M.as<float2>(), (size_t)d.pat.entries);
+    } else {
+        BEM_CUDA(cudaFuncSetAttribute(pc_diag_inverse_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        pc_diag_inverse_kernel<double2><<<grid, 256, smem, c.stream>>>(
+            static_cast<const double2*>(A), lda, mstride, d.cl_off.as<int64_t>(), d.cl_idx.as<int64_t>(),
+            d.nb_off.as<int32_t>(), d.nb_blk.as<int64_t>(), d.M.as<float2>(), (size_t)d.pat.entries);
+    }
+    BEM_CHECK_LAUNCH(&c);
+}
+
+// Learned off-diagonal entries of system s (wavenumber k) into d.M.
+struct PairBufs {
+    DevBuf pi, pj, dst, F, scale, H1, H2, O;
+};
+
+static void upload_pairs(Context& c, const NearPattern& pat, PairBufs& b) {
+    const int64_t P = std::max<int64_t>(pat.npairs, 1);
+    b.pi.ensure(sizeof(int32_t) * P);
+    b.pj.ensure(sizeof(int32_t) * P);
+    b.dst.ensure(sizeof(int64_t) * P);
+    if (pat.npairs) {
+        BEM_CUDA(cudaMemcpyAsync(b.pi.p, pat.pair_i.data(), sizeof(int32_t) * pat.npairs, cudaMemcpyHostToDevice,
+                                 c.stream));
+        BEM_CUDA(cudaMemcpyAsync(b.pj.p, pat.pair_j.data(), sizeof(int32_t) * pat.npairs, cudaMemcpyHostToDevice,
+                                 c.stream));
+        BEM_CUDA(cudaMemcpyAsync(b.dst.p, pat.pair_dst.data(), sizeof(int64_t) * pat.npairs, cudaMemcpyHostToDevice,
+                                 c.stream));
+    }
+    b.F.ensure(sizeof(float) * P * NF);
+    b.scale.ensure(sizeof(float) * P);
+    b.H1.ensure(sizeof(float) * P * NH);
+    b.H2.ensure(sizeof(float) * P * NH);
+    b.O.ensure(sizeof(float) * P * NO);
+}
+
+static void learned_entries(Context& c, const Problem& p, const LearnedNet& net, const NearPattern& pat, PairBufs& b,
+                            double k, float2* Ms) {
+    const int64_t P = pat.npairs;
+    if (P == 0) return;
+    pc_features_kernel<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(
+        P, b.pi.as<int32_t>(), b.pj.as<int32_t>(), p.geo.npad, p.geo.arr(0), k, b.F.as<float>(), b.scale.as<float>());
+    BEM_CHECK_LAUNCH(&c);
+    mlp_forward(c, net, P, b.F.as<float>(), b.H1.as<float>(), b.H2.as<float>(), b.O.as<float>());
+    pc_write_learned_kernel<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(P, b.O.as<float>(), b.scale.as<float>(),
+                                                                                b.dst.as<int64_t>(), Ms);
+    BEM_CHECK_LAUNCH(&c);
+}
+
+struct PcHookData {
+    PcData data;
+    bool use_off;
+};
+
+static void pc_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
+    (void)mode;
+    PcHookData& h = *static_cast<PcHookData*>(user);
+    dim3 grid((unsigned)h.data.pat.nc, (unsigned)ws.bt.nsys);
+    pc_apply_gmres_kernel<<<grid, PC_LEAF, 0, c.stream>>>(h.data.dev(h.use_off ? 1 : 0), ws.bt);
+    BEM_CHECK_LAUNCH(&c);
+}
+
+bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks) {
+    require(kind == BEM_PRECOND_BLOCK_JACOBI || kind == BEM_PRECOND_LEARNED, "unknown preconditioner");
+    // without a trained or loaded network the learned form falls back to block-Jacobi
+    if (kind == BEM_PRECOND_LEARNED && !(c.net && c.net->ready)) kind = BEM_PRECOND_BLOCK_JACOBI;
+    auto h = std::make_shared<PcHookData>();
+    build_pattern(p, h->data.pat);
+    upload_pattern(c, h->data);
+    const int nsys = ws.bt.nsys;
+    diag_inverses(c, h->data, nsys, ws.bt.A, ws.fp32, ws.bt.lda, ws.bt.mat_stride);
+    h->use_off = false;
+    if (kind == BEM_PRECOND_LEARNED) {
+        PairBufs pb;
+        upload_pairs(c, h->data.pat, pb);
+        for (int s = 0; s < nsys; ++s)
+            learned_entries(c, p, *c.net, h->data.pat, pb, ks[s],
+                            h->data.M.as<float2>() + (size_t)s * h->data.pat.entries);
+        h->use_off = true;
+        c.sync();
+    }
+    ws.zmem.ensure(sizeof(double2) * (size_t)nsys * ws.bt.qstride);
+    ws.bt.Z = ws.zmem.as<double2>();
+    ws.precond = pc_hook;
+    ws.precond_user = h.get();
+    ws.precond_keep = h;
+    return kind;
+}
+
+// ---------------------------------------------------------------------------
+// Training on the operators of a set of problems (all their frequencies).
+double learned_train(Context& c, std::vector<Problem*>& probs, int steps, int nprobe, double lr, uint64_t seed,
+                     std::vector<double>& losses) {
+    if (!c.net) c.net = std::make_unique<LearnedNet>();
+    if (!c.net->ready) c.net->init(c, seed);
+    LearnedNet& net = *c.net;
+    struct Sys {
+        Problem* p;
+        int f;
+        double k;
+    };
+    struct Body {
+        Problem* p;
+        PcData pc;
+        PairBufs pb;
+        DevBuf A;
+        int64_t lda;
+        size_t mstride;
+        int nf;
+        std::vector<double> ks;
+    };
+    std::vector<std::unique_ptr<Body>> bodies;
+    for (Problem* p : probs) {
+        auto b = std::make_unique<Body>();
+        b->p = p;
+        build_pattern(*p, b->pc.pat);
+        upload_pattern(c, b->pc);
+        upload_pairs(c, b->pc.pat, b->pb);
+        b->nf = (int)p->freqs.size();
+        b->lda = p->geo.npad;
+        b->mstride = (size_t)b->lda * p->n;
+        b->A.ensure(sizeof(float2) * b->mstride * b->nf);
+        std::vector<cd> al(b->nf), be(b->nf), ga(b->nf), de(b->nf);
+        int64_t saved = p->ifreq;
+        for (int f = 0; f < b->nf; ++f) {
+            p->ifreq = f;
+            b->ks.push_back(p->wavenumber());
+            lhs_factors(*p, al[f], be[f]);
+            rhs_factors(*p, ga[f], de[f]);
+        }
+        p->ifreq = saved;
+        DevBuf nrm;
+        nrm.ensure(sizeof(double) * b->nf);
+        assemble_system_fp32_body(c, *p, b->ks.data(), al.data(), be.data(), ga.data(), de.data(), b->nf,
+                                  b->A.as<float2>(), b->lda, b->mstride, nullptr, 0, nrm.as<double>());
+        diag_inverses(c, b->pc, b->nf, b->A.p, true, b->lda, b->mstride);
+        c.sync();
+        bodies.push_back(std::move(b));
+    }
+    require(!bodies.empty(), "no training problems");
+    DevBuf grad, lossacc, D1, D2, dO, Z, Y, W, R, G;
+    grad.ensure(sizeof(float) * NPARAM);
+    lossacc.ensure(sizeof(double) * 2);
+    int64_t pmax = 1, nmax = 1;
+    for (auto& b : bodies) {
+        pmax = std::max(pmax, b->pc.pat.npairs);
+        nmax = std::max(nmax, b->p->n);
+    }
+    D1.ensure(sizeof(float) * pmax * NH);
+    D2.ensure(sizeof(float) * pmax * NH);
+    dO.ensure(sizeof(float) * pmax * NO);
+    for (DevBuf* v : {&Z, &Y, &W, &R, &G}) v->ensure(sizeof(double2) * (size_t)nmax * nprobe);
+    losses.clear();
+    int64_t sidx = 0;
+    for (int it = 0; it < steps; ++it) {
+        Body& b = *bodies[(size_t)((sidx / 1) % bodies.size())];
+        const int f = (int)((sidx / (int64_t)bodies.size()) % b.nf);
+        ++sidx;
+        const int64_t n = b.p->n, P = b.pc.pat.npairs;
+        float2* Ms = b.pc.M.as<float2>() + (size_t)f * b.pc.pat.entries;
+        const float2* As = b.A.as<float2>() + (size_t)f * b.mstride;
+        // forward: features, MLP, learned entries of this system
+        if (P > 0) {
+            pc_features_kernel<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(
+                P, b.pb.pi.as<int32_t>(), b.pb.pj.as<int32_t>(), b.p->geo.npad, b.p->geo.arr(0), b.ks[(size_t)f],
+                b.pb.F.as<float>(), b.pb.scale.as<float>());
+            BEM_CHECK_LAUNCH(&c);
+            mlp_forward(c, net, P, b.pb.F.as<float>(), b.pb.H1.as<float>(), b.pb.H2.as<float>(), b.pb.O.as<float>());
+            pc_write_learned_kernel<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(
+                P, b.pb.O.as<float>(), b.pb.scale.as<float>(), b.pb.dst.as<int64_t>(), Ms);
+            BEM_CHECK_LAUNCH(&c);
+        }
+        // probe loss: R = A M Z - Z, G = A^H R
+        const int64_t tot = n * nprobe;
+        probes_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(tot, seed * 7919 + (uint64_t)it,
+                                                                            Z.as<double2>());
+        BEM_CHECK_LAUNCH(&c);
+        pc_apply_probes_kernel<<<dim3((unsigned)b.pc.pat.nc, (unsigned)nprobe), PC_LEAF, 0, c.stream>>>(
+            b.pc.dev(1), f, Z.as<double2>(), Y.as<double2>(), n);
+        BEM_CHECK_LAUNCH(&c);
+        probe_matvec_kernel<<<dim3((unsigned)((n + 127) / 128), (unsigned)nprobe), 128, 0, c.stream>>>(
+            n, As, b.lda, Y.as<double2>(), W.as<double2>(), 0);
+        BEM_CHECK_LAUNCH(&c);
+        BEM_CUDA(cudaMemsetAsync(lossacc.p, 0, sizeof(double) * 2, c.stream));
+        probe_residual_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(
+            tot, W.as<double2>(), Z.as<double2>(), R.as<double2>(), lossacc.as<double>());
+        BEM_CHECK_LAUNCH(&c);
+        probe_matvec_kernel<<<dim3((unsigned)((n * 32 + 127) / 128), (unsigned)nprobe), 128, 0, c.stream>>>(
+            n, As, b.lda, R.as<double2>(), G.as<double2>(), 1);
+        BEM_CHECK_LAUNCH(&c);
+        double la[2];
+        BEM_CUDA(cudaMemcpyAsync(la, lossacc.p, sizeof(la), cudaMemcpyDeviceToHost, c.stream));
+        // backward and Adam
+        BEM_CUDA(cudaMemsetAsync(grad.p, 0, sizeof(float) * NPARAM, c.stream));
+        if (P > 0) {
+            pair_grad_kernel<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(
+                P, nprobe, n, b.pb.pi.as<int32_t>(), b.pb.pj.as<int32_t>(), b.pb.scale.as<float>(), G.as<double2>(),
+                Z.as<double2>(), lossacc.as<double>(), dO.as<float>());
+            BEM_CHECK_LAUNCH(&c);
+            mlp_backward(c, net, P, b.pb.F.as<float>(), b.pb.H1.as<float>(), b.pb.H2.as<float>(), dO.as<float>(),
+                         D2.as<float>(), D1.as<float>(), grad.as<float>());
+        }
+        net.step += 1;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.f - std::pow(b1, (float)net.step), c2 = 1.f - std::pow(b2, (float)net.step);
+        adam_kernel<<<(NPARAM + 255) / 256, 256, 0, c.stream>>>(NPARAM, net.w.as<float>(), grad.as<float>(),
+                                                                 net.m1.as<float>(), net.m2.as<float>(), (float)lr, b1,
+                                                                 b2, c1, c2, 1e-8f);
+        BEM_CHECK_LAUNCH(&c);
+        net.refresh(c);
+        c.sync();
+        losses.push_back(la[0] / la[1]);
+    }
+    net.w_host.resize(NPARAM);
+    BEM_CUDA(cudaMemcpyAsync(net.w_host.data(), net.w.p, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    return losses.empty() ? 0.0 : losses.back();
+}
+
+// MLP forward (and backward for given output gradients) on caller features:
+// exposes the network kernels for checking against a CPU restatement.
+void learned_mlp_eval(Context& c, int64_t P, const float* hF, const float* hdO, float* hO, float* hgrad) {
+    require(c.net && c.net->ready, "no network loaded");
+    DevBuf F, H1, H2, O, dO, D1, D2, grad;
+    F.ensure(sizeof(float) * P * NF);
+    H1.ensure(sizeof(float) * P * NH);
+    H2.ensure(sizeof(float) * P * NH);
+    O.ensure(sizeof(float) * P * NO);
+    BEM_CUDA(cudaMemcpyAsync(F.p, hF, sizeof(float) * P * NF, cudaMemcpyHostToDevice, c.stream));
+    mlp_forward(c, *c.net, P, F.as<float>(), H1.as<float>(), H2.as<float>(), O.as<float>());
+    if (hO) BEM_CUDA(cudaMemcpyAsync(hO, O.p, sizeof(float) * P * NO, cudaMemcpyDeviceToHost, c.stream));
+    if (hdO && hgrad) {
+        dO.ensure(sizeof(float) * P * NO);
+        D1.ensure(sizeof(float) * P * NH);
+        D2.ensure(sizeof(float) * P * NH);
+        grad.ensure(sizeof(float) * NPARAM);
+        BEM_CUDA(cudaMemcpyAsync(dO.p, hdO, sizeof(float) * P * NO, cudaMemcpyHostToDevice, c.stream));
+        BEM_CUDA(cudaMemsetAsync(grad.p, 0, sizeof(float) * NPARAM, c.stream));
+        mlp_backward(c, *c.net, P, F.as<float>(), H1.as<float>(), H2.as<float>(), dO.as<float>(), D2.as<float>(),
+                     D1.as<float>(), grad.as<float>());
+        BEM_CUDA(cudaMemcpyAsync(hgrad, grad.p, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, c.stream));
+    }
+    c.sync();
 }
 
 }  // namespace bem

@@ -1,10 +1,44 @@
 // Preconditioners for the batched GMRES (block-Jacobi and learned).
 #pragma once
+#include <memory>
+
 #include "common.cuh"
 #include "gmres.cuh"
 
 namespace bem {
 
-void precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks);
+// Leaves of the cluster tree and their near-field neighbours.
+struct NearPattern {
+    int64_t n = 0;
+    int nc = 0;
+    std::vector<int64_t> cl_off, cl_idx;  // leaf c holds cl_idx[cl_off[c] .. cl_off[c+1])
+    std::vector<int32_t> nb_off, nb_d;    // neighbours d of leaf c (the first is c itself)
+    std::vector<int64_t> nb_blk;          // storage offset of block (c, d), b_c x b_d column-major
+    int64_t entries = 0;                  // block entries of one system
+    std::vector<int32_t> pair_i, pair_j;  // every entry of the off-diagonal near blocks
+    std::vector<int64_t> pair_dst;        // its storage index
+    int64_t npairs = 0;
+};
+
+// The preconditioner network: FP32 master weights, their BF16-rounded copy
+// used by the forward pass, Adam moments.
+struct LearnedNet {
+    DevBuf w, wbf, m1, m2;
+    std::vector<float> w_host;
+    int64_t step = 0;
+    bool ready = false;
+    void init(Context& c, uint64_t seed);
+    void upload(Context& c);
+    void refresh(Context& c);
+};
+
+int learned_num_params();
+void build_pattern(const Problem& p, NearPattern& P);
+// Installs the preconditioner on the batch; returns the kind actually used
+// (the learned form falls back to block-Jacobi when no network is available).
+bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks);
+double learned_train(Context& c, std::vector<Problem*>& probs, int steps, int nprobe, double lr, uint64_t seed,
+                     std::vector<double>& losses);
+void learned_mlp_eval(Context& c, int64_t P, const float* F, const float* dO, float* O, float* grad);
 
 }  // namespace bem

@@ -220,6 +220,24 @@ BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* p, bem_form form, bem_prec
 /* Surface solutions of the last bem_run (n per frequency, frequency-major). */
 BEM_API bem_status bem_last_surface(bem_ctx* ctx, const bem_problem* p, bem_cplx* phi, bem_cplx* vn);
 
+/* ---- learned preconditioner (no counterpart in the reference) ------------ */
+/* Near-field block preconditioner M = blockdiag(A_cc)^-1 + C where the entries
+ * of C on the near off-diagonal leaf blocks come from a 3-layer MLP (width 128,
+ * BF16 weights/activations, FP32 accumulation) over pair geometry and ka.
+ * bem_learned_train trains the context's network on the GPU on the operators of
+ * the given problems (all their frequencies) by minimising E ||A M z - z||^2 /
+ * ||z||^2 over random probes; losses (steps entries, may be NULL) receive the
+ * per-step loss.  Used by bem_run with BEM_PRECOND_LEARNED. */
+BEM_API bem_status bem_learned_train(bem_ctx* ctx, bem_problem* const* problems, int nproblems, int steps,
+                                     int nprobe, double lr, uint64_t seed, double* losses);
+BEM_API int64_t bem_learned_num_params(void);
+BEM_API bem_status bem_learned_get_weights(bem_ctx* ctx, float* w);
+BEM_API bem_status bem_learned_set_weights(bem_ctx* ctx, const float* w);
+/* Network forward on P feature rows (P x 16) -> outputs (P x 2); with dO
+ * (P x 2) also the parameter gradients of sum(dO * O) (num_params floats). */
+BEM_API bem_status bem_learned_mlp_eval(bem_ctx* ctx, int64_t P, const float* features, const float* dO,
+                                        float* out, float* grad);
+
 /* ---- H-matrix (h_matrix.rs, aca.rs, cluster.rs, block.rs) -------------- */
 /* h_matrix.rs:127-148 HMatrix::new_from over the problem's collocation points
  * for the given side (leaf, eta and ACA tolerance from the problem). */
