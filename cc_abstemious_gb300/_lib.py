@@ -87,6 +87,7 @@ SIGNATURES = {
     "bem_learned_get_weights": (_i, [_vp, _vp]),
     "bem_learned_set_weights": (_i, [_vp, _vp]),
     "bem_learned_mlp_eval": (_i, [_vp, _i64, _vp, _vp, _vp, _vp]),
+    "bem_learned_mlp_infer": (_i, [_vp, _i64, _vp, _vp]),
     "bem_hmatrix_build": (_i, [_vp, _vp, _i, _PP]),
     "bem_hmatrix_destroy": (None, [_vp]),
     "bem_hmatrix_gemv": (_i, [_vp, _vp, Cplx, _vp, Cplx, _vp]),

@@ -739,6 +739,14 @@ BEM_API bem_status bem_learned_mlp_eval(bem_ctx* ctx, int64_t P, const float* fe
     });
 }
 
+BEM_API bem_status bem_learned_mlp_infer(bem_ctx* ctx, int64_t P, const float* features, float* out) {
+    if (!ctx || P < 1 || !features || !out) return BEM_ERR_BAD_INPUT;
+    return guard(ctx, [&] {
+        set_device(ctx->c);
+        learned_mlp_infer(ctx->c, P, features, out);
+    });
+}
+
 BEM_API bem_status bem_last_surface(bem_ctx* ctx, const bem_problem* pp, bem_cplx* phi, bem_cplx* vn) {
     if (!ctx || !pp) return BEM_ERR_BAD_INPUT;
     Context& c = ctx->c;

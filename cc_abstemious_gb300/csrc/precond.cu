@@ -637,10 +637,8 @@ static void learned_entries(Context& c, const Problem& p, const LearnedNet& net,
     pc_features_kernel<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(
         P, b.pi.as<int32_t>(), b.pj.as<int32_t>(), p.geo.npad, p.geo.arr(0), k, b.F.as<float>(), b.scale.as<float>());
     BEM_CHECK_LAUNCH(&c);
-    mlp_forward(c, net, P, b.F.as<float>(), b.H1.as<float>(), b.H2.as<float>(), b.O.as<float>());
-    pc_write_learned_kernel<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(P, b.O.as<float>(), b.scale.as<float>(),
-                                                                                b.dst.as<int64_t>(), Ms);
-    BEM_CHECK_LAUNCH(&c);
+    // inference on the tensor cores, entries written straight into the blocks
+    mlp_infer_tc(c, net, P, b.F.as<float>(), nullptr, b.dst.as<int64_t>(), b.scale.as<float>(), Ms);
 }
 
 struct PcHookData {
@@ -811,6 +809,18 @@ double learned_train(Context& c, std::vector<Problem*>& probs, int steps, int np
     BEM_CUDA(cudaMemcpyAsync(net.w_host.data(), net.w.p, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, c.stream));
     c.sync();
     return losses.empty() ? 0.0 : losses.back();
+}
+
+// Tensor-core inference on caller features (host arrays).
+void learned_mlp_infer(Context& c, int64_t P, const float* hF, float* hO) {
+    require(c.net && c.net->ready, "no network loaded");
+    DevBuf F, O;
+    F.ensure(sizeof(float) * P * NF);
+    O.ensure(sizeof(float) * P * NO);
+    BEM_CUDA(cudaMemcpyAsync(F.p, hF, sizeof(float) * P * NF, cudaMemcpyHostToDevice, c.stream));
+    mlp_infer_tc(c, *c.net, P, F.as<float>(), O.as<float>(), nullptr, nullptr, nullptr);
+    BEM_CUDA(cudaMemcpyAsync(hO, O.p, sizeof(float) * P * NO, cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
 }
 
 // MLP forward (and backward for given output gradients) on caller features:

@@ -40,5 +40,10 @@ bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond k
 double learned_train(Context& c, std::vector<Problem*>& probs, int steps, int nprobe, double lr, uint64_t seed,
                      std::vector<double>& losses);
 void learned_mlp_eval(Context& c, int64_t P, const float* F, const float* dO, float* O, float* grad);
+void learned_mlp_infer(Context& c, int64_t P, const float* F, float* O);
+// Tensor-core inference (tc_mlp.cu): outputs to O (P x 2) and/or the learned
+// entries s_p (o_1 + i o_2) to M[dst[p]].
+void mlp_infer_tc(Context& c, const LearnedNet& net, int64_t P, const float* F, float* O, const int64_t* dst,
+                  const float* scale, float2* M);
 
 }  // namespace bem

@@ -237,6 +237,9 @@ BEM_API bem_status bem_learned_set_weights(bem_ctx* ctx, const float* w);
  * (P x 2) also the parameter gradients of sum(dO * O) (num_params floats). */
 BEM_API bem_status bem_learned_mlp_eval(bem_ctx* ctx, int64_t P, const float* features, const float* dO,
                                         float* out, float* grad);
+/* Network outputs (P x 2) by the tensor-core (tcgen05) inference kernel that
+ * bem_run uses to emit the learned preconditioner entries. */
+BEM_API bem_status bem_learned_mlp_infer(bem_ctx* ctx, int64_t P, const float* features, float* out);
 
 /* ---- H-matrix (h_matrix.rs, aca.rs, cluster.rs, block.rs) -------------- */
 /* h_matrix.rs:127-148 HMatrix::new_from over the problem's collocation points

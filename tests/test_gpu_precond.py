@@ -56,6 +56,28 @@ def test_mlp_kernels_match_cpu(ctx):
         assert np.linalg.norm(grad[lo:hi] - g_ref[lo:hi]) <= 1e-2 * np.linalg.norm(g_ref[lo:hi]), (lo, hi)
 
 
+@pytest.mark.parametrize("P", [1, 127, 128, 129, 5000])
+def test_tensor_core_inference_matches_cpu(ctx, P):
+    """tcgen05 inference (BF16 operands in shared memory, FP32 accumulators in
+    tensor memory) against the CPU restatement and the CUDA-core forward."""
+    w = _random_weights(7)
+    bem.learned_set_weights(w, ctx=ctx)
+    rng = np.random.default_rng(P)
+    F = rng.normal(size=(P, OM.NF)).astype(np.float32)
+    out = np.zeros((P, 2), dtype=np.float32)
+    ctx.check(ctx.lib.bem_learned_mlp_infer(ctx.h, P, bem._ptr(F), bem._ptr(out)))
+    ref = OM.forward(w, F)[3]
+    cuda_core = bem.learned_mlp_eval(F, ctx=ctx)
+    scale = max(np.max(np.abs(ref)), 1e-6)
+    assert np.max(np.abs(out - ref)) <= 2e-2 * scale
+    assert np.linalg.norm(out - ref) <= 3e-3 * np.linalg.norm(ref)
+    # both GPU forwards round activations to BF16 with different FP32
+    # summation orders: each is within 3e-3 of the restatement, so within 6e-3
+    # of each other; a wrong tile row would differ by O(1)
+    assert np.linalg.norm(out - cuda_core) <= 6e-3 * np.linalg.norm(cuda_core)
+    assert np.max(np.abs(out - cuda_core)) <= 2e-2 * scale
+
+
 def _run(ctx, inp, precond):
     a = bem.Analysis(ctx)
     a.set_input(inp)
