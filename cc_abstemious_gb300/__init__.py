@@ -401,6 +401,41 @@ class Analysis:
         write_results_at_point(self.predata, self.results, index, out)
 
 
+_PRECONDS = {None: PRECOND_NONE, "none": PRECOND_NONE, "block_jacobi": PRECOND_BLOCK_JACOBI,
+             "learned": PRECOND_LEARNED}
+
+
+def run_batch(predatas, precond=None, check_vs_lu=False, max_operator_bytes=0, ctx=None):
+    """Several bodies in one batch (mixed form, no reference counterpart: the
+    reference runs one Analysis per body).  Returns, per body, a list of
+    FPResult (pressure / potential as Analysis.run leaves them) and the
+    per-frequency solve reports."""
+    ctx = ctx or (predatas[0].ctx if predatas else Context.default())
+    nb = len(predatas)
+    outs, ptrs_s, ptrs_i, reps = [], (C.c_void_p * max(nb, 1))(), (C.c_void_p * max(nb, 1))(), []
+    rep_ptrs = (C.c_void_p * max(nb, 1))()
+    handles = (C.c_void_p * max(nb, 1))()
+    for b, pd in enumerate(predatas):
+        nf, nfp = len(pd.frequencies), pd.nfp
+        sc = np.zeros((nf, max(nfp, 1)), dtype=np.complex128)
+        inc = np.zeros((nf, max(nfp, 1)), dtype=np.complex128)
+        r = (SolveReport * max(nf, 1))()
+        outs.append((sc, inc))
+        reps.append(r)
+        ptrs_s[b], ptrs_i[b] = sc.ctypes.data, inc.ctypes.data
+        rep_ptrs[b] = C.cast(r, C.c_void_p)
+        handles[b] = pd.h
+    ctx.check(ctx.lib.bem_run_batch(ctx.h, handles, nb, _PRECONDS[precond], ptrs_s, ptrs_i, rep_ptrs,
+                                    1 if check_vs_lu else 0, int(max_operator_bytes)))
+    results = []
+    for b, pd in enumerate(predatas):
+        nf, nfp = len(pd.frequencies), pd.nfp
+        sc, inc = outs[b]
+        results.append(([FPResult(float(pd.frequencies[i]), sc[i, :nfp].copy(), inc[i, :nfp].copy())
+                         for i in range(nf)], [reps[b][i].as_dict() for i in range(nf)]))
+    return results
+
+
 class HMatrix:
     """h_matrix.rs:110-247 over a problem's collocation points."""
 

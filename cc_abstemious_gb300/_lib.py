@@ -82,6 +82,7 @@ SIGNATURES = {
     "bem_convert_to_pressure": (_i, [_vp, _d, _vp, _i64]),
     "bem_run": (_i, [_vp, _vp, _i, _i, _vp, _vp, C.POINTER(SolveReport), _i]),
     "bem_last_surface": (_i, [_vp, _vp, _vp, _vp]),
+    "bem_run_batch": (_i, [_vp, _PP, _i, _i, _PP, _PP, _PP, _i, _i64]),
     "bem_learned_train": (_i, [_vp, _vp, _i, _i, _i, _d, C.c_uint64, _vp]),
     "bem_learned_num_params": (_i64, []),
     "bem_learned_get_weights": (_i, [_vp, _vp]),

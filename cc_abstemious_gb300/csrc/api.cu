@@ -622,6 +622,31 @@ BEM_API bem_status bem_convert_to_pressure(const bem_problem* pp, double frequen
     return BEM_OK;
 }
 
+BEM_API bem_status bem_run_batch(bem_ctx* ctx, bem_problem* const* problems, int nprob, bem_precond precond,
+                                 bem_cplx* const* scattered, bem_cplx* const* incident,
+                                 bem_solve_report* const* reports, int check_vs_lu, int64_t max_operator_bytes) {
+    if (!ctx || !problems || nprob < 0 || max_operator_bytes < 0) return BEM_ERR_BAD_INPUT;
+    for (int i = 0; i < nprob; ++i)
+        if (!problems[i]) return BEM_ERR_BAD_INPUT;
+    return guard(ctx, [&] {
+        Context& c = ctx->c;
+        set_device(c);
+        std::vector<Problem*> probs;
+        for (int i = 0; i < nprob; ++i) {
+            Problem& p = problems[i]->p;
+            probs.push_back(&p);
+            if (reports && reports[i])
+                for (size_t f = 0; f < p.freqs.size(); ++f) {
+                    std::memset(&reports[i][f], 0, sizeof(bem_solve_report));
+                    reports[i][f].rel_err_vs_lu = -1;
+                }
+        }
+        if (nprob == 0) return;
+        run_mixed_batch(c, probs, precond, scattered, incident, reports, check_vs_lu != 0,
+                        (size_t)max_operator_bytes);
+    });
+}
+
 BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* pp, bem_form form, bem_precond precond, bem_cplx* scattered,
                            bem_cplx* incident, bem_solve_report* reports, int check_vs_lu) {
     if (!ctx || !pp) return BEM_ERR_BAD_INPUT;

@@ -112,15 +112,27 @@ __device__ __forceinline__ Sep32 separation32(float axh, float axl, float ayh, f
     return o;
 }
 
+struct Asm32Smem {
+    TileGeo32 t;
+    uint64_t bar;
+    float red[ASM_THREADS / 32][MAX_SYS32];
+};
+
+// One 64 x 64 tile (row tile ti, column tile tj) of every system of a body;
+// the squared Frobenius norm partial of system s goes to
+// norm_part[s * norm_stride + tile_index].
 template <int WITH_RHS>
-__global__ void __launch_bounds__(ASM_THREADS) assemble32_kernel(
-    int64_t n, int64_t npad, const float* __restrict__ g32, const double* __restrict__ geo, Asm32Params prm,
-    float2* __restrict__ A, int64_t ld, size_t mat_stride, double2* __restrict__ part, size_t part_stride,
-    double* __restrict__ norm_part, int* __restrict__ err) {
-    __shared__ __align__(128) TileGeo32 t;
-    __shared__ __align__(8) uint64_t bar;
-    __shared__ float red[ASM_THREADS / 32][MAX_SYS32];
-    const int64_t I0 = (int64_t)blockIdx.y * TILE, J0 = (int64_t)blockIdx.x * TILE;
+__device__ __forceinline__ void assemble32_tile(int64_t n, int64_t npad, const float* __restrict__ g32,
+                                                const double* __restrict__ geo, const Asm32Params& prm,
+                                                float2* __restrict__ A, int64_t ld, size_t mat_stride,
+                                                double2* __restrict__ part, size_t part_stride,
+                                                double* __restrict__ norm_part, size_t norm_stride,
+                                                size_t tile_index, int ti, int tj, int* __restrict__ err,
+                                                Asm32Smem& sm) {
+    TileGeo32& t = sm.t;
+    uint64_t& bar = sm.bar;
+    auto& red = sm.red;
+    const int64_t I0 = (int64_t)ti * TILE, J0 = (int64_t)tj * TILE;
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_mbar_init();
@@ -236,7 +248,7 @@ __global__ void __launch_bounds__(ASM_THREADS) assemble32_kernel(
     if (threadIdx.x < prm.nsys) {
         double sum = 0;
         for (int w = 0; w < ASM_THREADS / 32; ++w) sum += red[w][threadIdx.x];
-        norm_part[(size_t)threadIdx.x * gridDim.x * gridDim.y + (size_t)blockIdx.y * gridDim.x + blockIdx.x] = sum;
+        norm_part[(size_t)threadIdx.x * norm_stride + tile_index] = sum;
     }
     if (WITH_RHS) {
         __shared__ float2 rred[ASM_THREADS];
@@ -252,10 +264,62 @@ __global__ void __launch_bounds__(ASM_THREADS) assemble32_kernel(
                     sx += rred[tx + TILE * q2].x;
                     sy += rred[tx + TILE * q2].y;
                 }
-                part[s * part_stride + (int64_t)blockIdx.x * npad + i] = make_double2(sx, sy);
+                part[s * part_stride + (int64_t)tj * npad + i] = make_double2(sx, sy);
             }
         }
     }
+}
+
+template <int WITH_RHS>
+__global__ void __launch_bounds__(ASM_THREADS) assemble32_kernel(
+    int64_t n, int64_t npad, const float* __restrict__ g32, const double* __restrict__ geo, Asm32Params prm,
+    float2* __restrict__ A, int64_t ld, size_t mat_stride, double2* __restrict__ part, size_t part_stride,
+    double* __restrict__ norm_part, int* __restrict__ err) {
+    __shared__ __align__(128) Asm32Smem sm;
+    assemble32_tile<WITH_RHS>(n, npad, g32, geo, prm, A, ld, mat_stride, part, part_stride, norm_part,
+                              (size_t)gridDim.x * gridDim.y, (size_t)blockIdx.y * gridDim.x + blockIdx.x,
+                              (int)blockIdx.y, (int)blockIdx.x, err, sm);
+}
+
+// Several bodies (each with its own frequencies) in one launch: a flattened
+// grid over every body's tiles, the body found by bisection on tile0 and its
+// parameters staged in shared memory.
+struct Body32 {
+    int64_t n, npad;
+    const float* g32;
+    const double* geo;
+    float2* A;          // system s of the body at A + s * mat_stride
+    int64_t ld;
+    size_t mat_stride;
+    double* norm_part;  // nsys x ntiles^2 partials
+    int64_t tile0;
+    int ntiles, pad;
+};
+
+__global__ void __launch_bounds__(ASM_THREADS, 3) assemble32_multi_kernel(const Body32* __restrict__ bodies,
+                                                                      int nbodies,
+                                                                      const Asm32Params* __restrict__ prms,
+                                                                      int* __restrict__ err) {
+    __shared__ __align__(128) Asm32Smem sm;
+    __shared__ __align__(16) Asm32Params prm;
+    const int64_t t = blockIdx.x;
+    int lo = 0, hi = nbodies - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (bodies[mid].tile0 <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const Body32 B = bodies[lo];
+    {
+        const int* src = reinterpret_cast<const int*>(prms + lo);
+        int* dst = reinterpret_cast<int*>(&prm);
+        for (int w = threadIdx.x; w < (int)(sizeof(Asm32Params) / sizeof(int)); w += ASM_THREADS) dst[w] = src[w];
+    }
+    __syncthreads();
+    const int64_t local = t - B.tile0;
+    const int ti = (int)(local / B.ntiles), tj = (int)(local % B.ntiles);
+    assemble32_tile<0>(B.n, B.npad, B.g32, B.geo, prm, B.A, B.ld, B.mat_stride, nullptr, 0, B.norm_part,
+                       (size_t)B.ntiles * B.ntiles, (size_t)local, ti, tj, err, sm);
 }
 
 __global__ void finish_norm_kernel(const double* __restrict__ part, int64_t nparts, double* __restrict__ out) {
@@ -333,6 +397,114 @@ void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks,
         }
     }
     check_device_err(ctx);
+}
+
+// Norm of system g from its partials part[off[g] .. off[g] + cnt[g]).
+__global__ void finish_norm_multi_kernel(const double* __restrict__ part, const int64_t* __restrict__ off,
+                                         const int64_t* __restrict__ cnt, double* __restrict__ out) {
+    __shared__ double sh[256];
+    const int g = blockIdx.x;
+    double v = 0;
+    for (int64_t t = threadIdx.x; t < cnt[g]; t += blockDim.x) v += part[off[g] + t];
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[g] = sqrt(sh[0]);
+}
+
+static void fill_params(const Problem& p, const double* ks, const cd* alphas, const cd* betas, const cd* gammas,
+                        const cd* deltas, int nsys, Asm32Params& prm) {
+    const float P1 = 1.5703125f;  // 201/128: n * P1 exact for n < 2^16
+    const double rem1 = PI_D / 2 - (double)P1;
+    prm = Asm32Params{};
+    prm.nsys = nsys;
+    prm.bm = p.in.method_type == 1;
+    prm.hdiag = p.in.problem_type == 1 ? -0.5 : 0.0;
+    prm.P1 = P1;
+    prm.P2 = (float)rem1;
+    prm.P3 = (float)(rem1 - (double)prm.P2);
+    prm.two_over_pi = (float)(2.0 / PI_D);
+    for (int s = 0; s < nsys; ++s) {
+        const double k = ks[s];
+        Sys32& S = prm.s[s];
+        S.kh = (float)k;
+        S.kl = (float)(k - (double)S.kh);
+        S.kd = k;
+        S.k2 = (float)(k * k);
+        S.beta_im = prm.bm ? (float)(1.0 / k) : 0.f;
+        S.gdiag_im = prm.bm ? 0.5 * (1.0 / k) : 0.0;
+        S.alpha = make_float2((float)alphas[s].re, (float)alphas[s].im);
+        S.beta = make_float2((float)betas[s].re, (float)betas[s].im);
+        if (gammas) S.gamma = make_float2((float)gammas[s].re, (float)gammas[s].im);
+        if (deltas) S.delta = make_float2((float)deltas[s].re, (float)deltas[s].im);
+    }
+}
+
+void assemble_fp32_multi(Context& ctx, const std::vector<BodyAsm32>& bodies, double* norms) {
+    if (bodies.empty()) return;
+    // split bodies with more than MAX_SYS32 systems into entries of <= MAX_SYS32
+    std::vector<Body32> ent;
+    std::vector<Asm32Params> prms;
+    std::vector<int64_t> off, cnt;
+    int64_t tiles = 0, parts = 0;
+    for (const BodyAsm32& b : bodies) {
+        const Problem& p = *b.p;
+        const int ntiles = (int)(p.geo.npad / TILE);
+        for (int s0 = 0; s0 < b.nsys; s0 += MAX_SYS32) {
+            const int ns = std::min(MAX_SYS32, b.nsys - s0);
+            Body32 e{};
+            e.n = p.n;
+            e.npad = p.geo.npad;
+            e.g32 = p.geo.arr32(0);
+            e.geo = p.geo.arr(0);
+            e.A = b.A + (size_t)s0 * b.mat_stride;
+            e.ld = b.ld;
+            e.mat_stride = b.mat_stride;
+            e.norm_part = reinterpret_cast<double*>(parts);  // offset for now
+            e.tile0 = tiles;
+            e.ntiles = ntiles;
+            Asm32Params prm;
+            fill_params(p, b.ks + s0, b.alphas + s0, b.betas + s0, nullptr, nullptr, ns, prm);
+            for (int s = 0; s < ns; ++s) {
+                off.push_back(parts + (int64_t)s * ntiles * ntiles);
+                cnt.push_back((int64_t)ntiles * ntiles);
+            }
+            parts += (int64_t)ns * ntiles * ntiles;
+            tiles += (int64_t)ntiles * ntiles;
+            ent.push_back(e);
+            prms.push_back(prm);
+        }
+    }
+    const size_t nent = ent.size(), nsys = off.size();
+    const size_t b_ent = sizeof(Body32) * nent, b_prm = sizeof(Asm32Params) * nent, b_idx = sizeof(int64_t) * nsys;
+    DevBuf& nbuf = ctx.w_norm;
+    nbuf.ensure(sizeof(double) * (size_t)parts);
+    for (Body32& e : ent) e.norm_part = nbuf.as<double>() + reinterpret_cast<int64_t>(e.norm_part);
+    DevBuf& meta = ctx.w_small;
+    const size_t o_prm = (b_ent + 255) / 256 * 256, o_off = o_prm + (b_prm + 255) / 256 * 256,
+                 o_cnt = o_off + (b_idx + 255) / 256 * 256;
+    meta.ensure(o_cnt + b_idx);
+    char* mb = meta.as<char>();
+    BEM_CUDA(cudaMemcpyAsync(mb, ent.data(), b_ent, cudaMemcpyHostToDevice, ctx.stream));
+    BEM_CUDA(cudaMemcpyAsync(mb + o_prm, prms.data(), b_prm, cudaMemcpyHostToDevice, ctx.stream));
+    BEM_CUDA(cudaMemcpyAsync(mb + o_off, off.data(), b_idx, cudaMemcpyHostToDevice, ctx.stream));
+    BEM_CUDA(cudaMemcpyAsync(mb + o_cnt, cnt.data(), b_idx, cudaMemcpyHostToDevice, ctx.stream));
+    int* err = device_err(ctx);
+    BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx.stream));
+    require(tiles < (int64_t)INT32_MAX, "multi-body assembly: too many tiles");
+    assemble32_multi_kernel<<<(unsigned)tiles, ASM_THREADS, 0, ctx.stream>>>(
+        reinterpret_cast<const Body32*>(mb), (int)nent, reinterpret_cast<const Asm32Params*>(mb + o_prm), err);
+    BEM_CHECK_LAUNCH(&ctx);
+    if (norms) {
+        finish_norm_multi_kernel<<<(unsigned)nsys, 256, 0, ctx.stream>>>(
+            nbuf.as<double>(), reinterpret_cast<const int64_t*>(mb + o_off), reinterpret_cast<const int64_t*>(mb + o_cnt),
+            norms);
+        BEM_CHECK_LAUNCH(&ctx);
+    }
+    check_device_err(ctx);  // synchronises: the host metadata above may be released after return
 }
 
 // ---------------------------------------------------------------------------

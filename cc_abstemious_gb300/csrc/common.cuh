@@ -198,6 +198,18 @@ void assemble_system_fp64(Context& ctx, const Problem& p, double2* A, int64_t ld
 void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
                                const cd* betas, const cd* gammas, const cd* deltas, int nsys, float2* A,
                                int64_t ld, size_t mat_stride, double2* rowsum, size_t vec_stride, double* norms);
+// Several bodies, each with nsys frequencies (LHS operator only), in one
+// launch; norms[g] = ||A_g||_F for the systems in body-major order.
+struct BodyAsm32 {
+    const Problem* p;
+    int nsys;
+    const double* ks;
+    const cd *alphas, *betas;
+    float2* A;  // system s at A + s * mat_stride
+    int64_t ld;
+    size_t mat_stride;
+};
+void assemble_fp32_multi(Context& ctx, const std::vector<BodyAsm32>& bodies, double* norms);
 void evaluate_field32_batch(Context& ctx, const Problem& p, const double* ks, int nsys, const double2* phi,
                             const double2* vn, int64_t vstride, const double2* inc, double2* out);
 void field_matrices_fp64(Context& ctx, const Problem& p, double2* M, double2* L, int64_t ld);

@@ -1,5 +1,6 @@
 // Restarted GMRES (gmres.rs:35-202) as a device-side state machine over a
-// batch of independent systems of equal size n.
+// batch of independent systems: of equal size n (uniform layout), or of
+// different sizes (ragged layout, per-system offsets in GmSys).
 //
 // One iteration is the fixed launch sequence
 //   apply(START) -> start -> apply(Q) -> arnoldi -> apply(CHECK) -> check
@@ -63,19 +64,40 @@ constexpr int MV_UNROLL = 8;
 
 template <typename T, int EXACT>
 __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mode) {
-    const int s = blockIdx.z;
+    int s, bx, by;
+    if (bt.sys) {
+        // ragged batch: one flattened grid over every system's (row block,
+        // column chunk) tiles; the system is found by bisection on tile0
+        const int64_t t = blockIdx.x;
+        int lo = 0, hi = bt.nsys - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (bt.sys[mid].tile0 <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        s = lo;
+        const int64_t local = t - bt.sys[s].tile0;
+        const int rbs = bt.sys[s].rb;
+        bx = (int)(local % rbs);
+        by = (int)(local / rbs);
+    } else {
+        s = blockIdx.z;
+        bx = blockIdx.x;
+        by = blockIdx.y;
+    }
     GmState& st = bt.st[s];
     if (!mv_active(st, mode)) return;
     // outside the reference-faithful mode the first cycle starts from x = 0,
     // so its residual is b itself: no product needed
     if (mode == MV_START && !bt.ref_dotc && st.restarts == 0) return;
-    const int64_t n = bt.n;
+    const GmView g = gm_view(bt, s);
+    const int64_t n = g.n;
     const double2* kv = bt.Z ? bt.Z : bt.Q;  // right preconditioning applies A to M q_k
-    const double2* v = (mode == MV_Q) ? kv + (size_t)s * bt.qstride + (size_t)st.k * n : bt.X + (size_t)s * n;
+    const double2* v = (mode == MV_Q) ? kv + g.q + (size_t)st.k * n : bt.X + g.v;
     __shared__ float2 xh[MV_COLS], xl[MV_COLS];
     __shared__ double2 xd[MV_COLS];
     __shared__ int last;
-    const int64_t j0 = (int64_t)blockIdx.y * MV_COLS;
+    const int64_t j0 = (int64_t)by * MV_COLS;
     const int jn = (int)min((int64_t)MV_COLS, n - j0);
     for (int t = threadIdx.x; t < MV_COLS; t += MV_THREADS) {
         double2 x = t < jn ? v[j0 + t] : make_double2(0, 0);
@@ -88,12 +110,13 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
         }
     }
     __syncthreads();
-    const int64_t i0 = (int64_t)blockIdx.x * MV_ROWS + MV_ROWS_PER_THREAD * threadIdx.x;
+    const int64_t i0 = (int64_t)bx * MV_ROWS + MV_ROWS_PER_THREAD * threadIdx.x;
+    const int64_t lda = g.lda;
     double2 r0 = make_double2(0, 0), r1 = make_double2(0, 0);
     if (i0 < n) {
         const bool pair = (i0 + 1 < n);
         if (sizeof(T) == sizeof(float2)) {
-            const float2* A = reinterpret_cast<const float2*>(bt.A) + (size_t)s * bt.mat_stride + i0;
+            const float2* A = reinterpret_cast<const float2*>(bt.A) + g.a + i0;
             // float-float accumulators for (re0, im0, re1, im1)
             float h0 = 0, l0 = 0, h1 = 0, l1 = 0, h2 = 0, l2 = 0, h3 = 0, l3 = 0;
             for (int q0 = 0; q0 < jn; q0 += MV_UNROLL) {
@@ -102,7 +125,7 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
                 for (int u = 0; u < MV_UNROLL; ++u) {
                     const int q = q0 + u;
                     if (q < jn) {
-                        const float2* col = A + (j0 + q) * bt.lda;
+                        const float2* col = A + (j0 + q) * lda;
                         if (pair) a[u] = __ldcs(reinterpret_cast<const float4*>(col));
                         else { float2 t = col[0]; a[u] = make_float4(t.x, t.y, 0.f, 0.f); }
                     } else {
@@ -144,13 +167,13 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
             r0 = make_double2((double)h0 + (double)l0, (double)h1 + (double)l1);
             r1 = make_double2((double)h2 + (double)l2, (double)h3 + (double)l3);
         } else {
-            const double2* A = reinterpret_cast<const double2*>(bt.A) + (size_t)s * bt.mat_stride + i0;
+            const double2* A = reinterpret_cast<const double2*>(bt.A) + g.a + i0;
             for (int q0 = 0; q0 < jn; q0 += MV_UNROLL) {
                 double2 a0[MV_UNROLL], a1[MV_UNROLL];
 #pragma unroll
                 for (int u = 0; u < MV_UNROLL; ++u) {
                     const int q = q0 + u;
-                    const double2* col = A + (j0 + (q < jn ? q : 0)) * bt.lda;
+                    const double2* col = A + (j0 + (q < jn ? q : 0)) * lda;
                     a0[u] = q < jn ? col[0] : make_double2(0, 0);
                     a1[u] = (q < jn && pair) ? col[1] : make_double2(0, 0);
                 }
@@ -162,27 +185,27 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
                 }
             }
         }
-        double2* part = bt.part + ((size_t)s * gridDim.y + blockIdx.y) * bt.n_pad;
+        double2* part = bt.part + g.p + (size_t)by * g.n_pad;
         part[i0] = r0;
         if (pair) part[i0 + 1] = r1;
     }
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
-        int* tk = bt.tickets + (size_t)s * gridDim.x + blockIdx.x;
-        last = (atomicAdd(tk, 1) == (int)gridDim.y - 1);
+        int* tk = bt.tickets + g.t + bx;
+        last = (atomicAdd(tk, 1) == g.cb - 1);
         if (last) *tk = 0;
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-    double2* W = bt.W + (size_t)s * n;
+    double2* W = bt.W + g.v;
     for (int rr = 0; rr < MV_ROWS_PER_THREAD; ++rr) {
         int64_t i = i0 + rr;
         if (i >= n) break;
         double2 acc = make_double2(0, 0);
-        const double2* part = bt.part + (size_t)s * gridDim.y * bt.n_pad;
-        for (int c = 0; c < (int)gridDim.y; ++c) acc = cadd(acc, part[(size_t)c * bt.n_pad + i]);
+        const double2* part = bt.part + g.p;
+        for (int c = 0; c < g.cb; ++c) acc = cadd(acc, part[(size_t)c * g.n_pad + i]);
         W[i] = acc;
     }
 }
@@ -239,10 +262,11 @@ __global__ void __launch_bounds__(AR_THREADS) gm_start_kernel(GmBatch bt) {
     GmState& st = bt.st[s];
     if (st.done || !st.need_start) return;
     __shared__ double sh[80];
-    const int64_t n = bt.n;
-    const double2* b = bt.B + (size_t)s * n;
-    const double2* W = bt.W + (size_t)s * n;
-    double2* Q = bt.Q + (size_t)s * bt.qstride;
+    const GmView g = gm_view(bt, s);
+    const int64_t n = g.n;
+    const double2* b = bt.B + g.v;
+    const double2* W = bt.W + g.v;
+    double2* Q = bt.Q + g.q;
     const bool zero_x = !bt.ref_dotc && st.restarts == 0;  // x = 0: A x not formed
     double acc = 0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
@@ -255,7 +279,7 @@ __global__ void __launch_bounds__(AR_THREADS) gm_start_kernel(GmBatch bt) {
         double2 r = Q[i];
         Q[i] = make_double2(r.x / rn, r.y / rn);
     }
-    double xn = vec_norm(bt.X + (size_t)s * n, n, sh);
+    double xn = vec_norm(bt.X + g.v, n, sh);
     if (threadIdx.x == 0) {
         GmSmall sm = gm_small(bt, s);
         for (int i = 0; i <= bt.m; ++i) sm.beta[i] = make_double2(0, 0);
@@ -282,11 +306,12 @@ __global__ void __launch_bounds__(AR_THREADS) gm_arnoldi_kernel(GmBatch bt, int 
     extern __shared__ double2 wsh[];
     __shared__ double sh[80];
     __shared__ double2 hsh;
-    const int64_t n = bt.n;
+    const GmView g = gm_view(bt, s);
+    const int64_t n = g.n;
     const int k = st.k;
     const int m = bt.m;
-    double2* Q = bt.Q + (size_t)s * bt.qstride;
-    double2* Wg = bt.W + (size_t)s * n;
+    double2* Q = bt.Q + g.q;
+    double2* Wg = bt.W + g.v;
     double2* w = w_in_smem ? wsh : Wg;
     if (w_in_smem)
         for (int64_t i = threadIdx.x; i < n; i += blockDim.x) w[i] = Wg[i];
@@ -341,7 +366,7 @@ __global__ void __launch_bounds__(AR_THREADS) gm_arnoldi_kernel(GmBatch bt, int 
         st.error = cabs_(sm.beta[k + 1]) / (st.anorm * st.xnorm + st.bnorm);
         st.num_mv += 1;
         st.iterations += 1;
-        int chk = (st.error < st.tol) || (k == m - 1);
+        int chk = (st.error < st.tol) || (k == st.m - 1);
         st.check = chk;
         if (chk) {
             // y = H_k^{-1} beta_k: H_k is upper triangular after the rotations
@@ -358,8 +383,8 @@ __global__ void __launch_bounds__(AR_THREADS) gm_arnoldi_kernel(GmBatch bt, int 
     __syncthreads();
     if (hsh.x != 0.0) {
         // x += Q_k y, or Z_k y with flexible right preconditioning
-        double2* x = bt.X + (size_t)s * n;
-        const double2* Zs = bt.Z ? bt.Z + (size_t)s * bt.qstride : Q;
+        double2* x = bt.X + g.v;
+        const double2* Zs = bt.Z ? bt.Z + g.q : Q;
         for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
             double2 a = x[l];
             for (int j = 0; j <= k; ++j) cfma(a, Zs[(size_t)j * n + l], sm.y[j]);
@@ -374,16 +399,17 @@ __global__ void __launch_bounds__(AR_THREADS) gm_check_kernel(GmBatch bt) {
     GmState& st = bt.st[s];
     if (st.done || !st.check) return;
     __shared__ double sh[80];
-    const int64_t n = bt.n;
-    const double2* b = bt.B + (size_t)s * n;
-    const double2* W = bt.W + (size_t)s * n;
+    const GmView g = gm_view(bt, s);
+    const int64_t n = g.n;
+    const double2* b = bt.B + g.v;
+    const double2* W = bt.W + g.v;
     double acc = 0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
         double2 r = csub(b[i], W[i]);
         acc += r.x * r.x + r.y * r.y;
     }
     double rn = sqrt(block_sum(acc, sh));
-    double xn = vec_norm(bt.X + (size_t)s * n, n, sh);
+    double xn = vec_norm(bt.X + g.v, n, sh);
     if (threadIdx.x == 0) {
         st.num_mv += 1;
         st.xnorm = xn;
@@ -392,7 +418,7 @@ __global__ void __launch_bounds__(AR_THREADS) gm_check_kernel(GmBatch bt) {
         if (st.error < st.tol) {
             st.done = 1;
             st.converged = 1;
-        } else if (st.k == bt.m - 1 || !bt.ref_dotc) {
+        } else if (st.k == st.m - 1 || !bt.ref_dotc) {
             // End of the cycle.  Outside the reference-faithful mode a failed
             // check also restarts from the updated x (an iterative-refinement
             // step), instead of continuing the Arnoldi process and adding the
@@ -407,18 +433,22 @@ __global__ void __launch_bounds__(AR_THREADS) gm_check_kernel(GmBatch bt) {
 }
 
 // Zero initial guess and the per-system constants.
-__global__ void gm_init_kernel(GmBatch bt, const double* anorm, double tol, int64_t max_restarts) {
+__global__ void gm_init_kernel(GmBatch bt, const double* anorm, double tol, int64_t max_restarts,
+                               const double* __restrict__ tols, const int64_t* __restrict__ maxrs,
+                               const int* __restrict__ ms) {
     const int s = blockIdx.x;
     __shared__ double sh[80];
-    const int64_t n = bt.n;
-    double2* x = bt.X + (size_t)s * n;
+    const GmView g = gm_view(bt, s);
+    const int64_t n = g.n;
+    double2* x = bt.X + g.v;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) x[i] = make_double2(0, 0);
-    double bn = vec_norm(bt.B + (size_t)s * n, n, sh);
+    double bn = vec_norm(bt.B + g.v, n, sh);
     if (threadIdx.x == 0) {
         GmState& st = bt.st[s];
         st.anorm = anorm[s];
         st.bnorm = bn;
-        st.tol = tol;
+        st.tol = tols ? tols[s] : tol;
+        st.m = ms ? ms[s] : bt.m;
         st.xnorm = 0;
         st.error = 1.0;
         st.k = 0;
@@ -429,7 +459,7 @@ __global__ void gm_init_kernel(GmBatch bt, const double* anorm, double tol, int6
         st.num_mv = 0;
         st.iterations = 0;
         st.restarts = 0;
-        st.max_restarts = max_restarts;
+        st.max_restarts = maxrs ? maxrs[s] : max_restarts;
         if (bn == 0.0) {  // zero right-hand side: x = 0 is exact
             st.done = 1;
             st.converged = 1;
@@ -486,6 +516,11 @@ void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const
     int rb = (int)((n + MV_ROWS - 1) / MV_ROWS), cb = (int)((n + MV_COLS - 1) / MV_COLS);
     ws.rb = rb;
     ws.cb = cb;
+    bt.rb = rb;
+    bt.cb = cb;
+    bt.sys = nullptr;
+    bt.ntiles = 0;
+    ws.sys_host.clear();
     size_t small = gm_small_size(m);
     size_t bytes = 0;
     auto carve = [&](size_t b) { size_t o = bytes; bytes += (b + 255) / 256 * 256; return o; };
@@ -549,6 +584,11 @@ size_t gm_prepare_external(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, i
     ws.fp32 = fp32;
     ws.rb = rb;
     ws.cb = cb;
+    bt.rb = rb;
+    bt.cb = cb;
+    bt.sys = nullptr;
+    bt.ntiles = 0;
+    ws.sys_host.clear();
     char* base = static_cast<char*>(mem);
     bt.X = reinterpret_cast<double2*>(base + oX);
     bt.B = reinterpret_cast<double2*>(base + oB);
@@ -572,8 +612,114 @@ size_t gm_prepare_external(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, i
     return bytes;
 }
 
+void gm_prepare_ragged(Context& ctx, GmWorkspace& ws, const std::vector<int64_t>& ns,
+                       const std::vector<int64_t>& ldas, const std::vector<size_t>& a_offs, int m, const void* A,
+                       bool fp32) {
+    const int nsys = (int)ns.size();
+    require(nsys >= 1 && ldas.size() == ns.size() && a_offs.size() == ns.size(), "ragged batch: bad layout");
+    std::vector<GmSys>& sys = ws.sys_host;
+    sys.assign(nsys, GmSys{});
+    size_t v = 0, q = 0, p = 0, t = 0;
+    int64_t tiles = 0, nmax = 0, npmax = 0;
+    for (int s = 0; s < nsys; ++s) {
+        GmSys& d = sys[s];
+        d.n = ns[s];
+        require(d.n >= 1 && ldas[s] >= d.n, "ragged batch: bad system size");
+        d.lda = ldas[s];
+        d.rb = (int)((d.n + MV_ROWS - 1) / MV_ROWS);
+        d.cb = (int)((d.n + MV_COLS - 1) / MV_COLS);
+        d.n_pad = (int64_t)d.rb * MV_ROWS;
+        d.a_off = a_offs[s];
+        d.v_off = v;
+        d.q_off = q;
+        d.p_off = p;
+        d.t_off = t;
+        d.tile0 = tiles;
+        v += (size_t)d.n;
+        q += (size_t)d.n * (m + 1);
+        p += (size_t)d.cb * d.n_pad;
+        t += (size_t)d.rb;
+        tiles += (int64_t)d.rb * d.cb;
+        nmax = std::max(nmax, d.n);
+        npmax = std::max(npmax, d.n_pad);
+    }
+    GmBatch& bt = ws.bt;
+    bt.nsys = nsys;
+    bt.n = nmax;
+    bt.n_pad = npmax;
+    bt.m = m;
+    bt.A = A;
+    bt.lda = 0;
+    bt.mat_stride = 0;
+    bt.ref_dotc = 0;
+    bt.qstride = 0;
+    bt.rb = bt.cb = 0;
+    bt.ntiles = tiles;
+    ws.fp32 = fp32;
+    ws.rb = ws.cb = 0;
+    const size_t small = gm_small_size(m);
+    size_t bytes = 0;
+    auto carve = [&](size_t b) { size_t o = bytes; bytes += (b + 255) / 256 * 256; return o; };
+    size_t oX = carve(sizeof(double2) * v), oB = carve(sizeof(double2) * v);
+    size_t oQ = carve(sizeof(double2) * q), oW = carve(sizeof(double2) * v);
+    size_t oP = carve(sizeof(double2) * p), oT = carve(sizeof(int) * t);
+    size_t oS = carve(sizeof(double2) * nsys * small), oSt = carve(sizeof(GmState) * nsys);
+    size_t oN = carve(sizeof(double) * nsys * 1024 + sizeof(double) * nsys);
+    size_t oD = carve(sizeof(GmSys) * nsys);
+    ws.mem.ensure(bytes);
+    char* base = ws.mem.as<char>();
+    bt.X = reinterpret_cast<double2*>(base + oX);
+    bt.B = reinterpret_cast<double2*>(base + oB);
+    bt.Q = reinterpret_cast<double2*>(base + oQ);
+    bt.W = reinterpret_cast<double2*>(base + oW);
+    bt.part = reinterpret_cast<double2*>(base + oP);
+    bt.tickets = reinterpret_cast<int*>(base + oT);
+    bt.small = reinterpret_cast<double2*>(base + oS);
+    bt.small_stride = small;
+    bt.st = reinterpret_cast<GmState*>(base + oSt);
+    ws.norm_part = reinterpret_cast<double*>(base + oN);
+    ws.anorm = ws.norm_part + (size_t)nsys * 1024;
+    GmSys* dsys = reinterpret_cast<GmSys*>(base + oD);
+    BEM_CUDA(cudaMemcpyAsync(dsys, sys.data(), sizeof(GmSys) * nsys, cudaMemcpyHostToDevice, ctx.stream));
+    bt.sys = dsys;
+    BEM_CUDA(cudaMemsetAsync(bt.tickets, 0, sizeof(int) * t, ctx.stream));
+    ws.w_in_smem = (nmax * sizeof(double2) <= 200 * 1024);
+    if (ws.w_in_smem) {
+        BEM_CUDA(cudaFuncSetAttribute(gm_arnoldi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(nmax * sizeof(double2))));
+    }
+    if (ws.graph_exec) {
+        cudaGraphExecDestroy(ws.graph_exec);
+        ws.graph_exec = nullptr;
+    }
+}
+
+size_t gm_q_total(const GmWorkspace& ws) {
+    if (ws.sys_host.empty()) return (size_t)ws.bt.nsys * ws.bt.qstride;
+    const GmSys& d = ws.sys_host.back();
+    return d.q_off + (size_t)d.n * (ws.bt.m + 1);
+}
+
 void gm_matrix_norms(Context& ctx, GmWorkspace& ws) {
     const int nb = 512;
+    if (!ws.sys_host.empty()) {
+        for (int s = 0; s < ws.bt.nsys; ++s) {
+            const GmSys& d = ws.sys_host[s];
+            dim3 g1(nb, 1);
+            if (ws.fp32)
+                batch_frob_kernel<float2><<<g1, 256, 0, ctx.stream>>>(
+                    static_cast<const float2*>(ws.bt.A) + d.a_off, d.n, d.lda, 0, ws.norm_part + (size_t)s * nb, nb);
+            else
+                batch_frob_kernel<double2><<<g1, 256, 0, ctx.stream>>>(
+                    static_cast<const double2*>(ws.bt.A) + d.a_off, d.n, d.lda, 0, ws.norm_part + (size_t)s * nb,
+                    nb);
+            BEM_CHECK_LAUNCH(&ctx);
+        }
+        finish_norms_kernel<<<(ws.bt.nsys + 127) / 128, 128, 0, ctx.stream>>>(ws.norm_part, nb, ws.bt.nsys,
+                                                                               ws.anorm);
+        BEM_CHECK_LAUNCH(&ctx);
+        return;
+    }
     dim3 grid(nb, ws.bt.nsys);
     if (ws.fp32)
         batch_frob_kernel<float2><<<grid, 256, 0, ctx.stream>>>(ws.bt.A, ws.bt.n, ws.bt.lda, ws.bt.mat_stride,
@@ -587,8 +733,27 @@ void gm_matrix_norms(Context& ctx, GmWorkspace& ws) {
 }
 
 void gm_init(Context& ctx, GmWorkspace& ws, double tol, int64_t max_restarts) {
-    gm_init_kernel<<<ws.bt.nsys, AR_THREADS, 0, ctx.stream>>>(ws.bt, ws.anorm, tol, max_restarts);
+    gm_init_kernel<<<ws.bt.nsys, AR_THREADS, 0, ctx.stream>>>(ws.bt, ws.anorm, tol, max_restarts, nullptr, nullptr,
+                                                              nullptr);
     BEM_CHECK_LAUNCH(&ctx);
+}
+
+void gm_init_each(Context& ctx, GmWorkspace& ws, const std::vector<double>& tol,
+                  const std::vector<int64_t>& max_restarts, const std::vector<int>& m) {
+    const size_t ns = (size_t)ws.bt.nsys;
+    require(tol.size() == ns && max_restarts.size() == ns && m.size() == ns, "gmres: per-system settings");
+    for (int x : m) require(x >= 1 && x <= ws.bt.m, "gmres: restart length above the batch's");
+    ws.init_args.ensure(ns * (sizeof(double) + sizeof(int64_t) + sizeof(int)));
+    char* base = ws.init_args.as<char>();
+    BEM_CUDA(cudaMemcpyAsync(base, tol.data(), ns * sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
+    BEM_CUDA(cudaMemcpyAsync(base + ns * 8, max_restarts.data(), ns * sizeof(int64_t), cudaMemcpyHostToDevice,
+                             ctx.stream));
+    BEM_CUDA(cudaMemcpyAsync(base + ns * 16, m.data(), ns * sizeof(int), cudaMemcpyHostToDevice, ctx.stream));
+    gm_init_kernel<<<ws.bt.nsys, AR_THREADS, 0, ctx.stream>>>(
+        ws.bt, ws.anorm, 0.0, 0, reinterpret_cast<const double*>(base), reinterpret_cast<const int64_t*>(base + ns * 8),
+        reinterpret_cast<const int*>(base + ns * 16));
+    BEM_CHECK_LAUNCH(&ctx);
+    ctx.sync();  // the host arrays are pageable and owned by the caller
 }
 
 static void launch_apply(Context& ctx, GmWorkspace& ws, int mode) {
@@ -596,7 +761,7 @@ static void launch_apply(Context& ctx, GmWorkspace& ws, int mode) {
         ws.hook(ctx, ws, mode, ws.hook_user);
         return;
     }
-    dim3 grid((unsigned)ws.rb, (unsigned)ws.cb, (unsigned)ws.bt.nsys);
+    dim3 grid = ws.bt.sys ? dim3((unsigned)ws.bt.ntiles) : dim3((unsigned)ws.rb, (unsigned)ws.cb, (unsigned)ws.bt.nsys);
     if (ws.fp32) {
         if (mode == MV_Q) gm_apply_kernel<float2, 0><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
         else gm_apply_kernel<float2, 1><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
@@ -651,11 +816,14 @@ void gm_run(Context& ctx, GmWorkspace& ws, int chunk, int64_t max_total_iteratio
             if (ctx.profiling) {
                 float ms = 0;
                 BEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                int64_t active = 0;
-                for (size_t s = 0; s < st.size(); ++s) active += st[s].iterations - prev[s].iterations;
-                if (active > 0)
+                double entries = 0;
+                for (size_t s = 0; s < st.size(); ++s) {
+                    const double ns = ws.sys_host.empty() ? (double)ws.bt.n : (double)ws.sys_host[s].n;
+                    entries += (double)(st[s].iterations - prev[s].iterations) * ns * ns;
+                }
+                if (entries > 0)
                     ctx.stage_add(ws.fp32 ? "gmres_matvec_fp32" : "gmres_matvec_fp64", ms, 1,
-                                  (double)active * ws.bt.n * ws.bt.n * (ws.fp32 ? 8.0 : 16.0));
+                                  entries * (ws.fp32 ? 8.0 : 16.0));
             }
             prev = st;
             bool all = true;

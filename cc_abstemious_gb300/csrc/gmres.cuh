@@ -8,14 +8,29 @@ enum { MV_START = 0, MV_Q = 1, MV_CHECK = 2 };
 
 struct GmState {
     double anorm, bnorm, tol, xnorm, error;
-    int k, need_start, check, done, converged, pad;
+    int k, need_start, check, done, converged, m;  // m: this system's restart length (<= batch m)
     long long num_mv, iterations, restarts, max_restarts;
 };
 
+// Per-system layout of a ragged batch (systems of different sizes).
+struct GmSys {
+    int64_t n, lda, n_pad;
+    size_t a_off;   // operator entries before this system's matrix
+    size_t v_off;   // X, B, W
+    size_t q_off;   // Q, Z
+    size_t p_off;   // column-chunk partial sums
+    size_t t_off;   // last-CTA tickets
+    int64_t tile0;  // first CTA of this system in the flattened mat-vec grid
+    int rb, cb;     // row blocks, column chunks
+};
+
 struct GmBatch {
-    int nsys, m, ref_dotc, pad;
-    int64_t n, n_pad, lda;
+    int nsys, m, ref_dotc, rb;
+    int64_t n, n_pad, lda;  // uniform batch (sys == nullptr); ragged: largest n
     size_t mat_stride, qstride, small_stride;
+    const GmSys* sys;   // ragged batch: per-system layout (nullptr: uniform)
+    int64_t ntiles;     // ragged: CTAs of the flattened mat-vec grid
+    int cb, pad;
     const void* A;      // nsys matrices (double2 or float2), column-major, leading dim lda
     double2* X;         // nsys x n solutions
     double2* B;         // nsys x n right-hand sides
@@ -34,6 +49,29 @@ __device__ __forceinline__ bool gm_apply_active(const GmBatch& bt, const GmState
     if (mode == MV_START) return s.need_start != 0 && !(!bt.ref_dotc && s.restarts == 0);
     if (mode == MV_Q) return s.need_start == 0 && s.check == 0;
     return s.check != 0;  // MV_CHECK
+}
+
+// A system's sizes and offsets in either layout.
+struct GmView {
+    int64_t n, lda, n_pad;
+    size_t a, v, q, p, t;
+    int rb, cb;
+};
+
+__host__ __device__ __forceinline__ GmView gm_view(const GmBatch& bt, int s) {
+    GmView v;
+    if (bt.sys) {
+        const GmSys& d = bt.sys[s];
+        v.n = d.n; v.lda = d.lda; v.n_pad = d.n_pad;
+        v.a = d.a_off; v.v = d.v_off; v.q = d.q_off; v.p = d.p_off; v.t = d.t_off;
+        v.rb = d.rb; v.cb = d.cb;
+    } else {
+        v.n = bt.n; v.lda = bt.lda; v.n_pad = bt.n_pad;
+        v.a = (size_t)s * bt.mat_stride; v.v = (size_t)s * bt.n; v.q = (size_t)s * bt.qstride;
+        v.p = (size_t)s * bt.cb * bt.n_pad; v.t = (size_t)s * bt.rb;
+        v.rb = bt.rb; v.cb = bt.cb;
+    }
+    return v;
 }
 
 struct GmSmall {
@@ -73,6 +111,8 @@ struct GmWorkspace {
     std::shared_ptr<void> precond_keep;  // owns the preconditioner data
     DevBuf zmem;
     DevBuf mem;
+    DevBuf init_args;
+    std::vector<GmSys> sys_host;  // ragged layout (empty: uniform)
     bool fp32 = false;
     bool w_in_smem = false;
     int rb = 0, cb = 0;
@@ -86,10 +126,20 @@ struct GmWorkspace {
 
 void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const void* A, int64_t lda,
                 size_t mat_stride, bool fp32, bool ref_dotc);
+// Ragged batch: system s has size ns[s], leading dimension ldas[s] and its
+// matrix at entry offset a_offs[s] of A.
+void gm_prepare_ragged(Context& ctx, GmWorkspace& ws, const std::vector<int64_t>& ns,
+                       const std::vector<int64_t>& ldas, const std::vector<size_t>& a_offs, int m, const void* A,
+                       bool fp32);
 size_t gm_prepare_external(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const void* A, int64_t lda,
                            size_t mat_stride, bool fp32, bool ref_dotc, void* mem, size_t capacity);
+// Entries of the Krylov basis Q (and of Z) over the whole batch.
+size_t gm_q_total(const GmWorkspace& ws);
 void gm_matrix_norms(Context& ctx, GmWorkspace& ws);
 void gm_init(Context& ctx, GmWorkspace& ws, double tol, int64_t max_restarts);
+// Per-system tolerance, restart count and restart length (m[s] <= batch m).
+void gm_init_each(Context& ctx, GmWorkspace& ws, const std::vector<double>& tol,
+                  const std::vector<int64_t>& max_restarts, const std::vector<int>& m);
 void gm_launch_iteration(Context& ctx, GmWorkspace& ws, cudaEvent_t ev_q0, cudaEvent_t ev_q1);
 void gm_read_states(Context& ctx, GmWorkspace& ws, std::vector<GmState>& out);
 void gm_run(Context& ctx, GmWorkspace& ws, int chunk, int64_t max_total_iterations);

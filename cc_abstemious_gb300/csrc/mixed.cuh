@@ -6,6 +6,11 @@ namespace bem {
 
 void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered, bem_cplx* incident,
                bem_solve_report* reports, bool check_vs_lu);
+// Several bodies: every frequency of every body in one ragged batch (chunks
+// of at most budget_bytes of operators; 0: a share of the free memory).
+void run_mixed_batch(Context& c, const std::vector<Problem*>& probs, bem_precond precond,
+                     bem_cplx* const* scattered, bem_cplx* const* incident, bem_solve_report* const* reports,
+                     bool check_vs_lu, size_t budget_bytes);
 // ||x - x_LU64|| / ||x_LU64|| for the unknown solved at the problem's current
 // frequency (phi for velocity/impedance conditions, vn for pressure).
 double lu_reference_error(Context& c, const Problem& p, const double* phi_host, const double* vn_host);

@@ -37,7 +37,7 @@ constexpr double PC_ETA = 2.0;
 
 // ---------------------------------------------------------------------------
 // Near-field leaf pattern (host).
-void build_pattern(const Problem& p, NearPattern& P) {
+void build_pattern(const Problem& p, NearPattern& P, bool diag_only) {
     auto leaves = cluster_leaves(p.cpts, 8, PC_LEAF);
     P.n = p.n;
     P.nc = (int)leaves.size();
@@ -56,7 +56,7 @@ void build_pattern(const Problem& p, NearPattern& P) {
     P.pair_dst.clear();
     for (int c = 0; c < P.nc; ++c) {
         std::vector<int> near{c};
-        for (int d = 0; d < P.nc; ++d) {
+        for (int d = 0; d < P.nc && !diag_only; ++d) {
             if (d == c) continue;
             bool adm = std::fmin(leaves[c].diam, leaves[d].diam) <= PC_ETA * box_distance(leaves[c], leaves[d]);
             if (!adm) near.push_back(d);
@@ -85,21 +85,47 @@ void build_pattern(const Problem& p, NearPattern& P) {
 // ---------------------------------------------------------------------------
 // Exact inverse of every diagonal leaf block, [A_cc | I] reduced by
 // Gauss-Jordan with partial pivoting in FP32, one CTA per (block, system).
+struct PcDev {
+    const int64_t *cl_off, *cl_idx, *nb_blk;
+    const int32_t *nb_off, *nb_d;
+    const float2* M;
+    size_t Mstride;
+    int offdiag, nc;
+    // several bodies in one batch: body of each system, first leaf of each
+    // body, offset of each system's blocks in M (all nullptr: one body)
+    const int32_t *sys_body, *body_leaf0;
+    const size_t* sys_moff;
+};
+
+// Leaf index of the c-th leaf of system s's body, or -1 past its last leaf.
+__device__ __forceinline__ int pc_leaf(const PcDev& pc, int s, int c) {
+    if (!pc.sys_body) return c < pc.nc ? c : -1;
+    const int b = pc.sys_body[s];
+    const int l0 = pc.body_leaf0[b];
+    return c < pc.body_leaf0[b + 1] - l0 ? l0 + c : -1;
+}
+
+__device__ __forceinline__ size_t pc_moff(const PcDev& pc, int s) {
+    return pc.sys_moff ? pc.sys_moff[s] : (size_t)s * pc.Mstride;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) pc_diag_inverse_kernel(const T* __restrict__ A, int64_t lda, size_t mstride,
-                                                              const int64_t* __restrict__ cl_off,
-                                                              const int64_t* __restrict__ cl_idx,
-                                                              const int32_t* __restrict__ nb_off,
-                                                              const int64_t* __restrict__ nb_blk,
-                                                              float2* __restrict__ M, size_t Mstride) {
+                                                              const GmSys* __restrict__ sys, PcDev pc,
+                                                              float2* __restrict__ M) {
     extern __shared__ float2 aug[];  // b x 2b, row-major
     __shared__ int s_piv;
     __shared__ float2 fcol[PC_LEAF];  // elimination factors of the current column
-    const int c = blockIdx.x, s = blockIdx.y;
+    const int s = blockIdx.y;
+    const int c = pc_leaf(pc, s, blockIdx.x);
+    if (c < 0) return;
+    const int64_t* cl_off = pc.cl_off;
+    const int64_t* cl_idx = pc.cl_idx;
     const int64_t o = cl_off[c];
     const int b = (int)(cl_off[c + 1] - o);
     const int w = 2 * b;
-    const T* As = A + (size_t)s * mstride;
+    if (sys) lda = sys[s].lda;
+    const T* As = A + (sys ? sys[s].a_off : (size_t)s * mstride);
     for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
         int i = t % b, j = t / b;
         T v = As[cl_idx[o + j] * lda + cl_idx[o + i]];
@@ -144,7 +170,7 @@ __global__ void __launch_bounds__(256) pc_diag_inverse_kernel(const T* __restric
         __syncthreads();
         // the pivot column of the other rows was consumed; zero it for clarity
     }
-    float2* Mo = M + (size_t)s * Mstride + nb_blk[nb_off[c]];  // first neighbour is the block itself
+    float2* Mo = M + pc_moff(pc, s) + pc.nb_blk[pc.nb_off[c]];  // first neighbour is the block itself
     for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
         int i = t % b, j = t / b;
         Mo[(size_t)j * b + i] = aug[i * w + b + j];
@@ -179,29 +205,23 @@ __device__ __forceinline__ void pc_block_apply(int c, const int64_t* cl_off, con
     if (i < bc) z[cl_idx[oc + i]] = acc;
 }
 
-struct PcDev {
-    const int64_t *cl_off, *cl_idx, *nb_blk;
-    const int32_t *nb_off, *nb_d;
-    const float2* M;
-    size_t Mstride;
-    int offdiag;
-};
-
 __global__ void __launch_bounds__(PC_LEAF) pc_apply_gmres_kernel(PcDev pc, GmBatch bt) {
     const int s = blockIdx.y;
     const GmState& st = bt.st[s];
     if (!gm_apply_active(bt, st, MV_Q)) return;
-    const double2* q = bt.Q + (size_t)s * bt.qstride + (size_t)st.k * bt.n;
-    double2* z = bt.Z + (size_t)s * bt.qstride + (size_t)st.k * bt.n;
-    pc_block_apply(blockIdx.x, pc.cl_off, pc.cl_idx, pc.nb_off, pc.nb_d, pc.nb_blk, pc.M + (size_t)s * pc.Mstride, q,
-                   z, pc.offdiag);
+    const int c = pc_leaf(pc, s, blockIdx.x);
+    if (c < 0) return;
+    const GmView g = gm_view(bt, s);
+    const double2* q = bt.Q + g.q + (size_t)st.k * g.n;
+    double2* z = bt.Z + g.q + (size_t)st.k * g.n;
+    pc_block_apply(c, pc.cl_off, pc.cl_idx, pc.nb_off, pc.nb_d, pc.nb_blk, pc.M + pc_moff(pc, s), q, z, pc.offdiag);
 }
 
 // Probe form: Y[:, q] = M_s Z[:, q] for nprobe vectors (training).
 __global__ void __launch_bounds__(PC_LEAF) pc_apply_probes_kernel(PcDev pc, int s, const double2* __restrict__ Zp,
                                                                   double2* __restrict__ Yp, int64_t n) {
     const int q = blockIdx.y;
-    pc_block_apply(blockIdx.x, pc.cl_off, pc.cl_idx, pc.nb_off, pc.nb_d, pc.nb_blk, pc.M + (size_t)s * pc.Mstride,
+    pc_block_apply(blockIdx.x, pc.cl_off, pc.cl_idx, pc.nb_off, pc.nb_d, pc.nb_blk, pc.M + pc_moff(pc, s),
                    Zp + (size_t)q * n, Yp + (size_t)q * n, pc.offdiag);
 }
 
@@ -551,9 +571,12 @@ int learned_num_params() { return NPARAM; }
 // ---------------------------------------------------------------------------
 // Preconditioner data of a batch (one body, nsys frequencies).
 struct PcData {
-    NearPattern pat;
+    NearPattern pat;  // one body, or the concatenated leaves of several
     DevBuf cl_off, cl_idx, nb_off, nb_d, nb_blk, M;
-    bool offdiag = false;
+    DevBuf sys_body, body_leaf0, sys_moff;  // several bodies
+    bool multi = false;
+    int nc_max = 0;  // leaves of the largest body
+    size_t m_total = 0;
     PcDev dev(int use_off) const {
         PcDev d;
         d.cl_off = cl_off.as<int64_t>();
@@ -564,6 +587,10 @@ struct PcData {
         d.M = M.as<float2>();
         d.Mstride = (size_t)pat.entries;
         d.offdiag = use_off;
+        d.nc = pat.nc;
+        d.sys_body = multi ? sys_body.as<int32_t>() : nullptr;
+        d.body_leaf0 = multi ? body_leaf0.as<int32_t>() : nullptr;
+        d.sys_moff = multi ? sys_moff.as<size_t>() : nullptr;
         return d;
     }
 };
@@ -580,27 +607,28 @@ static void upload_pattern(Context& c, PcData& d) {
     up(d.nb_blk, d.pat.nb_blk.data(), sizeof(int64_t) * d.pat.nb_blk.size());
 }
 
-// Block-Jacobi inverses of every system of a batch into d.M.
-static void diag_inverses(Context& c, PcData& d, int nsys, const void* A, bool fp32, int64_t lda, size_t mstride) {
-    d.M.ensure(sizeof(float2) * (size_t)d.pat.entries * nsys);
-    BEM_CUDA(cudaMemsetAsync(d.M.p, 0, sizeof(float2) * (size_t)d.pat.entries * nsys, c.stream));
+// Block-Jacobi inverses of every system of a batch into d.M (`sys`: ragged
+// batch layout, else uniform with lda / mstride).
+static void diag_inverses(Context& c, PcData& d, int nsys, const void* A, bool fp32, int64_t lda, size_t mstride,
+                          const GmSys* sys = nullptr) {
+    const size_t total = d.multi ? d.m_total : (size_t)d.pat.entries * nsys;
+    d.M.ensure(sizeof(float2) * std::max<size_t>(total, 1));
+    BEM_CUDA(cudaMemsetAsync(d.M.p, 0, sizeof(float2) * total, c.stream));
     int bmax = 0;
     for (int cc = 0; cc < d.pat.nc; ++cc)
         bmax = std::max(bmax, (int)(d.pat.cl_off[cc + 1] - d.pat.cl_off[cc]));
     size_t smem = sizeof(float2) * (size_t)bmax * 2 * bmax;
-    dim3 grid((unsigned)d.pat.nc, (unsigned)nsys);
+    dim3 grid((unsigned)(d.multi ? d.nc_max : d.pat.nc), (unsigned)nsys);
     if (fp32) {
         BEM_CUDA(cudaFuncSetAttribute(pc_diag_inverse_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-        pc_diag_inverse_kernel<float2><<<grid, 256, smem, c.stream>>>(
-            static_cast<const float2*>(A), lda, mstride, d.cl_off.as<int64_t>(), d.cl_idx.as<int64_t>(),
-            d.nb_off.as<int32_t>(), d.nb_blk.as<int64_t>(), d.M.as<float2>(), (size_t)d.pat.entries);
+        pc_diag_inverse_kernel<float2><<<grid, 256, smem, c.stream>>>(static_cast<const float2*>(A), lda, mstride,
+                                                                      sys, d.dev(0), d.M.as<float2>());
     } else {
         BEM_CUDA(cudaFuncSetAttribute(pc_diag_inverse_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-        pc_diag_inverse_kernel<double2><<<grid, 256, smem, c.stream>>>(
-            static_cast<const double2*>(A), lda, mstride, d.cl_off.as<int64_t>(), d.cl_idx.as<int64_t>(),
-            d.nb_off.as<int32_t>(), d.nb_blk.as<int64_t>(), d.M.as<float2>(), (size_t)d.pat.entries);
+        pc_diag_inverse_kernel<double2><<<grid, 256, smem, c.stream>>>(static_cast<const double2*>(A), lda, mstride,
+                                                                       sys, d.dev(0), d.M.as<float2>());
     }
     BEM_CHECK_LAUNCH(&c);
 }
@@ -649,7 +677,7 @@ struct PcHookData {
 static void pc_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
     (void)mode;
     PcHookData& h = *static_cast<PcHookData*>(user);
-    dim3 grid((unsigned)h.data.pat.nc, (unsigned)ws.bt.nsys);
+    dim3 grid((unsigned)(h.data.multi ? h.data.nc_max : h.data.pat.nc), (unsigned)ws.bt.nsys);
     pc_apply_gmres_kernel<<<grid, PC_LEAF, 0, c.stream>>>(h.data.dev(h.use_off ? 1 : 0), ws.bt);
     BEM_CHECK_LAUNCH(&c);
 }
@@ -659,7 +687,8 @@ bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond k
     // without a trained or loaded network the learned form falls back to block-Jacobi
     if (kind == BEM_PRECOND_LEARNED && !(c.net && c.net->ready)) kind = BEM_PRECOND_BLOCK_JACOBI;
     auto h = std::make_shared<PcHookData>();
-    build_pattern(p, h->data.pat);
+    // block-Jacobi needs the diagonal blocks only
+    build_pattern(p, h->data.pat, kind != BEM_PRECOND_LEARNED);
     upload_pattern(c, h->data);
     const int nsys = ws.bt.nsys;
     diag_inverses(c, h->data, nsys, ws.bt.A, ws.fp32, ws.bt.lda, ws.bt.mat_stride);
@@ -673,7 +702,81 @@ bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond k
         h->use_off = true;
         c.sync();
     }
-    ws.zmem.ensure(sizeof(double2) * (size_t)nsys * ws.bt.qstride);
+    ws.zmem.ensure(sizeof(double2) * gm_q_total(ws));
+    ws.bt.Z = ws.zmem.as<double2>();
+    ws.precond = pc_hook;
+    ws.precond_user = h.get();
+    ws.precond_keep = h;
+    return kind;
+}
+
+// Several bodies in one ragged batch: system s belongs to body sys_body[s]
+// (wavenumber ks[s]); the bodies' leaf patterns are concatenated and every
+// system's blocks are stored back to back.
+bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies, const std::vector<int>& sys_body,
+                                GmWorkspace& ws, bem_precond kind, const double* ks) {
+    require(kind == BEM_PRECOND_BLOCK_JACOBI || kind == BEM_PRECOND_LEARNED, "unknown preconditioner");
+    require(!ws.sys_host.empty() && (int)sys_body.size() == ws.bt.nsys, "multi-body preconditioner: bad batch");
+    if (kind == BEM_PRECOND_LEARNED && !(c.net && c.net->ready)) kind = BEM_PRECOND_BLOCK_JACOBI;
+    const bool learned = kind == BEM_PRECOND_LEARNED;
+    auto h = std::make_shared<PcHookData>();
+    PcData& d = h->data;
+    const int nb = (int)bodies.size(), nsys = ws.bt.nsys;
+    std::vector<NearPattern> pats((size_t)nb);
+    std::vector<int32_t> leaf0(1, 0);
+    NearPattern& P = d.pat;
+    P.cl_off.assign(1, 0);
+    P.nb_off.assign(1, 0);
+    for (int b = 0; b < nb; ++b) {
+        build_pattern(*bodies[(size_t)b], pats[(size_t)b], !learned);
+        const NearPattern& q = pats[(size_t)b];
+        const int64_t idx0 = (int64_t)P.cl_idx.size();
+        const int32_t nb0 = (int32_t)P.nb_d.size();
+        for (int l = 0; l < q.nc; ++l) {
+            P.cl_off.push_back(idx0 + q.cl_off[(size_t)l + 1]);
+            P.nb_off.push_back(nb0 + q.nb_off[(size_t)l + 1]);
+        }
+        P.cl_idx.insert(P.cl_idx.end(), q.cl_idx.begin(), q.cl_idx.end());
+        for (int32_t x : q.nb_d) P.nb_d.push_back(x + leaf0.back());
+        P.nb_blk.insert(P.nb_blk.end(), q.nb_blk.begin(), q.nb_blk.end());
+        d.nc_max = std::max(d.nc_max, q.nc);
+        leaf0.push_back(leaf0.back() + q.nc);
+    }
+    P.nc = leaf0.back();
+    P.entries = 0;
+    std::vector<size_t> moff((size_t)nsys);
+    size_t tot = 0;
+    for (int s = 0; s < nsys; ++s) {
+        moff[(size_t)s] = tot;
+        tot += (size_t)pats[(size_t)sys_body[(size_t)s]].entries;
+    }
+    d.m_total = tot;
+    d.multi = true;
+    upload_pattern(c, d);
+    d.sys_body.ensure(sizeof(int32_t) * nsys);
+    d.body_leaf0.ensure(sizeof(int32_t) * leaf0.size());
+    d.sys_moff.ensure(sizeof(size_t) * nsys);
+    BEM_CUDA(cudaMemcpyAsync(d.sys_body.p, sys_body.data(), sizeof(int32_t) * nsys, cudaMemcpyHostToDevice, c.stream));
+    BEM_CUDA(cudaMemcpyAsync(d.body_leaf0.p, leaf0.data(), sizeof(int32_t) * leaf0.size(), cudaMemcpyHostToDevice,
+                             c.stream));
+    BEM_CUDA(cudaMemcpyAsync(d.sys_moff.p, moff.data(), sizeof(size_t) * nsys, cudaMemcpyHostToDevice, c.stream));
+    diag_inverses(c, d, nsys, ws.bt.A, ws.fp32, 0, 0, ws.bt.sys);
+    h->use_off = false;
+    if (learned) {
+        PairBufs pb;
+        for (int b = 0; b < nb; ++b) {
+            if (pats[(size_t)b].npairs == 0) continue;
+            upload_pairs(c, pats[(size_t)b], pb);
+            for (int s = 0; s < nsys; ++s)
+                if (sys_body[(size_t)s] == b)
+                    learned_entries(c, *bodies[(size_t)b], *c.net, pats[(size_t)b], pb, ks[s],
+                                    d.M.as<float2>() + moff[(size_t)s]);
+            c.sync();  // the pair buffers are reused by the next body
+        }
+        h->use_off = true;
+    }
+    c.sync();
+    ws.zmem.ensure(sizeof(double2) * gm_q_total(ws));
     ws.bt.Z = ws.zmem.as<double2>();
     ws.precond = pc_hook;
     ws.precond_user = h.get();

@@ -33,10 +33,15 @@ struct LearnedNet {
 };
 
 int learned_num_params();
-void build_pattern(const Problem& p, NearPattern& P);
+// Leaves of p's cluster tree and their near neighbours (diag_only: each leaf
+// with itself only, the block-Jacobi pattern).
+void build_pattern(const Problem& p, NearPattern& P, bool diag_only = false);
 // Installs the preconditioner on the batch; returns the kind actually used
 // (the learned form falls back to block-Jacobi when no network is available).
 bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks);
+// Several bodies in a ragged batch: system s belongs to bodies[sys_body[s]].
+bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies, const std::vector<int>& sys_body,
+                                GmWorkspace& ws, bem_precond kind, const double* ks);
 double learned_train(Context& c, std::vector<Problem*>& probs, int steps, int nprobe, double lr, uint64_t seed,
                      std::vector<double>& losses);
 void learned_mlp_eval(Context& c, int64_t P, const float* F, const float* dO, float* O, float* grad);

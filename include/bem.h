@@ -217,6 +217,19 @@ BEM_API bem_status bem_convert_to_pressure(const bem_problem* p, double frequenc
 BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* p, bem_form form, bem_precond precond,
                            bem_cplx* scattered, bem_cplx* incident, bem_solve_report* reports,
                            int check_vs_lu);
+/* Several bodies in one batch (mixed form).  No counterpart in the reference,
+ * which runs one Analysis per body (analysis.rs:87-111): here every frequency
+ * of every body is assembled by one multi-body launch and all systems are
+ * solved by one batched GMRES over systems of different sizes.  scattered[b],
+ * incident[b] and reports[b] are the per-body arrays of bem_run (the pointer
+ * arrays, or any entry, may be NULL).  max_operator_bytes bounds the operators
+ * held at once (bodies are grouped into chunks; 0: a share of the free device
+ * memory).  Bodies with a classical formulation and a pressure condition keep
+ * an FP64 operator and run one by one as in bem_run. */
+BEM_API bem_status bem_run_batch(bem_ctx* ctx, bem_problem* const* problems, int nprob, bem_precond precond,
+                                 bem_cplx* const* scattered, bem_cplx* const* incident,
+                                 bem_solve_report* const* reports, int check_vs_lu,
+                                 int64_t max_operator_bytes);
 /* Surface solutions of the last bem_run (n per frequency, frequency-major). */
 BEM_API bem_status bem_last_surface(bem_ctx* ctx, const bem_problem* p, bem_cplx* phi, bem_cplx* vn);
 
