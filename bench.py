@@ -49,6 +49,14 @@ def parse():
     ap.add_argument("--nfreq", type=int, default=16)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="one mixed run (for ncu launch lists)")
+    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "perturbed_spheres", "held_out_learned"],
+                    help="rigid_sphere_bm (the metric's configuration, default); perturbed_spheres (bodies of "
+                         "500-5000 triangles x 8 frequencies in one batch); held_out_learned (learned vs "
+                         "block-Jacobi on a held-out 20000-triangle body)")
+    ap.add_argument("--bodies", type=int, default=256, help="perturbed_spheres: number of bodies")
+    ap.add_argument("--train-bodies", type=int, default=16, help="held_out_learned: training bodies")
+    ap.add_argument("--train-steps", type=int, default=400, help="held_out_learned: training steps")
+    ap.add_argument("--held-out-tri", type=int, default=20000, help="held_out_learned: triangles")
     return ap.parse_args()
 
 
@@ -174,6 +182,10 @@ def run_reference_arm(args, inp):
 
 def main():
     args = parse()
+    if args.workload == "perturbed_spheres":
+        return bench_perturbed_spheres(args)
+    if args.workload == "held_out_learned":
+        return bench_held_out_learned(args)
     rank, world, local = dist_env()
     from cc_abstemious_gb300 import workloads
     workdir = tempfile.mkdtemp(prefix="bem_bench_")
@@ -355,6 +367,261 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# Further workloads (one JSON line each, same keys as the default line).
+
+def _timed_region(args, device, fn, stream):
+    """W warm-up calls, then K calls between CUDA events on the library stream,
+    clocks sampled meanwhile; returns (ms per call, clocks)."""
+    import torch
+    for _ in range(max(args.warmup, 3)):
+        fn()
+    clocks = Clocks(device)
+    clocks.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    return e0.elapsed_time(e1) / args.steps, clk
+
+
+def _roofline_from_profile(prof, what):
+    hbm_peak, peak_kind = measured_peaks()
+    mv = prof.get("gmres_matvec_fp32", {})
+    achieved = mv["bytes"] / (mv["ms"] * 1e-3) / 1e9 if mv.get("ms") else None
+    ratio = ncu_traffic_ratio()
+    alg = mv["bytes"] / max(mv["launches"], 1) if mv else None
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak if achieved else None,
+            "traffic": ratio * alg if (ratio and alg) else None,
+            "kernel": "gm_apply_kernel<float2, 0> (" + what + ")", "algorithmic_bytes_per_launch": alg,
+            "peak_kind": peak_kind + " (burst copy)",
+            "traffic_note": "ncu dram read+write / algorithmic bytes of the same kernel on the rigid-sphere "
+                            "case (profiles/gm_apply_fp32_rigid_sphere_bm.md), scaled to this launch"}
+
+
+def bench_perturbed_spheres(args):
+    """Bodies r = 1 + sum a_lm Y_lm (l <= 4), 500-5000 triangles each, impedance
+    Z = rho c (1 + 0.2 i), Burton-Miller, 8 frequencies ka 0.5..8 each: all
+    bodies and frequencies in one batch (bem_run_batch).  GMRES tolerance 1e-8
+    on the backward error, so the forward error stays below 1e-6."""
+    import numpy as np
+    import torch
+    import cc_abstemious_gb300 as bem
+    from cc_abstemious_gb300 import workloads
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    workdir = tempfile.mkdtemp(prefix="bem_bench_ps_")
+    inps = workloads.perturbed_spheres(workdir, count=args.bodies, seed=0, nfreq=8, tol=1e-8)
+    if args.impl == "reference":
+        return _reference_arm_generic(args, inps[len(inps) // 2], "perturbed_spheres",
+                                      {"bodies": len(inps), "frequencies_per_body": 8})
+    ctx = bem.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    texts = [json.dumps(d) for d in inps]
+    pds = [bem.PreData.from_json(t, ctx=ctx) for t in texts]
+    ns = [pd.n for pd in pds]
+    nsys = sum(len(pd.frequencies) for pd in pds)
+    pc = None if args.precond == "none" else args.precond
+    last = {}
+
+    def step():
+        last["out"] = bem.run_batch(pds, precond=pc, ctx=ctx)
+
+    launches0 = ctx.kernel_launches
+    ms, clk = _timed_region(args, local, step, stream)
+    gpu_launches = (ctx.kernel_launches - launches0) * args.steps // (args.steps + max(args.warmup, 3))
+    value = world * nsys * 1000.0 / ms
+    iters = [r["iterations"] for _, reps in last["out"] for r in reps]
+
+    # end to end: JSON text + mesh files on the host -> results on the host
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        p2 = [bem.PreData.from_json(t, ctx=ctx) for t in texts]
+        bem.run_batch(p2, precond=pc, ctx=ctx)
+        del p2
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    nfp = pds[0].nfp
+    h2d = sum(8 * 3 * pd.info["mesh_nodes"] + 8 * 5 * pd.n + 8 * 3 * pd.nfp for pd in pds)
+    d2h = sum(16 * 2 * len(pd.frequencies) * pd.nfp for pd in pds)
+
+    # plain FP64 drop-in form, body by body (one pass)
+    plain = None
+    if not args.no_plain:
+        sc = np.zeros((8, nfp), dtype=np.complex128)
+        inc = np.zeros((8, nfp), dtype=np.complex128)
+        reps = (bem.SolveReport * 8)()
+        ep0, ep1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ep0.record(stream)
+        pit = []
+        for pd in pds:
+            ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_PLAIN_FP64, 0, bem._ptr(sc), bem._ptr(inc), reps, 0))
+            pit += [reps[i].iterations for i in range(len(pd.frequencies))]
+        ep1.record(stream)
+        ep1.synchronize()
+        pms = ep0.elapsed_time(ep1)
+        plain = {"value": nsys * 1000.0 / pms, "unit": UNIT, "ms_per_step": pms,
+                 "iterations_mean": float(np.mean(pit)), "iterations_max": int(max(pit))}
+
+    # error against FP64 LU: the smallest, a middle and the largest body, all
+    # their frequencies (each system's GMRES is independent of the others)
+    order = np.argsort(ns)
+    pick = sorted({int(order[0]), int(order[len(order) // 2]), int(order[-1])})
+    chk = bem.run_batch([pds[i] for i in pick], precond=pc, check_vs_lu=True, ctx=ctx)
+    errs = {"body%d_N%d" % (i, ns[i]): max(r["rel_err_vs_lu"] for r in reps) for i, (_, reps) in zip(pick, chk)}
+
+    ctx.set_profiling(True)
+    bem.run_batch(pds, precond=pc, ctx=ctx)
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    roofline = _roofline_from_profile(prof, "ragged batch over all bodies and frequencies")
+
+    threads = max((os.cpu_count() or 2) // 2, 2)
+    mid = int(order[len(order) // 2])
+    cv, cdt, sample = cpu_reference(inps[mid], 1, threads)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 operator / fp64 vectors (complex)",
+        "data": "synthetic (seeded harmonic-perturbed spheres, no dataset)",
+        "config": {"workload": "perturbed_spheres", "bodies": len(pds), "frequencies_per_body": 8,
+                   "systems": nsys, "n_min": int(min(ns)), "n_max": int(max(ns)), "n_mean": float(np.mean(ns)),
+                   "ka": [0.5, 8.0], "bc": "impedance rho c (1 + 0.2i)", "solver": "GMRES tol 1e-8",
+                   "form": "one multi-body assembly launch + one ragged batched GMRES",
+                   "precond": args.precond,
+                   "l2": "operators %.1f GB > L2 (no flush needed)" % (8e-9 * sum(
+                       (-(-pd.n // 64) * 64) * pd.n * len(pd.frequencies) for pd in pds)),
+                   "parallelism": "replicas only"},
+        "e2e": {"value": world * nsys * 1000.0 / e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "note": "JSON text + VTK files on host -> results on host"},
+        "gpu_launches": gpu_launches, "roofline": roofline,
+        "cpu_baseline": {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample + "; the median-size body; oracle/ C restatement"},
+        "clocks": clk, "plain_fp64": plain,
+        "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
+        "rel_err_vs_fp64_lu": errs, "max_rel_err_vs_fp64_lu": max(errs.values()),
+        "gmres_iterations_mean": float(np.mean(iters)), "gmres_iterations_max": int(max(iters)),
+        "stages_ms": {k: v["ms"] for k, v in prof.items()},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def bench_held_out_learned(args):
+    """Learned preconditioner on a held-out body: the network is trained on the
+    GPU on operators of perturbed spheres drawn like the batch workload, then a
+    held-out sphere of the same distribution (20000 triangles, ka 4..16 at 12
+    frequencies, GMRES tolerance 1e-6) is solved with no preconditioner,
+    block-Jacobi and the learned correction."""
+    import numpy as np
+    import torch
+    import cc_abstemious_gb300 as bem
+    from cc_abstemious_gb300 import workloads
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    workdir = tempfile.mkdtemp(prefix="bem_bench_lh_")
+    kas = np.linspace(4.0, 16.0, 12)
+    held = workloads.perturbed_sphere_input(workdir, 777777, args.held_out_tri, kas, tol=1e-6)
+    if args.impl == "reference":
+        return _reference_arm_generic(args, held, "held_out_learned", {"n_triangles": args.held_out_tri})
+    ctx = bem.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    train = workloads.perturbed_spheres(workdir, count=args.train_bodies, seed=1, nfreq=8, tri_lo=500,
+                                        tri_hi=3000)
+    tpds = [bem.PreData.from_dict(d, ctx=ctx) for d in train]
+    t0 = time.perf_counter()
+    losses = bem.learned_train(tpds, steps=args.train_steps, nprobe=8, lr=2e-3, seed=5, ctx=ctx)
+    train_s = time.perf_counter() - t0
+    del tpds
+    pd = bem.PreData.from_dict(held, ctx=ctx)
+    nf = len(pd.frequencies)
+    sc = np.zeros((nf, pd.nfp), dtype=np.complex128)
+    inc = np.zeros((nf, pd.nfp), dtype=np.complex128)
+    results = {}
+    for name, code in (("none", 0), ("block_jacobi", 1), ("learned", 2)):
+        reps = (bem.SolveReport * nf)()
+
+        def step():
+            ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_MIXED, code, bem._ptr(sc), bem._ptr(inc), reps, 0))
+
+        ms, clk = _timed_region(args, local, step, stream)
+        results[name] = {"value": nf * 1000.0 / ms, "ms_per_step": ms, "clocks": clk,
+                         "iterations": [reps[i].iterations for i in range(nf)],
+                         "precond_used": [reps[i].precond for i in range(nf)]}
+    # FP64 LU error of the learned form at the lowest and highest ka
+    errs = {}
+    for i in (0, nf - 1):
+        one = dict(held, frequency={"List": {"values": [held["frequency"]["List"]["values"][i]]}})
+        p1 = bem.PreData.from_dict(one, ctx=ctx)
+        r1 = (bem.SolveReport * 1)()
+        s1 = np.zeros((1, pd.nfp), dtype=np.complex128)
+        ctx.check(ctx.lib.bem_run(ctx.h, p1.h, bem.FORM_MIXED, 2, bem._ptr(s1), bem._ptr(s1), r1, 1))
+        errs["ka%.2f" % kas[i]] = r1[0].rel_err_vs_lu
+        del p1
+    plain = None
+    if not args.no_plain:
+        reps = (bem.SolveReport * nf)()
+        ep0, ep1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ep0.record(stream)
+        ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_PLAIN_FP64, 0, bem._ptr(sc), bem._ptr(inc), reps, 0))
+        ep1.record(stream)
+        ep1.synchronize()
+        pms = ep0.elapsed_time(ep1)
+        plain = {"value": nf * 1000.0 / pms, "unit": UNIT, "ms_per_step": pms,
+                 "iterations": [reps[i].iterations for i in range(nf)]}
+    ctx.set_profiling(True)
+    ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_MIXED, 2, bem._ptr(sc), bem._ptr(inc),
+                              (bem.SolveReport * nf)(), 0))
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    value = results["learned"]["value"]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": results["learned"]["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32 operator / fp64 vectors (complex); bf16 network",
+        "data": "synthetic (seeded harmonic-perturbed spheres, no dataset)",
+        "config": {"workload": "held_out_learned", "n_unknowns": pd.n, "frequencies": nf, "ka": [4.0, 16.0],
+                   "solver": "GMRES tol 1e-6", "precond": "learned (block-Jacobi + MLP near-field correction)",
+                   "training": {"bodies": len(train), "steps": args.train_steps, "seconds": train_s,
+                                "loss_first": float(np.mean(losses[:10])), "loss_last": float(np.mean(losses[-10:]))},
+                   "parallelism": "replicas only"},
+        "clocks": results["learned"]["clocks"], "by_precond": results, "plain_fp64": plain,
+        "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
+        "rel_err_vs_fp64_lu": errs, "max_rel_err_vs_fp64_lu": max(errs.values()),
+        "roofline": _roofline_from_profile(prof, "12 frequencies of the held-out body"),
+        "stages_ms": {k: v["ms"] for k, v in prof.items()},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def _reference_arm_generic(args, inp, workload, cfg):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    threads = max((os.cpu_count() or 2) // 2, 2)
+    vals, t_total, sample = [], 0.0, ""
+    for _ in range(max(args.steps, 1)):
+        v, dt, sample = cpu_reference(inp, 1, threads)
+        vals.append(v)
+        t_total += dt
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 complex",
+            "data": "synthetic", "config": dict(cfg, workload=workload, parallelism="replicas only"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample + " per step; oracle/ C restatement of the reference"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

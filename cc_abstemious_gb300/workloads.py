@@ -90,8 +90,8 @@ def perturbed_sphere_input(workdir, body_seed, n_tri, ka_values, tol=1e-6):
                       bc={"bc_type": "Impedance", "value": z})
 
 
-def perturbed_spheres(workdir, count=256, seed=0, nfreq=8, tri_lo=500, tri_hi=5000):
+def perturbed_spheres(workdir, count=256, seed=0, nfreq=8, tri_lo=500, tri_hi=5000, tol=1e-6):
     rng = np.random.default_rng(seed)
     counts = rng.integers(tri_lo, tri_hi + 1, size=count)
-    return [perturbed_sphere_input(workdir, 1000 * seed + b, int(t), np.linspace(0.5, 8.0, nfreq))
+    return [perturbed_sphere_input(workdir, 1000 * seed + b, int(t), np.linspace(0.5, 8.0, nfreq), tol=tol)
             for b, t in enumerate(counts)]
