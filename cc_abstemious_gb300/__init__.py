@@ -20,7 +20,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (BemError, FORM_MIXED, FORM_PLAIN_FP64, MEM_DEVICE, MEM_HOST, PRECOND_BLOCK_JACOBI,
-                   PRECOND_LEARNED, PRECOND_NONE, SIDE_LHS, SIDE_RHS, SolveReport)
+                   PRECOND_LEARNED, PRECOND_LU, PRECOND_NONE, SIDE_LHS, SIDE_RHS, SolveReport)
 
 __all__ = ["Analysis", "Context", "PreData", "FPResult", "BemError", "get_dense_surface_matrices",
            "get_dense_field_matrices", "get_surface_row_or_column", "get_incident_surface", "get_incident_field",
@@ -371,7 +371,7 @@ class Analysis:
         reps = (SolveReport * max(nf, 1))()
         f = FORM_MIXED if form == "mixed" else FORM_PLAIN_FP64
         pc = {None: PRECOND_NONE, "none": PRECOND_NONE, "block_jacobi": PRECOND_BLOCK_JACOBI,
-              "learned": PRECOND_LEARNED}[precond]
+              "learned": PRECOND_LEARNED, "lu": PRECOND_LU}[precond]
         st = ctx.lib.bem_run(ctx.h, pd.h, f, pc, _ptr(sc), _ptr(inc), reps, 1 if check_vs_lu else 0)
         ctx.check(st)
         self.results = [FPResult(float(pd.frequencies[i]), sc[i, :nfp].copy(), inc[i, :nfp].copy())
@@ -402,7 +402,7 @@ class Analysis:
 
 
 _PRECONDS = {None: PRECOND_NONE, "none": PRECOND_NONE, "block_jacobi": PRECOND_BLOCK_JACOBI,
-             "learned": PRECOND_LEARNED}
+             "learned": PRECOND_LEARNED, "lu": PRECOND_LU}
 
 
 def run_batch(predatas, precond=None, check_vs_lu=False, max_operator_bytes=0, ctx=None):

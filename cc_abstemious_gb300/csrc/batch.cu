@@ -278,8 +278,11 @@ void run_mixed_batch(Context& c, const std::vector<Problem*>& probs, bem_precond
     while (i < batched.size()) {
         std::vector<BodyPlan*> chunk;
         size_t bytes = 0;
-        while (i < batched.size() && (chunk.empty() || bytes + batched[i]->op_bytes <= budget_bytes)) {
-            bytes += batched[i]->op_bytes;
+        // the LU preconditioner keeps a factored copy of every operator
+        const double per_op = precond == BEM_PRECOND_LU ? 2.2 : 1.0;
+        while (i < batched.size() &&
+               (chunk.empty() || (double)bytes + per_op * (double)batched[i]->op_bytes <= (double)budget_bytes)) {
+            bytes += (size_t)(per_op * (double)batched[i]->op_bytes);
             chunk.push_back(batched[i]);
             ++i;
         }

@@ -776,8 +776,8 @@ void gm_launch_iteration(Context& ctx, GmWorkspace& ws, cudaEvent_t ev_q0, cudaE
     launch_apply(ctx, ws, MV_START);
     gm_start_kernel<<<nsys, AR_THREADS, 0, ctx.stream>>>(ws.bt);
     BEM_CHECK_LAUNCH(&ctx);
-    if (ev_q0) BEM_CUDA(cudaEventRecord(ev_q0, ctx.stream));
     if (ws.precond) ws.precond(ctx, ws, MV_Q, ws.precond_user);
+    if (ev_q0) BEM_CUDA(cudaEventRecord(ev_q0, ctx.stream));
     launch_apply(ctx, ws, MV_Q);
     if (ev_q1) BEM_CUDA(cudaEventRecord(ev_q1, ctx.stream));
     size_t dyn = ws.w_in_smem ? (size_t)ws.bt.n * sizeof(double2) : 0;

@@ -1,0 +1,826 @@
+// Mixed-precision LU preconditioner for the batched GMRES.
+//
+// Every operator of the batch (FP32 complex, column-major) is copied and
+// factored A = L U without pivoting, in blocks of LB = 128 unknowns, all
+// systems of a (possibly ragged) batch advancing block step k together:
+//
+//   diag   one CTA per system: A11 = L11 U11 in shared memory (tiny pivots are
+//          replaced and counted), then L11^-1 and U11^-1 in place; the two
+//          inverses are kept per block (strict lower / upper of one tile).
+//   u12    U12 = L11^-1 A12 (row panel), CUDA cores.
+//   l21    L21 = A21 U11^-1 (column panel), CUDA cores; also writes L21 in
+//          the real embedding below, row-major, for the tensor cores.
+//   gemm   A22 -= L21 U12 on the tensor cores (tcgen05, kind::tf32, FP32
+//          accumulation in tensor memory).  The complex product is one real
+//          GEMM: with A' the 2m x 2k real matrix holding [[ar, -ai], [ai, ar]]
+//          per complex entry, A' times the natural real view of U12
+//          (2k x n, re/im interleaved along the rows, which is how the
+//          column-major complex storage reads as floats) gives the natural
+//          real view of the product.  Tiles of 128 real rows x 256 columns,
+//          K = 256 in chunks of 32 staged by cp.async in the no-swizzle
+//          K-major core-matrix layout; a persistent warp-specialised kernel
+//          (producer warp, MMA warp, eight epilogue warps, a four-stage operand
+//          ring and two tensor-memory accumulators) so that operand loads, MMAs
+//          and the read-modify-write of A22 overlap; every wait is bounded.
+//
+// Applying M = U^-1 L^-1 to a Krylov vector (flexible right preconditioning:
+// Z[:, k] = M Q[:, k]) is a blocked forward and back substitution with the
+// kept diagonal-block inverses, one launch per block step, FP32 factors and
+// FP64 vectors.  The factorization is TF32-accurate, which is plenty for a
+// preconditioner: the FP64 outer GMRES with exact residuals decides the
+// answer, the factors only decide the iteration count.
+#include <algorithm>
+#include <cmath>
+#include <memory>
+
+#include "common.cuh"
+#include "complex.cuh"
+#include "gmres.cuh"
+#include "kernels.cuh"
+#include "precond.cuh"
+#include "umma.cuh"
+
+namespace bem {
+
+namespace {
+
+constexpr int LB = 128;                 // block size (complex unknowns)
+constexpr int GM = 128, GN = 256;       // GEMM tile: real rows x columns
+constexpr int GK = 32;                  // real K per pipeline chunk
+constexpr int GCHUNKS = 2 * LB / GK;    // 8
+constexpr int GS = 4;                   // pipeline stages
+constexpr int GTHREADS = 320;           // producer warp, MMA warp, eight epilogue warps
+constexpr int GEPI = GTHREADS - 64;     // epilogue threads
+constexpr uint32_t GA_BYTES = GM * GK * 4, GB_BYTES = GN * GK * 4, GSTAGE = GA_BYTES + GB_BYTES;
+constexpr uint32_t G_SMEM = GS * GSTAGE + 256;  // stages + barriers + tensor-memory slot + abort flag
+constexpr uint32_t G_TMEM_COLS = 512;           // two accumulators of GN columns
+
+struct LuSys {
+    float2* F;    // factors (copy of the operator), column-major, leading dimension ld
+    float2* Dm;   // per block: L11^-1 (strict lower) and U11^-1 (upper), LB x LB column-major
+    float* W;     // real embedding of the current step's L21: 2n rows x 2 LB floats, row-major
+    int64_t n, ld;
+    int nblk, pad;
+};
+
+// One entry per (system, launch): the system and its first CTA in the
+// flattened grid of that launch.
+struct LuWork {
+    int sys, pad;
+    int64_t tile0;
+};
+
+__device__ __forceinline__ int lu_locate(const LuWork* __restrict__ wl, int nw, int64_t t, int64_t& local) {
+    int lo = 0, hi = nw - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (wl[mid].tile0 <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    local = t - wl[lo].tile0;
+    return wl[lo].sys;
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ void cfmaf_(float2& acc, float2 a, float2 b) {
+    acc.x = fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x));
+    acc.y = fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y));
+}
+
+// ---------------------------------------------------------------------------
+// Diagonal block: LU without pivoting, then both triangular inverses in place.
+__global__ void __launch_bounds__(1024) lu_diag_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
+                                                       int k, int* __restrict__ small_pivots) {
+    extern __shared__ float2 T[];  // LB x LB, column-major: T[c * LB + r]
+    __shared__ float2 part[8][LB];
+    const LuSys S = sys[wl[blockIdx.x].sys];
+    const int64_t k0 = (int64_t)k * LB;
+    const int nb = (int)min((int64_t)LB, S.n - k0);
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int c = ty; c < nb; c += 32)
+        for (int r = tx; r < nb; r += 32) T[c * LB + r] = S.F[(k0 + c) * S.ld + k0 + r];
+    __syncthreads();
+    for (int j = 0; j < nb; ++j) {
+        float2 p = T[j * LB + j];
+        float pn = p.x * p.x + p.y * p.y;
+        const bool tiny = !(pn > 1e-30f);  // also catches NaN
+        if (tiny) {
+            p = make_float2(1e-15f, 0.f);
+            pn = 1e-30f;
+        }
+        const float2 inv = make_float2(p.x / pn, -p.y / pn);
+        __syncthreads();  // every thread has read the pivot
+        if (threadIdx.x == 0 && tiny) {
+            T[j * LB + j] = p;
+            atomicAdd(small_pivots, 1);
+        }
+        for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) T[j * LB + i] = cmulf(T[j * LB + i], inv);
+        __syncthreads();
+        for (int c = j + 1 + ty; c < nb; c += 32) {
+            const float2 u = T[c * LB + j];
+            for (int i = j + 1 + tx; i < nb; i += 32) {
+                float2 a = T[c * LB + i];
+                const float2 l = T[j * LB + i];
+                a.x -= l.x * u.x - l.y * u.y;
+                a.y -= l.x * u.y + l.y * u.x;
+                T[c * LB + i] = a;
+            }
+        }
+        __syncthreads();
+    }
+    const int row = threadIdx.x & (LB - 1), sub = threadIdx.x >> 7;  // 128 rows x 8 slices
+    // L^-1 (unit lower) in place, columns right to left:
+    //   Linv[i][j] = -(L[i][j] + sum_{j<p<i} Linv[i][p] L[p][j])
+    for (int j = nb - 2; j >= 0; --j) {
+        float2 acc = make_float2(0.f, 0.f);
+        if (row < nb)
+            for (int p = j + 1 + sub; p < row; p += 8) cfmaf_(acc, T[p * LB + row], T[j * LB + p]);
+        part[sub][row] = acc;
+        __syncthreads();
+        if (sub == 0 && row > j && row < nb) {
+            float2 s = T[j * LB + row];
+            for (int q = 0; q < 8; ++q) {
+                s.x += part[q][row].x;
+                s.y += part[q][row].y;
+            }
+            T[j * LB + row] = make_float2(-s.x, -s.y);
+        }
+        __syncthreads();
+    }
+    // U^-1 in place, columns left to right:
+    //   Uinv[i][j] = (delta_ij - sum_{i<=p<j} Uinv[i][p] U[p][j]) / U[j][j]
+    for (int j = 0; j < nb; ++j) {
+        const float2 d = T[j * LB + j];
+        const float dn = d.x * d.x + d.y * d.y;
+        const float2 dinv = make_float2(d.x / dn, -d.y / dn);
+        float2 acc = make_float2(0.f, 0.f);
+        if (row < j)
+            for (int p = row + sub; p < j; p += 8) cfmaf_(acc, T[p * LB + row], T[j * LB + p]);
+        part[sub][row] = acc;
+        __syncthreads();
+        if (sub == 0 && row <= j) {
+            float2 s = make_float2(row == j ? 1.f : 0.f, 0.f);
+            for (int q = 0; q < 8; ++q) {
+                s.x -= part[q][row].x;
+                s.y -= part[q][row].y;
+            }
+            T[j * LB + row] = cmulf(s, dinv);
+        }
+        __syncthreads();
+    }
+    float2* Dk = S.Dm + (size_t)k * LB * LB;
+    for (int c = ty; c < nb; c += 32)
+        for (int r = tx; r < nb; r += 32) Dk[c * LB + r] = T[c * LB + r];
+}
+
+// U12 = L11^-1 A12 for 64 columns per CTA.
+__global__ void __launch_bounds__(256) lu_u12_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
+                                                     int nw, int k) {
+    extern __shared__ float2 sm[];
+    float2* Lf = sm;            // LB x LB column-major, unit diagonal, zero above
+    float2* X = sm + LB * LB;   // LB x 64 column-major
+    int64_t tile;
+    const LuSys S = sys[lu_locate(wl, nw, blockIdx.x, tile)];
+    const int64_t k0 = (int64_t)k * LB, j0 = k0 + LB + 64 * tile;
+    const int ncol = (int)min((int64_t)64, S.n - j0);
+    const float2* Dk = S.Dm + (size_t)k * LB * LB;
+    for (int t = threadIdx.x; t < LB * LB; t += blockDim.x) {
+        const int c = t / LB, r = t % LB;
+        Lf[t] = r > c ? Dk[t] : make_float2(r == c ? 1.f : 0.f, 0.f);
+    }
+    for (int t = threadIdx.x; t < 64 * LB; t += blockDim.x) {
+        const int c = t / LB, r = t % LB;
+        X[t] = c < ncol ? S.F[(j0 + c) * S.ld + k0 + r] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;  // rows tr + 32q, columns tc * 8 + c
+    float2 acc[4][8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[q][c] = make_float2(0.f, 0.f);
+    for (int p = 0; p < LB; ++p) {
+        float2 a[4], b[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a[q] = Lf[p * LB + tr + 32 * q];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) b[c] = X[(tc * 8 + c) * LB + p];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) cfmaf_(acc[q][c], a[q], b[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int col = tc * 8 + c;
+        if (col >= ncol) continue;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) S.F[(j0 + col) * S.ld + k0 + tr + 32 * q] = acc[q][c];
+    }
+}
+
+// L21 = A21 U11^-1 for 64 rows per CTA; natural form back into F and the
+// real embedding into W.
+__global__ void __launch_bounds__(256) lu_l21_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
+                                                     int nw, int k) {
+    extern __shared__ float2 sm[];
+    float2* Uf = sm;            // LB x LB column-major, zero below the diagonal
+    float2* Y = sm + LB * LB;   // 64 x LB: Y[p * 64 + i], reused for the output (row-major R[i * LB + c])
+    int64_t tile;
+    const LuSys S = sys[lu_locate(wl, nw, blockIdx.x, tile)];
+    const int64_t k0 = (int64_t)k * LB, kt = k0 + LB, i0 = kt + 64 * tile;
+    const int nrow = (int)min((int64_t)64, S.n - i0);
+    const float2* Dk = S.Dm + (size_t)k * LB * LB;
+    for (int t = threadIdx.x; t < LB * LB; t += blockDim.x) {
+        const int c = t / LB, r = t % LB;
+        Uf[t] = r <= c ? Dk[t] : make_float2(0.f, 0.f);
+    }
+    for (int t = threadIdx.x; t < 64 * LB; t += blockDim.x) {
+        const int p = t / 64, i = t % 64;
+        Y[t] = i < nrow ? S.F[(k0 + p) * S.ld + i0 + i] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;  // rows tr + 32q, columns tc * 16 + c
+    float2 acc[2][16];
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int c = 0; c < 16; ++c) acc[q][c] = make_float2(0.f, 0.f);
+    for (int p = 0; p < LB; ++p) {
+        const float2 a0 = Y[p * 64 + tr], a1 = Y[p * 64 + tr + 32];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            const float2 b = Uf[(tc * 16 + c) * LB + p];
+            cfmaf_(acc[0][c], a0, b);
+            cfmaf_(acc[1][c], a1, b);
+        }
+    }
+    __syncthreads();  // Y is reused below
+    float2* R = Y;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int i = tr + 32 * q;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            const int col = tc * 16 + c;
+            R[i * LB + col] = acc[q][c];
+            if (i < nrow) S.F[(k0 + col) * S.ld + i0 + i] = acc[q][c];
+        }
+    }
+    __syncthreads();
+    // real embedding: rows 2i and 2i + 1 of W (relative to the trailing block)
+    const int64_t wr0 = 2 * (i0 - kt);
+    for (int t = threadIdx.x; t < nrow * LB; t += blockDim.x) {
+        const int i = t / LB, c = t % LB;
+        const float2 v = R[i * LB + c];
+        float2* w0 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i) * (2 * LB));
+        float2* w1 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i + 1) * (2 * LB));
+        w0[c] = make_float2(v.x, -v.y);
+        w1[c] = make_float2(v.y, v.x);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Trailing update on the tensor cores.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Bulk prefetch into L2 (16-byte aligned address, size a multiple of 16).
+__device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Instruction descriptor, kind::tf32: TF32 A and B (both K-major), FP32 D.
+__host__ __device__ constexpr uint32_t umma_idesc_tf32_f32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Persistent, warp-specialised trailing update.  Warp 0 stages operand chunks
+// with cp.async into a ring of GS stages (GS - 1 chunks in flight; a stage is
+// published on its "full" barrier after the warp's own copies completed and
+// were fenced for the async proxy), lane 0 of warp 1 issues the MMAs of a
+// stage and releases it through tcgen05.commit on its "empty" barrier, and
+// warps 2-9 drain the accumulator of the previous tile (two accumulators of
+// 256 tensor-memory columns) while the next tile's MMAs run.
+struct GemmTile {
+    const float* W;
+    float* F;
+    int64_t n, rows, ld2, k0, kt, row0, col0;
+};
+
+__device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl, int nw,
+                                              int k, int64_t t) {
+    int64_t local;
+    const LuSys S = sys[lu_locate(wl, nw, t, local)];
+    GemmTile g;
+    g.W = S.W;
+    g.F = reinterpret_cast<float*>(S.F);
+    g.n = S.n;
+    g.k0 = (int64_t)k * LB;
+    g.kt = g.k0 + LB;
+    g.rows = 2 * (S.n - g.kt);
+    g.ld2 = 2 * S.ld;
+    const int64_t tiles_i = (g.rows + GM - 1) / GM;
+    g.row0 = (local % tiles_i) * GM;
+    g.col0 = g.kt + (local / tiles_i) * GN;
+    return g;
+}
+
+__global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __restrict__ sys,
+                                                              const LuWork* __restrict__ wl, int nw, int k,
+                                                              int64_t ntiles, int* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + GS * GSTAGE);
+    uint64_t* empty = full + GS;
+    uint64_t* tfull = empty + GS;
+    uint64_t* tempty = tfull + 2;
+    uint64_t* drain = tempty + 2;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) tmem_alloc(tmem_slot, G_TMEM_COLS);
+    if (tid == 0) {
+        for (int s = 0; s < GS; ++s) {
+            mbar_init(&full[s], 32);
+            mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(&tfull[a], 1);
+            mbar_init(&tempty[a], GEPI);
+        }
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t base = smem_u32(smem);
+    auto fail = [&]() {
+        *abort_flag = 1;
+        atomicOr(err, DEVERR_MBAR_TIMEOUT);
+    };
+
+    if (warp == 0) {
+        // ---- producer
+        const int rl = lane & 7, q0 = lane >> 3;  // this lane's row-in-core and first K quad
+        int64_t it = 0;
+        for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+            const GemmTile g = gemm_tile(sys, wl, nw, k, t);
+            for (int c = 0; c < GCHUNKS; ++c, ++it) {
+                const int st = (int)(it % GS);
+                const int64_t round = it / GS;
+                if (round > 0 && !mbar_wait_bounded(&empty[st], (uint32_t)((round - 1) & 1))) {
+                    fail();
+                    break;
+                }
+                const uint32_t As = base + st * GSTAGE, Bs = As + GA_BYTES;
+                // A: pieces (mg, q, rl) with q = q0 + 4 (i & 1), mg = i >> 1
+#pragma unroll
+                for (int i = 0; i < GM / 4; ++i) {
+                    const int mg = i >> 1, q = q0 + 4 * (i & 1);
+                    const int64_t r = g.row0 + mg * 8 + rl;
+                    const bool ok = r < g.rows;
+                    const float* src = g.W + (ok ? r : 0) * (2 * LB) + c * GK + q * 4;
+                    cp_async16(As + (uint32_t)((mg * 8 + q) * 128 + rl * 16), src, ok ? 16u : 0u);
+                }
+                // B: pieces (ng, q, rl), column j = col0 + 8 ng + rl
+#pragma unroll 8
+                for (int i = 0; i < GN / 4; ++i) {
+                    const int ng = i >> 1, q = q0 + 4 * (i & 1);
+                    const int64_t j = g.col0 + ng * 8 + rl;
+                    const bool ok = j < g.n;
+                    const float* src = g.F + (ok ? j : g.kt) * g.ld2 + 2 * g.k0 + c * GK + q * 4;
+                    cp_async16(Bs + (uint32_t)((ng * 8 + q) * 128 + rl * 16), src, ok ? 16u : 0u);
+                }
+                cp_async_commit();
+                if (it >= GS - 1) {
+                    // the chunk GS - 1 behind is complete: publish it
+                    cp_async_wait<GS - 1>();
+                    fence_proxy_async_shared();
+                    mbar_arrive(&full[(it - (GS - 1)) % GS]);
+                }
+            }
+        }
+        cp_async_wait<0>();
+        fence_proxy_async_shared();
+        for (int64_t j = (it >= GS - 1 ? it - (GS - 1) : 0); j < it; ++j) mbar_arrive(&full[j % GS]);
+    } else if (warp == 1) {
+        // ---- MMA issuer
+        const uint32_t idesc = umma_idesc_tf32_f32(GM, GN);
+        int64_t it = 0, tc = 0;
+        for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, ++tc) {
+            const int acc = (int)(tc & 1);
+            const int64_t use = tc >> 1;
+            if (lane > 0) {
+                // lanes 1-31: bring this tile's block of A22 into L2 for the epilogue
+                const GemmTile g = gemm_tile(sys, wl, nw, k, t);
+                const int64_t nrow = min((int64_t)GM, g.rows - g.row0);
+                const uint32_t bytes = (uint32_t)(nrow * 4) & ~15u;
+                for (int q = lane - 1; q < GN && bytes; q += 31) {
+                    const int64_t j = g.col0 + q;
+                    if (j >= g.n) break;
+                    l2_prefetch(g.F + j * g.ld2 + 2 * g.kt + g.row0, bytes);
+                }
+            }
+            if (lane == 0 && use > 0 && !mbar_wait_bounded(&tempty[acc], (uint32_t)((use - 1) & 1))) fail();
+            __syncwarp();
+            if (*abort_flag) break;
+            tc_fence_after();
+            for (int c = 0; c < GCHUNKS; ++c, ++it) {
+                const int st = (int)(it % GS);
+                if (lane == 0) {
+                    if (!mbar_wait_bounded(&full[st], (uint32_t)((it / GS) & 1))) fail();
+                    else {
+                        tc_fence_after();
+                        const uint32_t a = base + st * GSTAGE, b = a + GA_BYTES;
+#pragma unroll
+                        for (int kk = 0; kk < GK / 8; ++kk)
+                            umma_tf32(tmem + (uint32_t)(acc * GN), umma_smem_desc(a + kk * 256, 128, 1024),
+                                      umma_smem_desc(b + kk * 256, 128, 1024), idesc, (c | kk) ? 1u : 0u);
+                        umma_commit(&empty[st]);
+                    }
+                }
+                __syncwarp();
+                if (*abort_flag) break;
+            }
+            if (*abort_flag) break;
+            if (lane == 0) umma_commit(&tfull[acc]);
+            __syncwarp();
+        }
+    } else {
+        // ---- epilogue: A22 -= accumulator; two warps per lane quarter, each
+        // with half of the columns
+        const int quarter = warp & 3;  // tensor-memory lanes this warp may read
+        const int half = (warp - 2) >> 2;
+        const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;
+        int64_t tc = 0;
+        for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, ++tc) {
+            const int acc = (int)(tc & 1);
+            if (!mbar_wait_bounded(&tfull[acc], (uint32_t)((tc >> 1) & 1))) {
+                fail();
+                break;
+            }
+            tc_fence_after();
+            const GemmTile g = gemm_tile(sys, wl, nw, k, t);
+            const int64_t r = g.row0 + 32 * quarter + lane;
+            const bool rok = r < g.rows;
+            for (int cc = half * (GN / 64); cc < (half + 1) * (GN / 64); ++cc) {
+                const int64_t jb = g.col0 + cc * 32;
+                if (jb >= g.n) break;  // uniform over the warp
+                float v[32];
+                tmem_ld32(tmem + lane_base + (uint32_t)(acc * GN + cc * 32), v);
+                if (!rok) continue;
+                // all 32 loads in flight before the first store
+                const int nq = (int)min((int64_t)32, g.n - jb);
+                float* p0 = g.F + jb * g.ld2 + 2 * g.kt + r;
+                float cv[32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q) cv[q] = q < nq ? __ldcg(p0 + q * g.ld2) : 0.f;
+#pragma unroll
+                for (int q = 0; q < 32; ++q)
+                    if (q < nq) p0[q * g.ld2] = cv[q] - v[q];
+            }
+            tc_fence_before();
+            mbar_arrive(&tempty[acc]);
+        }
+    }
+    __syncthreads();
+    if (*abort_flag) {
+        // every MMA this CTA issued is tracked by one more commit
+        if (tid == 32) umma_commit(drain);
+        if (tid == 32) mbar_wait_bounded(drain, 0);
+        __syncthreads();
+    }
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, G_TMEM_COLS);
+}
+
+// ---------------------------------------------------------------------------
+// Preconditioner application.  Forward: z = q, then for every block step
+// z_b -= L_bk z_k below block k, the block k + 1 finishing with
+// z_{k+1} = L^-1_{k+1} z_{k+1}.  Backward likewise with the U blocks above.
+__device__ __forceinline__ void cfma_fd(double2& acc, float2 a, double2 x) {
+    acc.x = fma((double)a.x, x.x, fma(-(double)a.y, x.y, acc.x));
+    acc.y = fma((double)a.x, x.y, fma((double)a.y, x.x, acc.y));
+}
+
+// z[0..nr) <- T z with T the lower (unit) or upper part of a kept inverse tile.
+__device__ void lu_apply_inverse(const float2* __restrict__ Dk, int nr, bool lower, double2* __restrict__ z,
+                                 double2* xs, double2 (*red)[LB]) {
+    const int row = threadIdx.x & (LB - 1), half = threadIdx.x >> 7;
+    if (half == 0) xs[row] = row < nr ? z[row] : make_double2(0, 0);
+    __syncthreads();
+    double2 acc = make_double2(0, 0);
+    if (row < nr) {
+        const int p0 = half * (LB / 2), p1 = p0 + LB / 2;
+        for (int p = p0; p < p1; ++p) {
+            const bool use = lower ? (p < row) : (p >= row);
+            if (use && p < nr) cfma_fd(acc, Dk[p * LB + row], xs[p]);
+        }
+    }
+    red[half][row] = acc;
+    __syncthreads();
+    if (half == 0 && row < nr) {
+        double2 v = make_double2(red[0][row].x + red[1][row].x, red[0][row].y + red[1][row].y);
+        if (lower) v = make_double2(v.x + xs[row].x, v.y + xs[row].y);  // unit diagonal
+        z[row] = v;
+    }
+    __syncthreads();
+}
+
+// z[r0 .. r0+nr) -= B x, B the nr x nc block of F at (r0, c0).
+__device__ void lu_block_update(const LuSys& S, int64_t r0, int nr, int64_t c0, int nc, const double2* __restrict__ x,
+                                double2* __restrict__ z, double2* xs, double2 (*red)[LB]) {
+    const int row = threadIdx.x & (LB - 1), half = threadIdx.x >> 7;
+    if (half == 0) xs[row] = row < nc ? x[row] : make_double2(0, 0);
+    __syncthreads();
+    double2 acc = make_double2(0, 0);
+    if (row < nr) {
+        const int p0 = half * (LB / 2), p1 = min(p0 + LB / 2, nc);
+        for (int p = p0; p < p1; ++p) cfma_fd(acc, S.F[(c0 + p) * S.ld + r0 + row], xs[p]);
+    }
+    red[half][row] = acc;
+    __syncthreads();
+    if (half == 0 && row < nr) {
+        double2 v = z[r0 + row];
+        v.x -= red[0][row].x + red[1][row].x;
+        v.y -= red[0][row].y + red[1][row].y;
+        z[r0 + row] = v;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) lu_fwd_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
+                                                     int nw, int k, GmBatch bt) {
+    __shared__ double2 xs[LB];
+    __shared__ double2 red[2][LB];
+    int64_t local;
+    const int s = lu_locate(wl, nw, blockIdx.x, local);
+    const GmState& st = bt.st[s];
+    if (!gm_apply_active(bt, st, MV_Q)) return;
+    const LuSys S = sys[s];
+    const GmView g = gm_view(bt, s);
+    const double2* q = bt.Q + g.q + (size_t)st.k * g.n;
+    double2* z = bt.Z + g.q + (size_t)st.k * g.n;
+    if (k < 0) {
+        // z = q for block b; block 0 then z_0 = L^-1_0 z_0
+        const int64_t b = local, r0 = b * LB;
+        const int nr = (int)min((int64_t)LB, S.n - r0);
+        for (int r = threadIdx.x; r < nr; r += blockDim.x) z[r0 + r] = q[r0 + r];
+        __syncthreads();
+        if (b == 0) lu_apply_inverse(S.Dm, nr, true, z, xs, red);
+        return;
+    }
+    const int64_t b = k + 1 + local, r0 = b * LB;
+    const int nr = (int)min((int64_t)LB, S.n - r0);
+    lu_block_update(S, r0, nr, (int64_t)k * LB, LB, z + (int64_t)k * LB, z, xs, red);
+    if (b == k + 1) lu_apply_inverse(S.Dm + (size_t)b * LB * LB, nr, true, z + r0, xs, red);
+}
+
+__global__ void __launch_bounds__(256) lu_bwd_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
+                                                     int nw, int t, GmBatch bt) {
+    __shared__ double2 xs[LB];
+    __shared__ double2 red[2][LB];
+    int64_t local;
+    const int s = lu_locate(wl, nw, blockIdx.x, local);
+    const GmState& st = bt.st[s];
+    if (!gm_apply_active(bt, st, MV_Q)) return;
+    const LuSys S = sys[s];
+    const GmView g = gm_view(bt, s);
+    double2* z = bt.Z + g.q + (size_t)st.k * g.n;
+    if (t == 0) {
+        const int64_t b = S.nblk - 1, r0 = b * LB;
+        lu_apply_inverse(S.Dm + (size_t)b * LB * LB, (int)(S.n - r0), false, z + r0, xs, red);
+        return;
+    }
+    const int64_t kk = S.nblk - t;  // block solved by the previous launch
+    const int64_t b = local, r0 = b * LB, c0 = kk * LB;
+    const int nc = (int)min((int64_t)LB, S.n - c0);
+    lu_block_update(S, r0, LB, c0, nc, z + c0, z, xs, red);
+    if (b == kk - 1) lu_apply_inverse(S.Dm + (size_t)b * LB * LB, LB, false, z + r0, xs, red);
+}
+
+// ---------------------------------------------------------------------------
+struct LuData {
+    DevBuf F, Dm, W, sysbuf, work, info;
+    std::vector<LuSys> sys;
+    int nblk_max = 0;
+    // work lists: per launch, [offset, count, ctas] into `work`
+    struct Seg {
+        int64_t off = 0;
+        int count = 0;
+        int64_t ctas = 0;
+    };
+    std::vector<Seg> diag, u12, l21, gemm, fwd, bwd;
+    std::vector<LuWork> host;
+    int small_pivots = 0;
+};
+
+LuData::Seg add_segment(LuData& d, const std::vector<std::pair<int, int64_t>>& entries) {
+    LuData::Seg sg;
+    sg.off = (int64_t)d.host.size();
+    int64_t t = 0;
+    for (auto& e : entries) {
+        if (e.second <= 0) continue;
+        d.host.push_back(LuWork{e.first, 0, t});
+        t += e.second;
+    }
+    sg.count = (int)((int64_t)d.host.size() - sg.off);
+    sg.ctas = t;
+    return sg;
+}
+
+void lu_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
+    (void)mode;
+    LuData& d = *static_cast<LuData*>(user);
+    const LuSys* sys = d.sysbuf.as<LuSys>();
+    const LuWork* wk = d.work.as<LuWork>();
+    for (int i = 0; i < (int)d.fwd.size(); ++i) {
+        const auto& sg = d.fwd[(size_t)i];
+        if (!sg.ctas) continue;
+        lu_fwd_kernel<<<(unsigned)sg.ctas, 256, 0, c.stream>>>(sys, wk + sg.off, sg.count, i - 1, ws.bt);
+        BEM_CHECK_LAUNCH(&c);
+    }
+    for (int i = 0; i < (int)d.bwd.size(); ++i) {
+        const auto& sg = d.bwd[(size_t)i];
+        if (!sg.ctas) continue;
+        lu_bwd_kernel<<<(unsigned)sg.ctas, 256, 0, c.stream>>>(sys, wk + sg.off, sg.count, i, ws.bt);
+        BEM_CHECK_LAUNCH(&c);
+    }
+}
+
+}  // namespace
+
+// Factors every operator of the batch and installs the preconditioner hook.
+void lu_precond_setup(Context& c, GmWorkspace& ws) {
+    require(ws.fp32, "LU preconditioner: FP32 operators only");
+    auto d = std::make_shared<LuData>();
+    const int nsys = ws.bt.nsys;
+    std::vector<GmView> v((size_t)nsys);
+    size_t entries = 0, dm = 0, wsz = 0;
+    for (int s = 0; s < nsys; ++s) {
+        v[(size_t)s] = ws.sys_host.empty() ? gm_view(ws.bt, s) : GmView{};
+        if (!ws.sys_host.empty()) {
+            const GmSys& q = ws.sys_host[(size_t)s];
+            v[(size_t)s].n = q.n;
+            v[(size_t)s].lda = q.lda;
+            v[(size_t)s].a = q.a_off;
+        }
+        entries = std::max(entries, v[(size_t)s].a + (size_t)v[(size_t)s].lda * v[(size_t)s].n);
+        const int nb = (int)((v[(size_t)s].n + LB - 1) / LB);
+        dm += (size_t)nb * LB * LB;
+        wsz += (size_t)2 * v[(size_t)s].n * 2 * LB;
+        d->nblk_max = std::max(d->nblk_max, nb);
+    }
+    d->F.ensure(sizeof(float2) * entries);
+    d->Dm.ensure(sizeof(float2) * std::max<size_t>(dm, 1));
+    d->W.ensure(sizeof(float) * std::max<size_t>(wsz, 4));
+    BEM_CUDA(cudaMemcpyAsync(d->F.p, ws.bt.A, sizeof(float2) * entries, cudaMemcpyDeviceToDevice, c.stream));
+    d->sys.resize((size_t)nsys);
+    size_t od = 0, ow = 0;
+    for (int s = 0; s < nsys; ++s) {
+        LuSys& L = d->sys[(size_t)s];
+        L.F = d->F.as<float2>() + v[(size_t)s].a;
+        L.Dm = d->Dm.as<float2>() + od;
+        L.W = d->W.as<float>() + ow;
+        L.n = v[(size_t)s].n;
+        L.ld = v[(size_t)s].lda;
+        L.nblk = (int)((L.n + LB - 1) / LB);
+        od += (size_t)L.nblk * LB * LB;
+        ow += (size_t)2 * L.n * 2 * LB;
+    }
+    // work lists of every launch
+    for (int k = 0; k < d->nblk_max; ++k) {
+        std::vector<std::pair<int, int64_t>> ed, eu, el, eg;
+        for (int s = 0; s < nsys; ++s) {
+            const LuSys& L = d->sys[(size_t)s];
+            if (L.nblk <= k) continue;
+            ed.push_back({s, 1});
+            const int64_t mt = L.n - (int64_t)(k + 1) * LB;
+            if (mt > 0) {
+                eu.push_back({s, (mt + 63) / 64});
+                el.push_back({s, (mt + 63) / 64});
+                eg.push_back({s, ((2 * mt + GM - 1) / GM) * ((mt + GN - 1) / GN)});
+            }
+        }
+        d->diag.push_back(add_segment(*d, ed));
+        d->u12.push_back(add_segment(*d, eu));
+        d->l21.push_back(add_segment(*d, el));
+        d->gemm.push_back(add_segment(*d, eg));
+    }
+    for (int k = -1; k < d->nblk_max - 1; ++k) {
+        std::vector<std::pair<int, int64_t>> e;
+        for (int s = 0; s < nsys; ++s) {
+            const LuSys& L = d->sys[(size_t)s];
+            e.push_back({s, k < 0 ? (int64_t)L.nblk : (int64_t)std::max(0, L.nblk - k - 1)});
+        }
+        d->fwd.push_back(add_segment(*d, e));
+    }
+    for (int t = 0; t < d->nblk_max; ++t) {
+        std::vector<std::pair<int, int64_t>> e;
+        for (int s = 0; s < nsys; ++s) {
+            const LuSys& L = d->sys[(size_t)s];
+            e.push_back({s, t == 0 ? 1 : (int64_t)std::max(0, L.nblk - t)});
+        }
+        d->bwd.push_back(add_segment(*d, e));
+    }
+    d->sysbuf.ensure(sizeof(LuSys) * nsys);
+    d->work.ensure(sizeof(LuWork) * std::max<size_t>(d->host.size(), 1));
+    d->info.ensure(sizeof(int));
+    BEM_CUDA(cudaMemcpyAsync(d->sysbuf.p, d->sys.data(), sizeof(LuSys) * nsys, cudaMemcpyHostToDevice, c.stream));
+    BEM_CUDA(cudaMemcpyAsync(d->work.p, d->host.data(), sizeof(LuWork) * d->host.size(), cudaMemcpyHostToDevice,
+                             c.stream));
+    BEM_CUDA(cudaMemsetAsync(d->info.p, 0, sizeof(int), c.stream));
+    int* err = device_err(c);
+    BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c.stream));
+    const size_t diag_smem = sizeof(float2) * LB * LB, panel_smem = sizeof(float2) * (LB * LB + 64 * LB);
+    BEM_CUDA(cudaFuncSetAttribute(lu_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_smem));
+    BEM_CUDA(cudaFuncSetAttribute(lu_u12_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
+    BEM_CUDA(cudaFuncSetAttribute(lu_l21_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
+    BEM_CUDA(cudaFuncSetAttribute(lu_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    const LuSys* sys = d->sysbuf.as<LuSys>();
+    const LuWork* wk = d->work.as<LuWork>();
+    int nsm = 0;
+    BEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
+    // with profiling: CUDA events around every launch, summed per kernel
+    cudaEvent_t ev[5] = {};
+    float tsum[4] = {0, 0, 0, 0};
+    double flops[4] = {0, 0, 0, 0};
+    if (c.profiling)
+        for (auto& e : ev) BEM_CUDA(cudaEventCreate(&e));
+    for (int k = 0; k < d->nblk_max; ++k) {
+        const auto &sd = d->diag[(size_t)k], &su = d->u12[(size_t)k], &sl = d->l21[(size_t)k],
+                   &sg = d->gemm[(size_t)k];
+        if (c.profiling) BEM_CUDA(cudaEventRecord(ev[0], c.stream));
+        if (sd.ctas) {
+            lu_diag_kernel<<<(unsigned)sd.ctas, 1024, diag_smem, c.stream>>>(sys, wk + sd.off, k,
+                                                                             d->info.as<int>());
+            BEM_CHECK_LAUNCH(&c);
+        }
+        if (c.profiling) BEM_CUDA(cudaEventRecord(ev[1], c.stream));
+        if (su.ctas) {
+            lu_u12_kernel<<<(unsigned)su.ctas, 256, panel_smem, c.stream>>>(sys, wk + su.off, su.count, k);
+            BEM_CHECK_LAUNCH(&c);
+        }
+        if (c.profiling) BEM_CUDA(cudaEventRecord(ev[2], c.stream));
+        if (sl.ctas) {
+            lu_l21_kernel<<<(unsigned)sl.ctas, 256, panel_smem, c.stream>>>(sys, wk + sl.off, sl.count, k);
+            BEM_CHECK_LAUNCH(&c);
+        }
+        if (c.profiling) BEM_CUDA(cudaEventRecord(ev[3], c.stream));
+        if (sg.ctas) {
+            const unsigned grid = (unsigned)std::min<int64_t>(sg.ctas, nsm);
+            lu_gemm_kernel<<<grid, GTHREADS, G_SMEM, c.stream>>>(sys, wk + sg.off, sg.count, k, sg.ctas, err);
+            BEM_CHECK_LAUNCH(&c);
+        }
+        if (c.profiling) {
+            BEM_CUDA(cudaEventRecord(ev[4], c.stream));
+            BEM_CUDA(cudaEventSynchronize(ev[4]));
+            for (int q = 0; q < 4; ++q) {
+                float ms = 0;
+                BEM_CUDA(cudaEventElapsedTime(&ms, ev[q], ev[q + 1]));
+                tsum[q] += ms;
+            }
+            for (int s = 0; s < nsys; ++s) {
+                const double mt = (double)(d->sys[(size_t)s].n - (int64_t)(k + 1) * LB);
+                if (mt <= 0) continue;
+                flops[1] += 8.0 * LB * LB * mt;
+                flops[2] += 8.0 * LB * LB * mt;
+                flops[3] += 8.0 * LB * mt * mt;
+            }
+        }
+    }
+    if (c.profiling) {
+        const char* names[4] = {"lu_diag", "lu_u12", "lu_l21", "lu_gemm_tf32"};
+        for (int q = 0; q < 4; ++q) c.stage_add(names[q], tsum[q], d->nblk_max, flops[q]);
+        for (auto& e : ev) cudaEventDestroy(e);
+    }
+    check_device_err(c);
+    BEM_CUDA(cudaMemcpyAsync(&d->small_pivots, d->info.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    ws.zmem.ensure(sizeof(double2) * gm_q_total(ws));
+    ws.bt.Z = ws.zmem.as<double2>();
+    ws.precond = lu_hook;
+    ws.precond_user = d.get();
+    ws.precond_keep = d;
+}
+
+}  // namespace bem

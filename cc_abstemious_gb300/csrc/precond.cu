@@ -683,6 +683,11 @@ static void pc_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
 }
 
 bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks) {
+    if (kind == BEM_PRECOND_LU) {
+        if (!ws.fp32) return BEM_PRECOND_NONE;  // first-kind operators stay FP64
+        lu_precond_setup(c, ws);
+        return kind;
+    }
     require(kind == BEM_PRECOND_BLOCK_JACOBI || kind == BEM_PRECOND_LEARNED, "unknown preconditioner");
     // without a trained or loaded network the learned form falls back to block-Jacobi
     if (kind == BEM_PRECOND_LEARNED && !(c.net && c.net->ready)) kind = BEM_PRECOND_BLOCK_JACOBI;
@@ -715,6 +720,10 @@ bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond k
 // system's blocks are stored back to back.
 bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies, const std::vector<int>& sys_body,
                                 GmWorkspace& ws, bem_precond kind, const double* ks) {
+    if (kind == BEM_PRECOND_LU) {
+        lu_precond_setup(c, ws);
+        return kind;
+    }
     require(kind == BEM_PRECOND_BLOCK_JACOBI || kind == BEM_PRECOND_LEARNED, "unknown preconditioner");
     require(!ws.sys_host.empty() && (int)sys_body.size() == ws.bt.nsys, "multi-body preconditioner: bad batch");
     if (kind == BEM_PRECOND_LEARNED && !(c.net && c.net->ready)) kind = BEM_PRECOND_BLOCK_JACOBI;

@@ -39,6 +39,8 @@ void build_pattern(const Problem& p, NearPattern& P, bool diag_only = false);
 // Installs the preconditioner on the batch; returns the kind actually used
 // (the learned form falls back to block-Jacobi when no network is available).
 bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks);
+// TF32 tensor-core LU of every FP32 operator of the batch (lu32.cu).
+void lu_precond_setup(Context& c, GmWorkspace& ws);
 // Several bodies in a ragged batch: system s belongs to bodies[sys_body[s]].
 bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies, const std::vector<int>& sys_body,
                                 GmWorkspace& ws, bem_precond kind, const double* ks);

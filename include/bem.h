@@ -59,10 +59,22 @@ typedef enum { BEM_SIDE_RHS = 0, BEM_SIDE_LHS = 1 } bem_side;
  *              reports its error against an FP64 LU when requested. */
 typedef enum { BEM_FORM_PLAIN_FP64 = 0, BEM_FORM_MIXED = 1 } bem_form;
 
+/* Preconditioners of the mixed form (no counterpart in the reference, whose
+ * GMRES is unpreconditioned, gmres.rs:80-140).  Flexible right
+ * preconditioning; the FP64 residual decides convergence, so a preconditioner
+ * changes the iteration count, never the answer.
+ *  BLOCK_JACOBI: inverses of the diagonal cluster-leaf blocks.
+ *  LEARNED:      block-Jacobi plus a network-predicted near-field correction
+ *                (falls back to BLOCK_JACOBI without a trained network).
+ *  LU:           a TF32 tensor-core LU (no pivoting) of each FP32 operator,
+ *                applied by blocked triangular solves; for hard systems (high
+ *                frequency, fine meshes) where GMRES alone stalls.  FP32
+ *                operators only (none for first-kind operators). */
 typedef enum {
     BEM_PRECOND_NONE = 0,
     BEM_PRECOND_BLOCK_JACOBI = 1,
-    BEM_PRECOND_LEARNED = 2
+    BEM_PRECOND_LEARNED = 2,
+    BEM_PRECOND_LU = 3
 } bem_precond;
 
 typedef struct {

@@ -1,0 +1,90 @@
+"""LU preconditioner of the mixed form: FP32 operators factored without
+pivoting (TF32 tensor-core trailing updates), applied by blocked triangular
+solves inside the FP64 GMRES.  The answer is decided by the FP64 residual, so
+the checks are: every solve within 1e-6 of an FP64 LU, and far fewer
+iterations than without a preconditioner."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+bem = pytest.importorskip("cc_abstemious_gb300")
+from cc_abstemious_gb300 import meshgen, workloads  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return bem.Context.default()
+
+
+@pytest.fixture(scope="module")
+def wd():
+    return tempfile.mkdtemp(prefix="bem_lu_")
+
+
+def _run(ctx, inp, precond):
+    a = bem.Analysis(ctx)
+    a.set_input(inp)
+    a.run(form="mixed", precond=precond, check_vs_lu=True)
+    return a.reports
+
+
+def _icosphere_input(wd, sub, ka, method="BurtonMiller"):
+    nodes, tris = meshgen.icosphere(sub)
+    path = os.path.join(wd, "ico%d.vtk" % sub)
+    meshgen.write_vtk(path, nodes, tris, 5)
+    return workloads.base_input(path, [ka * 343.0 / (2 * np.pi)], method=method,
+                                solver={"Iterative": {"tolerance": 1e-9, "max_iterations": 1000}})
+
+
+@pytest.mark.parametrize("sub,method", [(1, "BurtonMiller"), (2, "BurtonMiller"), (3, "Classical")])
+def test_lu_small_and_block_multiples(ctx, wd, sub, method):
+    """80 unknowns (one partial block, no trailing update), 320, and 1280 (a
+    multiple of the block size)."""
+    inp = _icosphere_input(wd, sub, 2.0, method)
+    r0 = _run(ctx, inp, None)
+    r1 = _run(ctx, inp, "lu")
+    for a, b in zip(r0, r1):
+        assert b["flag"] == 1 and b["precond"] == bem.PRECOND_LU
+        assert 0 <= b["rel_err_vs_lu"] < 1e-6, b
+        assert b["iterations"] <= max(4, a["iterations"] // 2), (a["iterations"], b["iterations"])
+
+
+def test_lu_hard_impedance(ctx, wd):
+    """Impedance condition at high ka, where unpreconditioned GMRES(32) needs
+    hundreds of iterations."""
+    inp = workloads.perturbed_sphere_input(wd, 5, 1500, [3.0, 8.0, 12.0], tol=1e-8)
+    r0 = _run(ctx, inp, None)
+    r1 = _run(ctx, inp, "lu")
+    for a, b in zip(r0, r1):
+        assert b["flag"] == 1 and b["precond"] == bem.PRECOND_LU
+        assert 0 <= b["rel_err_vs_lu"] < 1e-6, b
+        assert b["iterations"] < a["iterations"]
+    print("iterations none / lu:", [r["iterations"] for r in r0], [r["iterations"] for r in r1])
+    assert max(r["iterations"] for r in r1) <= 30
+
+
+def test_lu_ragged_batch(ctx, wd):
+    inps = [workloads.perturbed_sphere_input(wd, 70 + i, t, [2.0, 6.0], tol=1e-8)
+            for i, t in enumerate((300, 1100, 640))]
+    pds = [bem.PreData.from_dict(d, ctx=ctx) for d in inps]
+    out = bem.run_batch(pds, precond="lu", check_vs_lu=True, ctx=ctx)
+    for inp, (res, reps) in zip(inps, out):
+        single = _run(ctx, inp, "lu")
+        for r, s in zip(reps, single):
+            assert r["flag"] == 1 and r["precond"] == bem.PRECOND_LU
+            assert 0 <= r["rel_err_vs_lu"] < 1e-6
+            assert abs(r["iterations"] - s["iterations"]) <= 1
+
+
+def test_lu_first_kind_falls_back(ctx, wd):
+    """A first-kind operator keeps an FP64 operator: no LU preconditioner."""
+    inp = workloads.perturbed_sphere_input(wd, 9, 400, [1.5], tol=1e-8)
+    inp["method_type"] = "Classical"
+    inp["surface_bc"] = {"bc_type": "Pressure", "value": [0.0, 0.0]}
+    r = _run(ctx, inp, "lu")[0]
+    assert r["flag"] == 1 and r["precond"] == bem.PRECOND_NONE
+    assert 0 <= r["rel_err_vs_lu"] < 1e-6
