@@ -99,6 +99,8 @@ void solve_chunk(Context& c, std::vector<BodyPlan*>& bodies, bem_precond precond
     c.w_mat.ensure(sizeof(float2) * ent);
     float2* A = c.w_mat.as<float2>();
     GmWorkspace ws;
+    ws.mem_pool = &c.w_gm;
+    ws.z_pool = &c.w_gmz;
     gm_prepare_ragged(c, ws, ns, lds, aoff, mmax, A, true);
     const std::vector<GmSys>& L = ws.sys_host;
     const size_t vtot = L.back().v_off + (size_t)L.back().n;

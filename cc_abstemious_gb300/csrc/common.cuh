@@ -164,6 +164,10 @@ struct Context {
     int64_t launches = 0;
     // workspaces (grow-only)
     DevBuf w_mat, w_mat2, w_vec, w_small, w_flags, w_part, w_norm;
+    // batched GMRES workspace and Krylov-preconditioned basis, LU factors,
+    // diagonal-block inverses and panel workspace (grow-only, reused by
+    // every mixed solve)
+    DevBuf w_gm, w_gmz, w_lu_F, w_lu_D, w_lu_W;
     // results of the last bem_run
     std::vector<double> last_phi, last_vn;
     int64_t last_n = 0, last_nf = 0;

@@ -529,8 +529,8 @@ void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const
     size_t oP = carve(sizeof(double2) * nsys * cb * bt.n_pad), oT = carve(sizeof(int) * nsys * rb);
     size_t oS = carve(sizeof(double2) * nsys * small), oSt = carve(sizeof(GmState) * nsys);
     size_t oN = carve(sizeof(double) * nsys * 1024 + sizeof(double) * nsys);
-    ws.mem.ensure(bytes);
-    char* base = ws.mem.as<char>();
+    ws.memb().ensure(bytes);
+    char* base = ws.memb().as<char>();
     bt.X = reinterpret_cast<double2*>(base + oX);
     bt.B = reinterpret_cast<double2*>(base + oB);
     bt.Q = reinterpret_cast<double2*>(base + oQ);
@@ -666,8 +666,8 @@ void gm_prepare_ragged(Context& ctx, GmWorkspace& ws, const std::vector<int64_t>
     size_t oS = carve(sizeof(double2) * nsys * small), oSt = carve(sizeof(GmState) * nsys);
     size_t oN = carve(sizeof(double) * nsys * 1024 + sizeof(double) * nsys);
     size_t oD = carve(sizeof(GmSys) * nsys);
-    ws.mem.ensure(bytes);
-    char* base = ws.mem.as<char>();
+    ws.memb().ensure(bytes);
+    char* base = ws.memb().as<char>();
     bt.X = reinterpret_cast<double2*>(base + oX);
     bt.B = reinterpret_cast<double2*>(base + oB);
     bt.Q = reinterpret_cast<double2*>(base + oQ);
@@ -776,7 +776,11 @@ void gm_launch_iteration(Context& ctx, GmWorkspace& ws, cudaEvent_t ev_q0, cudaE
     launch_apply(ctx, ws, MV_START);
     gm_start_kernel<<<nsys, AR_THREADS, 0, ctx.stream>>>(ws.bt);
     BEM_CHECK_LAUNCH(&ctx);
-    if (ws.precond) ws.precond(ctx, ws, MV_Q, ws.precond_user);
+    if (ws.precond) {
+        if (ws.ev_p0) BEM_CUDA(cudaEventRecord(ws.ev_p0, ctx.stream));
+        ws.precond(ctx, ws, MV_Q, ws.precond_user);
+        if (ws.ev_p1) BEM_CUDA(cudaEventRecord(ws.ev_p1, ctx.stream));
+    }
     if (ev_q0) BEM_CUDA(cudaEventRecord(ev_q0, ctx.stream));
     launch_apply(ctx, ws, MV_Q);
     if (ev_q1) BEM_CUDA(cudaEventRecord(ev_q1, ctx.stream));
@@ -807,6 +811,10 @@ void gm_run(Context& ctx, GmWorkspace& ws, int chunk, int64_t max_total_iteratio
         if (ctx.profiling) {
             BEM_CUDA(cudaEventCreate(&e0));
             BEM_CUDA(cudaEventCreate(&e1));
+            if (ws.precond) {
+                BEM_CUDA(cudaEventCreate(&ws.ev_p0));
+                BEM_CUDA(cudaEventCreate(&ws.ev_p1));
+            }
         }
         gm_read_states(ctx, ws, prev);
         for (;;) {
@@ -824,6 +832,11 @@ void gm_run(Context& ctx, GmWorkspace& ws, int chunk, int64_t max_total_iteratio
                 if (entries > 0)
                     ctx.stage_add(ws.fp32 ? "gmres_matvec_fp32" : "gmres_matvec_fp64", ms, 1,
                                   entries * (ws.fp32 ? 8.0 : 16.0));
+                if (ws.ev_p0 && entries > 0) {
+                    float pms = 0;
+                    BEM_CUDA(cudaEventElapsedTime(&pms, ws.ev_p0, ws.ev_p1));
+                    ctx.stage_add("precond_apply", pms, 1, 0);
+                }
             }
             prev = st;
             bool all = true;
@@ -832,6 +845,9 @@ void gm_run(Context& ctx, GmWorkspace& ws, int chunk, int64_t max_total_iteratio
         }
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
+        if (ws.ev_p0) cudaEventDestroy(ws.ev_p0);
+        if (ws.ev_p1) cudaEventDestroy(ws.ev_p1);
+        ws.ev_p0 = ws.ev_p1 = nullptr;
         return;
     }
     if (!ws.graph_exec || ws.graph_chunk != chunk) {

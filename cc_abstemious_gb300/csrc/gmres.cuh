@@ -111,6 +111,13 @@ struct GmWorkspace {
     std::shared_ptr<void> precond_keep;  // owns the preconditioner data
     DevBuf zmem;
     DevBuf mem;
+    // grow-only buffers of the context used instead of zmem / mem when set
+    // (no allocation per solve)
+    DevBuf* mem_pool = nullptr;
+    DevBuf* z_pool = nullptr;
+    DevBuf& memb() { return mem_pool ? *mem_pool : mem; }
+    cudaEvent_t ev_p0 = nullptr, ev_p1 = nullptr;  // profiling: preconditioner application
+    DevBuf& zb() { return z_pool ? *z_pool : zmem; }
     DevBuf init_args;
     std::vector<GmSys> sys_host;  // ragged layout (empty: uniform)
     bool fp32 = false;

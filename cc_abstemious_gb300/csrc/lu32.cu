@@ -17,8 +17,8 @@
 //          (2k x n, re/im interleaved along the rows, which is how the
 //          column-major complex storage reads as floats) gives the natural
 //          real view of the product.  Tiles of 128 real rows x 256 columns,
-//          K = 256 in chunks of 32 staged by cp.async in the no-swizzle
-//          K-major core-matrix layout; a persistent warp-specialised kernel
+//          K = 256 in chunks of 32 staged by 2-D tensor copies (TMA) in the
+//          128-byte swizzled K-major layout; a persistent warp-specialised kernel
 //          (producer warp, MMA warp, eight epilogue warps, a four-stage operand
 //          ring and two tensor-memory accumulators) so that operand loads, MMAs
 //          and the read-modify-write of A22 overlap; every wait is bounded.
@@ -26,9 +26,11 @@
 // Applying M = U^-1 L^-1 to a Krylov vector (flexible right preconditioning:
 // Z[:, k] = M Q[:, k]) is a blocked forward and back substitution with the
 // kept diagonal-block inverses, one launch per block step, FP32 factors and
-// FP64 vectors.  The factorization is TF32-accurate, which is plenty for a
+// arithmetic (the Krylov vectors stay FP64).  The factorization is TF32-accurate, which is plenty for a
 // preconditioner: the FP64 outer GMRES with exact residuals decides the
 // answer, the factors only decide the iteration count.
+#include <cuda.h>
+
 #include <algorithm>
 #include <cmath>
 #include <memory>
@@ -59,6 +61,8 @@ struct LuSys {
     float2* F;    // factors (copy of the operator), column-major, leading dimension ld
     float2* Dm;   // per block: L11^-1 (strict lower) and U11^-1 (upper), LB x LB column-major
     float* W;     // real embedding of the current step's L21: 2n rows x 2 LB floats, row-major
+    const CUtensorMap* tmW;  // W as 2n rows x 256 floats, 128-byte swizzled 32 x 128 boxes
+    const CUtensorMap* tmF;  // F's natural real view: n columns x 2n floats, 32 x 256 boxes
     int64_t n, ld;
     int nblk, pad;
 };
@@ -284,17 +288,28 @@ __global__ void __launch_bounds__(256) lu_l21_kernel(const LuSys* __restrict__ s
 
 // ---------------------------------------------------------------------------
 // Trailing update on the tensor cores.
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+// 2-D tensor copy global -> shared (tensor map in global memory), completing
+// on the mbarrier.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* tmap, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-// Bulk prefetch into L2 (16-byte aligned address, size a multiple of 16).
-__device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+
+// Shared-memory descriptor of a K-major operand in the 128-byte swizzle
+// layout written by the tensor copies: rows of 128 bytes, 8-row atoms of
+// 1024 bytes (stride between atoms), descriptor version bit 46, layout type 2.
+// The start address moves 32 bytes per MMA along K inside the atom.
+__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;             // leading byte offset (unused for this layout)
+    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;             // 128-byte swizzle
+    return d;
 }
 
 __device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
@@ -311,15 +326,14 @@ __host__ __device__ constexpr uint32_t umma_idesc_tf32_f32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// Persistent, warp-specialised trailing update.  Warp 0 stages operand chunks
-// with cp.async into a ring of GS stages (GS - 1 chunks in flight; a stage is
-// published on its "full" barrier after the warp's own copies completed and
-// were fenced for the async proxy), lane 0 of warp 1 issues the MMAs of a
-// stage and releases it through tcgen05.commit on its "empty" barrier, and
-// warps 2-9 drain the accumulator of the previous tile (two accumulators of
-// 256 tensor-memory columns) while the next tile's MMAs run.
+// Persistent, warp-specialised trailing update.  One thread of warp 0 stages
+// operand chunks with two tensor copies each into a ring of GS stages (the
+// copies complete on the stage's "full" barrier), lane 0 of warp 1 issues
+// the MMAs of a stage and releases it through tcgen05.commit on its "empty"
+// barrier, and warps 2-9 drain the accumulator of the previous tile (two
+// accumulators of 256 tensor-memory columns) while the next tile's MMAs run.
 struct GemmTile {
-    const float* W;
+    const CUtensorMap *tmW, *tmF;
     float* F;
     int64_t n, rows, ld2, k0, kt, row0, col0;
 };
@@ -329,7 +343,8 @@ __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, con
     int64_t local;
     const LuSys S = sys[lu_locate(wl, nw, t, local)];
     GemmTile g;
-    g.W = S.W;
+    g.tmW = S.tmW;
+    g.tmF = S.tmF;
     g.F = reinterpret_cast<float*>(S.F);
     g.n = S.n;
     g.k0 = (int64_t)k * LB;
@@ -357,7 +372,7 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
     if (warp == 0) tmem_alloc(tmem_slot, G_TMEM_COLS);
     if (tid == 0) {
         for (int s = 0; s < GS; ++s) {
-            mbar_init(&full[s], 32);
+            mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
         for (int a = 0; a < 2; ++a) {
@@ -379,49 +394,31 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
     };
 
     if (warp == 0) {
-        // ---- producer
-        const int rl = lane & 7, q0 = lane >> 3;  // this lane's row-in-core and first K quad
-        int64_t it = 0;
-        for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
-            const GemmTile g = gemm_tile(sys, wl, nw, k, t);
-            for (int c = 0; c < GCHUNKS; ++c, ++it) {
-                const int st = (int)(it % GS);
-                const int64_t round = it / GS;
-                if (round > 0 && !mbar_wait_bounded(&empty[st], (uint32_t)((round - 1) & 1))) {
-                    fail();
-                    break;
-                }
-                const uint32_t As = base + st * GSTAGE, Bs = As + GA_BYTES;
-                // A: pieces (mg, q, rl) with q = q0 + 4 (i & 1), mg = i >> 1
-#pragma unroll
-                for (int i = 0; i < GM / 4; ++i) {
-                    const int mg = i >> 1, q = q0 + 4 * (i & 1);
-                    const int64_t r = g.row0 + mg * 8 + rl;
-                    const bool ok = r < g.rows;
-                    const float* src = g.W + (ok ? r : 0) * (2 * LB) + c * GK + q * 4;
-                    cp_async16(As + (uint32_t)((mg * 8 + q) * 128 + rl * 16), src, ok ? 16u : 0u);
-                }
-                // B: pieces (ng, q, rl), column j = col0 + 8 ng + rl
-#pragma unroll 8
-                for (int i = 0; i < GN / 4; ++i) {
-                    const int ng = i >> 1, q = q0 + 4 * (i & 1);
-                    const int64_t j = g.col0 + ng * 8 + rl;
-                    const bool ok = j < g.n;
-                    const float* src = g.F + (ok ? j : g.kt) * g.ld2 + 2 * g.k0 + c * GK + q * 4;
-                    cp_async16(Bs + (uint32_t)((ng * 8 + q) * 128 + rl * 16), src, ok ? 16u : 0u);
-                }
-                cp_async_commit();
-                if (it >= GS - 1) {
-                    // the chunk GS - 1 behind is complete: publish it
-                    cp_async_wait<GS - 1>();
-                    fence_proxy_async_shared();
-                    mbar_arrive(&full[(it - (GS - 1)) % GS]);
+        // ---- producer: one thread, two tensor copies per stage
+        if (lane == 0) {
+            int64_t it = 0;
+            for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+                const GemmTile g = gemm_tile(sys, wl, nw, k, t);
+                for (int c = 0; c < GCHUNKS; ++c, ++it) {
+                    const int st = (int)(it % GS);
+                    const int64_t round = it / GS;
+                    if (round > 0 && !mbar_wait_bounded(&empty[st], (uint32_t)((round - 1) & 1))) {
+                        fail();
+                        break;
+                    }
+                    const uint32_t As = base + st * GSTAGE, Bs = As + GA_BYTES;
+                    mbar_arrive_expect_tx(&full[st], GSTAGE);
+                    tma_load_2d(As, g.tmW, c * GK, (int)g.row0, &full[st]);
+                    tma_load_2d(Bs, g.tmF, (int)(2 * g.k0) + c * GK, (int)g.col0, &full[st]);
                 }
             }
+            if (*abort_flag) {
+                // copies may still be landing in the last stages: wait for them
+                for (int64_t j = it > GS ? it - GS : 0; j < it; ++j)
+                    mbar_wait_bounded(&full[j % GS], (uint32_t)((j / GS) & 1));
+            }
         }
-        cp_async_wait<0>();
-        fence_proxy_async_shared();
-        for (int64_t j = (it >= GS - 1 ? it - (GS - 1) : 0); j < it; ++j) mbar_arrive(&full[j % GS]);
+        __syncwarp();
     } else if (warp == 1) {
         // ---- MMA issuer
         const uint32_t idesc = umma_idesc_tf32_f32(GM, GN);
@@ -429,17 +426,6 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
         for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, ++tc) {
             const int acc = (int)(tc & 1);
             const int64_t use = tc >> 1;
-            if (lane > 0) {
-                // lanes 1-31: bring this tile's block of A22 into L2 for the epilogue
-                const GemmTile g = gemm_tile(sys, wl, nw, k, t);
-                const int64_t nrow = min((int64_t)GM, g.rows - g.row0);
-                const uint32_t bytes = (uint32_t)(nrow * 4) & ~15u;
-                for (int q = lane - 1; q < GN && bytes; q += 31) {
-                    const int64_t j = g.col0 + q;
-                    if (j >= g.n) break;
-                    l2_prefetch(g.F + j * g.ld2 + 2 * g.kt + g.row0, bytes);
-                }
-            }
             if (lane == 0 && use > 0 && !mbar_wait_bounded(&tempty[acc], (uint32_t)((use - 1) & 1))) fail();
             __syncwarp();
             if (*abort_flag) break;
@@ -453,8 +439,8 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                         const uint32_t a = base + st * GSTAGE, b = a + GA_BYTES;
 #pragma unroll
                         for (int kk = 0; kk < GK / 8; ++kk)
-                            umma_tf32(tmem + (uint32_t)(acc * GN), umma_smem_desc(a + kk * 256, 128, 1024),
-                                      umma_smem_desc(b + kk * 256, 128, 1024), idesc, (c | kk) ? 1u : 0u);
+                            umma_tf32(tmem + (uint32_t)(acc * GN), umma_desc_sw128(a + kk * 32),
+                                      umma_desc_sw128(b + kk * 32), idesc, (c | kk) ? 1u : 0u);
                         umma_commit(&empty[st]);
                     }
                 }
@@ -517,52 +503,57 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
 // Preconditioner application.  Forward: z = q, then for every block step
 // z_b -= L_bk z_k below block k, the block k + 1 finishing with
 // z_{k+1} = L^-1_{k+1} z_{k+1}.  Backward likewise with the U blocks above.
-__device__ __forceinline__ void cfma_fd(double2& acc, float2 a, double2 x) {
-    acc.x = fma((double)a.x, x.x, fma(-(double)a.y, x.y, acc.x));
-    acc.y = fma((double)a.x, x.y, fma((double)a.y, x.x, acc.y));
-}
-
-// z[0..nr) <- T z with T the lower (unit) or upper part of a kept inverse tile.
+// The substitutions run in FP32 (the factors are TF32-accurate; FP64 would
+// only slow them down on this part): z[0..nr) <- T z with T the lower (unit)
+// or upper part of a kept inverse tile.
 __device__ void lu_apply_inverse(const float2* __restrict__ Dk, int nr, bool lower, double2* __restrict__ z,
-                                 double2* xs, double2 (*red)[LB]) {
+                                 float2* xs, float2 (*red)[LB]) {
     const int row = threadIdx.x & (LB - 1), half = threadIdx.x >> 7;
-    if (half == 0) xs[row] = row < nr ? z[row] : make_double2(0, 0);
+    if (half == 0) {
+        const double2 v = row < nr ? z[row] : make_double2(0, 0);
+        xs[row] = make_float2((float)v.x, (float)v.y);
+    }
     __syncthreads();
-    double2 acc = make_double2(0, 0);
+    float2 acc = make_float2(0.f, 0.f);
     if (row < nr) {
-        const int p0 = half * (LB / 2), p1 = p0 + LB / 2;
+        const int p0 = half * (LB / 2), p1 = min(p0 + LB / 2, nr);
         for (int p = p0; p < p1; ++p) {
             const bool use = lower ? (p < row) : (p >= row);
-            if (use && p < nr) cfma_fd(acc, Dk[p * LB + row], xs[p]);
+            if (use) cfmaf_(acc, Dk[p * LB + row], xs[p]);
         }
     }
     red[half][row] = acc;
     __syncthreads();
     if (half == 0 && row < nr) {
-        double2 v = make_double2(red[0][row].x + red[1][row].x, red[0][row].y + red[1][row].y);
-        if (lower) v = make_double2(v.x + xs[row].x, v.y + xs[row].y);  // unit diagonal
-        z[row] = v;
+        float2 v = make_float2(red[0][row].x + red[1][row].x, red[0][row].y + red[1][row].y);
+        if (lower) v = make_float2(v.x + xs[row].x, v.y + xs[row].y);  // unit diagonal
+        z[row] = make_double2(v.x, v.y);
     }
     __syncthreads();
 }
 
 // z[r0 .. r0+nr) -= B x, B the nr x nc block of F at (r0, c0).
 __device__ void lu_block_update(const LuSys& S, int64_t r0, int nr, int64_t c0, int nc, const double2* __restrict__ x,
-                                double2* __restrict__ z, double2* xs, double2 (*red)[LB]) {
+                                double2* __restrict__ z, float2* xs, float2 (*red)[LB]) {
     const int row = threadIdx.x & (LB - 1), half = threadIdx.x >> 7;
-    if (half == 0) xs[row] = row < nc ? x[row] : make_double2(0, 0);
+    if (half == 0) {
+        const double2 v = row < nc ? x[row] : make_double2(0, 0);
+        xs[row] = make_float2((float)v.x, (float)v.y);
+    }
     __syncthreads();
-    double2 acc = make_double2(0, 0);
+    float2 acc = make_float2(0.f, 0.f);
     if (row < nr) {
         const int p0 = half * (LB / 2), p1 = min(p0 + LB / 2, nc);
-        for (int p = p0; p < p1; ++p) cfma_fd(acc, S.F[(c0 + p) * S.ld + r0 + row], xs[p]);
+        const float2* col = S.F + (c0 + p0) * S.ld + r0 + row;
+#pragma unroll 8
+        for (int p = p0; p < p1; ++p, col += S.ld) cfmaf_(acc, *col, xs[p]);
     }
     red[half][row] = acc;
     __syncthreads();
     if (half == 0 && row < nr) {
         double2 v = z[r0 + row];
-        v.x -= red[0][row].x + red[1][row].x;
-        v.y -= red[0][row].y + red[1][row].y;
+        v.x -= (double)(red[0][row].x + red[1][row].x);
+        v.y -= (double)(red[0][row].y + red[1][row].y);
         z[r0 + row] = v;
     }
     __syncthreads();
@@ -570,8 +561,8 @@ __device__ void lu_block_update(const LuSys& S, int64_t r0, int nr, int64_t c0, 
 
 __global__ void __launch_bounds__(256) lu_fwd_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
                                                      int nw, int k, GmBatch bt) {
-    __shared__ double2 xs[LB];
-    __shared__ double2 red[2][LB];
+    __shared__ float2 xs[LB];
+    __shared__ float2 red[2][LB];
     int64_t local;
     const int s = lu_locate(wl, nw, blockIdx.x, local);
     const GmState& st = bt.st[s];
@@ -597,8 +588,8 @@ __global__ void __launch_bounds__(256) lu_fwd_kernel(const LuSys* __restrict__ s
 
 __global__ void __launch_bounds__(256) lu_bwd_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
                                                      int nw, int t, GmBatch bt) {
-    __shared__ double2 xs[LB];
-    __shared__ double2 red[2][LB];
+    __shared__ float2 xs[LB];
+    __shared__ float2 red[2][LB];
     int64_t local;
     const int s = lu_locate(wl, nw, blockIdx.x, local);
     const GmState& st = bt.st[s];
@@ -620,7 +611,7 @@ __global__ void __launch_bounds__(256) lu_bwd_kernel(const LuSys* __restrict__ s
 
 // ---------------------------------------------------------------------------
 struct LuData {
-    DevBuf F, Dm, W, sysbuf, work, info;
+    DevBuf sysbuf, work, info, maps;
     std::vector<LuSys> sys;
     int nblk_max = 0;
     // work lists: per launch, [offset, count, ctas] into `work`
@@ -672,6 +663,12 @@ void lu_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
 // Factors every operator of the batch and installs the preconditioner hook.
 void lu_precond_setup(Context& c, GmWorkspace& ws) {
     require(ws.fp32, "LU preconditioner: FP32 operators only");
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (c.profiling) {
+        BEM_CUDA(cudaEventCreate(&t0));
+        BEM_CUDA(cudaEventCreate(&t1));
+        BEM_CUDA(cudaEventRecord(t0, c.stream));
+    }
     auto d = std::make_shared<LuData>();
     const int nsys = ws.bt.nsys;
     std::vector<GmView> v((size_t)nsys);
@@ -690,23 +687,54 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         wsz += (size_t)2 * v[(size_t)s].n * 2 * LB;
         d->nblk_max = std::max(d->nblk_max, nb);
     }
-    d->F.ensure(sizeof(float2) * entries);
-    d->Dm.ensure(sizeof(float2) * std::max<size_t>(dm, 1));
-    d->W.ensure(sizeof(float) * std::max<size_t>(wsz, 4));
-    BEM_CUDA(cudaMemcpyAsync(d->F.p, ws.bt.A, sizeof(float2) * entries, cudaMemcpyDeviceToDevice, c.stream));
+    // the factors, block inverses and panel workspace live in grow-only
+    // buffers of the context
+    c.w_lu_F.ensure(sizeof(float2) * entries);
+    c.w_lu_D.ensure(sizeof(float2) * std::max<size_t>(dm, 1));
+    c.w_lu_W.ensure(sizeof(float) * std::max<size_t>(wsz, 4));
+    BEM_CUDA(cudaMemcpyAsync(c.w_lu_F.p, ws.bt.A, sizeof(float2) * entries, cudaMemcpyDeviceToDevice, c.stream));
     d->sys.resize((size_t)nsys);
+    d->maps.ensure(sizeof(CUtensorMap) * 2 * nsys);
+    std::vector<CUtensorMap> maps((size_t)(2 * nsys));
     size_t od = 0, ow = 0;
     for (int s = 0; s < nsys; ++s) {
         LuSys& L = d->sys[(size_t)s];
-        L.F = d->F.as<float2>() + v[(size_t)s].a;
-        L.Dm = d->Dm.as<float2>() + od;
-        L.W = d->W.as<float>() + ow;
+        L.F = c.w_lu_F.as<float2>() + v[(size_t)s].a;
+        L.Dm = c.w_lu_D.as<float2>() + od;
+        L.W = c.w_lu_W.as<float>() + ow;
         L.n = v[(size_t)s].n;
         L.ld = v[(size_t)s].lda;
         L.nblk = (int)((L.n + LB - 1) / LB);
         od += (size_t)L.nblk * LB * LB;
         ow += (size_t)2 * L.n * 2 * LB;
+        // W: 2n rows of 2 LB floats; boxes of 32 floats (128 bytes) x 128 rows
+        const cuuint32_t es[2] = {1, 1};
+        {
+            const cuuint64_t dims[2] = {(cuuint64_t)(2 * LB), (cuuint64_t)(2 * L.n)};
+            const cuuint64_t strides[1] = {(cuuint64_t)(2 * LB * sizeof(float))};
+            const cuuint32_t box[2] = {(cuuint32_t)GK, (cuuint32_t)GM};
+            const CUresult r = cuTensorMapEncodeTiled(&maps[(size_t)(2 * s)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                                                      L.W, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                                      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            require(r == CUDA_SUCCESS, "LU: tensor map of the panel workspace");
+        }
+        // F: n columns of 2n floats (natural real view), leading dimension 2 ld
+        {
+            const cuuint64_t dims[2] = {(cuuint64_t)(2 * L.n), (cuuint64_t)L.n};
+            const cuuint64_t strides[1] = {(cuuint64_t)(2 * L.ld * sizeof(float))};
+            const cuuint32_t box[2] = {(cuuint32_t)GK, (cuuint32_t)GN};
+            const CUresult r = cuTensorMapEncodeTiled(&maps[(size_t)(2 * s + 1)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                                                      L.F, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                                      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            require(r == CUDA_SUCCESS, "LU: tensor map of the factors");
+        }
+        L.tmW = d->maps.as<CUtensorMap>() + 2 * s;
+        L.tmF = d->maps.as<CUtensorMap>() + 2 * s + 1;
     }
+    BEM_CUDA(cudaMemcpyAsync(d->maps.p, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice,
+                             c.stream));
     // work lists of every launch
     for (int k = 0; k < d->nblk_max; ++k) {
         std::vector<std::pair<int, int64_t>> ed, eu, el, eg;
@@ -816,8 +844,17 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     check_device_err(c);
     BEM_CUDA(cudaMemcpyAsync(&d->small_pivots, d->info.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     c.sync();
-    ws.zmem.ensure(sizeof(double2) * gm_q_total(ws));
-    ws.bt.Z = ws.zmem.as<double2>();
+    if (c.profiling) {
+        BEM_CUDA(cudaEventRecord(t1, c.stream));
+        BEM_CUDA(cudaEventSynchronize(t1));
+        float ms = 0;
+        BEM_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+        c.stage_add("lu_setup_total", ms, 1, 0);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+    }
+    ws.zb().ensure(sizeof(double2) * gm_q_total(ws));
+    ws.bt.Z = ws.zb().as<double2>();
     ws.precond = lu_hook;
     ws.precond_user = d.get();
     ws.precond_keep = d;

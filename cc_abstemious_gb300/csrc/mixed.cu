@@ -125,6 +125,8 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     int m = (int)std::ceil(std::sqrt((double)max_it));
     int64_t restarts = max_it / m;
     GmWorkspace ws;
+    ws.mem_pool = &c.w_gm;
+    ws.z_pool = &c.w_gmz;
     gm_prepare(c, ws, (int)nf, n, m, first_kind ? (const void*)A64 : (const void*)A32, ld, mstride, !first_kind,
                false);
 

@@ -707,8 +707,8 @@ bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond k
         h->use_off = true;
         c.sync();
     }
-    ws.zmem.ensure(sizeof(double2) * gm_q_total(ws));
-    ws.bt.Z = ws.zmem.as<double2>();
+    ws.zb().ensure(sizeof(double2) * gm_q_total(ws));
+    ws.bt.Z = ws.zb().as<double2>();
     ws.precond = pc_hook;
     ws.precond_user = h.get();
     ws.precond_keep = h;
@@ -785,8 +785,8 @@ bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies,
         h->use_off = true;
     }
     c.sync();
-    ws.zmem.ensure(sizeof(double2) * gm_q_total(ws));
-    ws.bt.Z = ws.zmem.as<double2>();
+    ws.zb().ensure(sizeof(double2) * gm_q_total(ws));
+    ws.bt.Z = ws.zb().as<double2>();
     ws.precond = pc_hook;
     ws.precond_user = h.get();
     ws.precond_keep = h;
