@@ -60,7 +60,7 @@ def build(force=False, verbose=False, extra=()):
         objs = list(ex.map(lambda s: _compile(s, verbose, list(extra)), srcs))
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
         return LIB
-    cmd = [NVCC] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcuda"]
+    cmd = [NVCC] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs
     if verbose:
         print(" ".join(cmd), flush=True)
     subprocess.run(cmd, check=True)

@@ -30,6 +30,7 @@
 // preconditioner: the FP64 outer GMRES with exact residuals decides the
 // answer, the factors only decide the iteration count.
 #include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -660,6 +661,20 @@ void lu_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
 
 }  // namespace
 
+// The driver's tensor-map encoder, looked up through the runtime (the library
+// then needs no link-time dependency on the driver library).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        BEM_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        require(p != nullptr && q == cudaDriverEntryPointSuccess, "cuTensorMapEncodeTiled unavailable", BEM_ERR_CUDA);
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
 // Factors every operator of the batch and installs the preconditioner hook.
 void lu_precond_setup(Context& c, GmWorkspace& ws) {
     require(ws.fp32, "LU preconditioner: FP32 operators only");
@@ -696,6 +711,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     d->sys.resize((size_t)nsys);
     d->maps.ensure(sizeof(CUtensorMap) * 2 * nsys);
     std::vector<CUtensorMap> maps((size_t)(2 * nsys));
+    const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
     size_t od = 0, ow = 0;
     for (int s = 0; s < nsys; ++s) {
         LuSys& L = d->sys[(size_t)s];
@@ -713,7 +729,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
             const cuuint64_t dims[2] = {(cuuint64_t)(2 * LB), (cuuint64_t)(2 * L.n)};
             const cuuint64_t strides[1] = {(cuuint64_t)(2 * LB * sizeof(float))};
             const cuuint32_t box[2] = {(cuuint32_t)GK, (cuuint32_t)GM};
-            const CUresult r = cuTensorMapEncodeTiled(&maps[(size_t)(2 * s)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+            const CUresult r = encode(&maps[(size_t)(2 * s)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
                                                       L.W, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                                       CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -724,7 +740,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
             const cuuint64_t dims[2] = {(cuuint64_t)(2 * L.n), (cuuint64_t)L.n};
             const cuuint64_t strides[1] = {(cuuint64_t)(2 * L.ld * sizeof(float))};
             const cuuint32_t box[2] = {(cuuint32_t)GK, (cuuint32_t)GN};
-            const CUresult r = cuTensorMapEncodeTiled(&maps[(size_t)(2 * s + 1)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+            const CUresult r = encode(&maps[(size_t)(2 * s + 1)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
                                                       L.F, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                                       CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
