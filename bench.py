@@ -548,31 +548,44 @@ def bench_held_out_learned(args):
     sc = np.zeros((nf, pd.nfp), dtype=np.complex128)
     inc = np.zeros((nf, pd.nfp), dtype=np.complex128)
     results = {}
-    for name, code in (("none", 0), ("block_jacobi", 1), ("learned", 2), ("lu", 3)):
+    forms = {"none": (bem.FORM_MIXED, 0), "block_jacobi": (bem.FORM_MIXED, 1), "learned": (bem.FORM_MIXED, 2),
+             "lu": (bem.FORM_MIXED, 3), "lu_refined": (bem.FORM_REFINED, 3)}
+    for name, (form, code) in forms.items():
         reps = (bem.SolveReport * nf)()
 
         def step():
-            ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_MIXED, code, bem._ptr(sc), bem._ptr(inc), reps, 0))
+            ctx.check(ctx.lib.bem_run(ctx.h, pd.h, form, code, bem._ptr(sc), bem._ptr(inc), reps, 0))
 
         ms, clk = _timed_region(args, local, step, stream)
         results[name] = {"value": nf * 1000.0 / ms, "ms_per_step": ms, "clocks": clk,
                          "iterations": [reps[i].iterations for i in range(nf)],
                          "converged": all(reps[i].flag == 1 for i in range(nf)),
                          "precond_used": [reps[i].precond for i in range(nf)]}
-    # the headline form: the fastest whose every system converged
-    ok = [k for k in results if results[k]["converged"]] or list(results)
-    best = max(ok, key=lambda k: results[k]["value"])
-    code_best = {"none": 0, "block_jacobi": 1, "learned": 2, "lu": 3}[best]
-    # FP64 LU error of that form at the lowest and highest ka
-    errs = {}
-    for i in (0, nf - 1):
-        one = dict(held, frequency={"List": {"values": [held["frequency"]["List"]["values"][i]]}})
-        p1 = bem.PreData.from_dict(one, ctx=ctx)
-        r1 = (bem.SolveReport * 1)()
-        s1 = np.zeros((1, pd.nfp), dtype=np.complex128)
-        ctx.check(ctx.lib.bem_run(ctx.h, p1.h, bem.FORM_MIXED, code_best, bem._ptr(s1), bem._ptr(s1), r1, 1))
-        errs["ka%.2f" % kas[i]] = r1[0].rel_err_vs_lu
-        del p1
+    # the headline form: the fastest whose every system converged and whose
+    # error against FP64 LU (lowest and highest ka) is within 1e-6
+    def lu_errors(name):
+        form, code = forms[name]
+        out = {}
+        for i in (0, nf - 1):
+            one = dict(held, frequency={"List": {"values": [held["frequency"]["List"]["values"][i]]}})
+            p1 = bem.PreData.from_dict(one, ctx=ctx)
+            r1 = (bem.SolveReport * 1)()
+            s1 = np.zeros((1, pd.nfp), dtype=np.complex128)
+            ctx.check(ctx.lib.bem_run(ctx.h, p1.h, form, code, bem._ptr(s1), bem._ptr(s1), r1, 1))
+            out["ka%.2f" % kas[i]] = r1[0].rel_err_vs_lu
+            del p1
+        return out
+
+    ok = sorted([k for k in results if results[k]["converged"]] or list(results),
+                key=lambda k: -results[k]["value"])
+    best, errs = ok[0], {}
+    for cand in ok:
+        e = lu_errors(cand)
+        results[cand]["rel_err_vs_fp64_lu"] = e
+        best, errs = cand, e
+        if max(e.values()) <= 1e-6:
+            break
+    form_best, code_best = forms[best]
     plain = None
     if not args.no_plain:
         reps = (bem.SolveReport * nf)()
@@ -585,7 +598,7 @@ def bench_held_out_learned(args):
         plain = {"value": nf * 1000.0 / pms, "unit": UNIT, "ms_per_step": pms,
                  "iterations": [reps[i].iterations for i in range(nf)]}
     ctx.set_profiling(True)
-    ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_MIXED, code_best, bem._ptr(sc), bem._ptr(inc),
+    ctx.check(ctx.lib.bem_run(ctx.h, pd.h, form_best, code_best, bem._ptr(sc), bem._ptr(inc),
                               (bem.SolveReport * nf)(), 0))
     prof = ctx.profile()
     ctx.set_profiling(False)
@@ -598,8 +611,9 @@ def bench_held_out_learned(args):
         "config": {"workload": "held_out_learned", "n_unknowns": pd.n, "frequencies": nf, "ka": [4.0, 16.0],
                    "solver": "GMRES tol 1e-8 (backward error; 1e-6 leaves ~1.3e-6 forward error)",
                    "precond": best,
-                   "precond_note": "value = fastest preconditioner with every system converged; all four "
-                                   "are listed under by_precond",
+                   "precond_note": "value = fastest form with every system converged and its error "
+                                   "against FP64 LU within 1e-6; every candidate is listed under by_precond "
+                                   "(lu_refined: FP64 operator, TF32 LU preconditioner)",
                    "training": {"bodies": len(train), "steps": args.train_steps, "seconds": train_s,
                                 "loss_first": float(np.mean(losses[:10])), "loss_last": float(np.mean(losses[-10:]))},
                    "parallelism": "replicas only"},

@@ -19,7 +19,7 @@ import os
 import numpy as np
 
 from . import _lib
-from ._lib import (BemError, FORM_MIXED, FORM_PLAIN_FP64, MEM_DEVICE, MEM_HOST, PRECOND_BLOCK_JACOBI,
+from ._lib import (BemError, FORM_MIXED, FORM_PLAIN_FP64, FORM_REFINED, MEM_DEVICE, MEM_HOST, PRECOND_BLOCK_JACOBI,
                    PRECOND_LEARNED, PRECOND_LU, PRECOND_NONE, SIDE_LHS, SIDE_RHS, SolveReport)
 
 __all__ = ["Analysis", "Context", "PreData", "FPResult", "BemError", "get_dense_surface_matrices",
@@ -369,7 +369,7 @@ class Analysis:
         sc = np.zeros((nf, max(nfp, 1)), dtype=np.complex128)
         inc = np.zeros((nf, max(nfp, 1)), dtype=np.complex128)
         reps = (SolveReport * max(nf, 1))()
-        f = FORM_MIXED if form == "mixed" else FORM_PLAIN_FP64
+        f = {"plain": FORM_PLAIN_FP64, "mixed": FORM_MIXED, "refined": FORM_REFINED}[form]
         pc = {None: PRECOND_NONE, "none": PRECOND_NONE, "block_jacobi": PRECOND_BLOCK_JACOBI,
               "learned": PRECOND_LEARNED, "lu": PRECOND_LU}[precond]
         st = ctx.lib.bem_run(ctx.h, pd.h, f, pc, _ptr(sc), _ptr(inc), reps, 1 if check_vs_lu else 0)

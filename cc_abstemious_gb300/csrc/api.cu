@@ -660,8 +660,8 @@ BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* pp, bem_form form, bem_pre
                 std::memset(&reports[f], 0, sizeof(bem_solve_report));
                 reports[f].rel_err_vs_lu = -1;
             }
-        if (form == BEM_FORM_MIXED) {
-            run_mixed(c, p, precond, scattered, incident, reports, check_vs_lu != 0);
+        if (form == BEM_FORM_MIXED || form == BEM_FORM_REFINED) {
+            run_mixed(c, p, precond, scattered, incident, reports, check_vs_lu != 0, form == BEM_FORM_REFINED);
             return;
         }
         // analysis.rs:87-111, one frequency at a time

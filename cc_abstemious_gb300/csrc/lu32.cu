@@ -94,6 +94,14 @@ __device__ __forceinline__ void cfmaf_(float2& acc, float2 a, float2 b) {
     acc.y = fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y));
 }
 
+// FP32 rounding of an FP64 operator buffer.
+__global__ void lu_round_kernel(const double2* __restrict__ A, size_t n, float2* __restrict__ F) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double2 v = A[i];
+        F[i] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Diagonal block: LU without pivoting, then both triangular inverses in place.
 __global__ void __launch_bounds__(1024) lu_diag_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
@@ -677,7 +685,6 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 // Factors every operator of the batch and installs the preconditioner hook.
 void lu_precond_setup(Context& c, GmWorkspace& ws) {
-    require(ws.fp32, "LU preconditioner: FP32 operators only");
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     if (c.profiling) {
         BEM_CUDA(cudaEventCreate(&t0));
@@ -707,7 +714,15 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     c.w_lu_F.ensure(sizeof(float2) * entries);
     c.w_lu_D.ensure(sizeof(float2) * std::max<size_t>(dm, 1));
     c.w_lu_W.ensure(sizeof(float) * std::max<size_t>(wsz, 4));
-    BEM_CUDA(cudaMemcpyAsync(c.w_lu_F.p, ws.bt.A, sizeof(float2) * entries, cudaMemcpyDeviceToDevice, c.stream));
+    if (ws.fp32) {
+        BEM_CUDA(cudaMemcpyAsync(c.w_lu_F.p, ws.bt.A, sizeof(float2) * entries, cudaMemcpyDeviceToDevice, c.stream));
+    } else {
+        // FP64 operator (refined form): factor its FP32 rounding
+        const unsigned g = (unsigned)std::min<size_t>((entries + 255) / 256, (size_t)1 << 20);
+        lu_round_kernel<<<g, 256, 0, c.stream>>>(static_cast<const double2*>(ws.bt.A), entries,
+                                                 c.w_lu_F.as<float2>());
+        BEM_CHECK_LAUNCH(&c);
+    }
     d->sys.resize((size_t)nsys);
     d->maps.ensure(sizeof(CUtensorMap) * 2 * nsys);
     std::vector<CUtensorMap> maps((size_t)(2 * nsys));

@@ -79,7 +79,7 @@ double lu_reference_error(Context& c, const Problem& p, const double* phi_host, 
 }
 
 void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered, bem_cplx* incident,
-               bem_solve_report* reports, bool check_vs_lu) {
+               bem_solve_report* reports, bool check_vs_lu, bool fp64_operator) {
     require(p.in.solver != 2 || true, "");
     c.stages.clear();
     const int64_t nf = (int64_t)p.freqs.size(), n = p.n, nfp = p.nfp;
@@ -102,8 +102,9 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
 
     // A first-kind operator (classical formulation with a pressure condition:
     // the single layer G alone) is too ill-conditioned for single-precision
-    // storage at 1e-6; those systems keep an FP64 operator in the same batch.
-    const bool first_kind = p.in.method_type == 0 && p.in.bc_type == 0;
+    // storage at 1e-6; those systems keep an FP64 operator in the same batch,
+    // as every operator of the refined form does.
+    const bool first_kind = fp64_operator || (p.in.method_type == 0 && p.in.bc_type == 0);
     c.w_mat.ensure((first_kind ? sizeof(double2) : sizeof(float2)) * mstride * nf);
     float2* A32 = c.w_mat.as<float2>();
     double2* A64 = c.w_mat.as<double2>();

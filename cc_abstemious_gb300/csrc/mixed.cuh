@@ -5,7 +5,7 @@
 namespace bem {
 
 void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered, bem_cplx* incident,
-               bem_solve_report* reports, bool check_vs_lu);
+               bem_solve_report* reports, bool check_vs_lu, bool fp64_operator = false);
 // Several bodies: every frequency of every body in one ragged batch (chunks
 // of at most budget_bytes of operators; 0: a share of the free memory).
 void run_mixed_batch(Context& c, const std::vector<Problem*>& probs, bem_precond precond,

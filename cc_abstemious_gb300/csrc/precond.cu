@@ -684,8 +684,7 @@ static void pc_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
 
 bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks) {
     if (kind == BEM_PRECOND_LU) {
-        if (!ws.fp32) return BEM_PRECOND_NONE;  // first-kind operators stay FP64
-        lu_precond_setup(c, ws);
+        lu_precond_setup(c, ws);  // FP64 operators are factored from their FP32 rounding
         return kind;
     }
     require(kind == BEM_PRECOND_BLOCK_JACOBI || kind == BEM_PRECOND_LEARNED, "unknown preconditioner");

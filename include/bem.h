@@ -56,8 +56,13 @@ typedef enum { BEM_SIDE_RHS = 0, BEM_SIDE_LHS = 1 } bem_side;
  *  MIXED:      all frequencies batched; FP32 assembly with accurate phase
  *              reduction, FP64 restarted GMRES over the FP32 operator with
  *              compensated mat-vecs, optional preconditioner; each result
- *              reports its error against an FP64 LU when requested. */
-typedef enum { BEM_FORM_PLAIN_FP64 = 0, BEM_FORM_MIXED = 1 } bem_form;
+ *              reports its error against an FP64 LU when requested.
+ *  REFINED:    as MIXED, but every operator is assembled and kept in FP64
+ *              (residuals and the answer at FP64 accuracy; for operators whose
+ *              condition number makes FP32 storage miss 1e-6), while the
+ *              preconditioner is built from its FP32 rounding (the TF32
+ *              tensor-core LU of BEM_PRECOND_LU). */
+typedef enum { BEM_FORM_PLAIN_FP64 = 0, BEM_FORM_MIXED = 1, BEM_FORM_REFINED = 2 } bem_form;
 
 /* Preconditioners of the mixed form (no counterpart in the reference, whose
  * GMRES is unpreconditioned, gmres.rs:80-140).  Flexible right

@@ -80,11 +80,29 @@ def test_lu_ragged_batch(ctx, wd):
             assert abs(r["iterations"] - s["iterations"]) <= 1
 
 
-def test_lu_first_kind_falls_back(ctx, wd):
-    """A first-kind operator keeps an FP64 operator: no LU preconditioner."""
+def test_lu_first_kind(ctx, wd):
+    """A first-kind operator keeps an FP64 operator; the LU is built from its
+    FP32 rounding."""
     inp = workloads.perturbed_sphere_input(wd, 9, 400, [1.5], tol=1e-8)
     inp["method_type"] = "Classical"
     inp["surface_bc"] = {"bc_type": "Pressure", "value": [0.0, 0.0]}
+    r0 = _run(ctx, inp, None)[0]
     r = _run(ctx, inp, "lu")[0]
-    assert r["flag"] == 1 and r["precond"] == bem.PRECOND_NONE
+    assert r["flag"] == 1 and r["precond"] == bem.PRECOND_LU
     assert 0 <= r["rel_err_vs_lu"] < 1e-6
+    assert r["iterations"] < r0["iterations"]
+
+
+def test_refined_form(ctx, wd):
+    """FP64 operator + TF32 LU preconditioner: FP64-level agreement with the
+    FP64 LU where the FP32 operator of the mixed form stops near 1e-7."""
+    inp = workloads.perturbed_sphere_input(wd, 12, 2500, [4.0, 9.0], tol=1e-11)
+    a = bem.Analysis(ctx)
+    a.set_input(inp)
+    a.run(form="refined", precond="lu", check_vs_lu=True)
+    m = _run(ctx, inp, "lu")
+    for r, rm in zip(a.reports, m):
+        assert r["flag"] == 1 and r["precond"] == bem.PRECOND_LU
+        assert 0 <= r["rel_err_vs_lu"] < 1e-8, r
+        assert r["rel_err_vs_lu"] < rm["rel_err_vs_lu"]
+        assert r["iterations"] <= 12
