@@ -4,6 +4,7 @@
 // GMRES over the FP32 operators (compensated mat-vecs), and the field points
 // are evaluated in FP64.  The error against an FP64 LU of the same operator is
 // measured on request, outside any timed region.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -78,12 +79,11 @@ double lu_reference_error(Context& c, const Problem& p, const double* phi_host, 
     return std::sqrt(num / den);
 }
 
-void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered, bem_cplx* incident,
-               bem_solve_report* reports, bool check_vs_lu, bool fp64_operator) {
-    require(p.in.solver != 2 || true, "");
-    c.stages.clear();
-    const int64_t nf = (int64_t)p.freqs.size(), n = p.n, nfp = p.nfp;
-    require(nf >= 1, "no frequencies");
+// Frequencies [F0, F0 + nf) of the problem as one batch.
+static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_precond precond,
+                            bem_cplx* scattered, bem_cplx* incident, bem_solve_report* reports, bool check_vs_lu,
+                            bool fp64_operator) {
+    const int64_t n = p.n, nfp = p.nfp;
     const int64_t ld = p.geo.npad;  // multiple of 64: aligned float4 loads
     const size_t mstride = (size_t)ld * n;
     const int64_t saved_ifreq = p.ifreq;
@@ -93,7 +93,7 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     std::vector<double> ks(nf);
     std::vector<cd> al(nf), be(nf), ga(nf), de(nf);
     for (int64_t f = 0; f < nf; ++f) {
-        p.ifreq = f;
+        p.ifreq = F0 + f;
         ks[f] = p.wavenumber();
         lhs_factors(p, al[f], be[f]);
         rhs_factors(p, ga[f], de[f]);
@@ -134,7 +134,7 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     if (first_kind) {
         EventTimer t(c);
         for (int64_t f = 0; f < nf; ++f) {
-            p.ifreq = f;
+            p.ifreq = F0 + f;
             assemble_system_fp64(c, p, A64 + f * mstride, ld, al[f], be[f], ga[f], de[f],
                                  need_rowsum ? rowsum + f * n : nullptr);
         }
@@ -150,7 +150,7 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     {
         EventTimer t(c);
         for (int64_t f = 0; f < nf; ++f) {
-            p.ifreq = f;
+            p.ifreq = F0 + f;
             incident_surface(c, p, inc + f * n);
         }
         t.stop("incident", nf, 0);
@@ -175,7 +175,7 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     {
         EventTimer t(c);
         for (int64_t f = 0; f < nf; ++f) {
-            p.ifreq = f;
+            p.ifreq = F0 + f;
             unpack_solution(c, p, ws.bt.X + f * n, phi + f * n, vn + f * n);
             incident_field(c, p, finc + f * nfp);
         }
@@ -183,20 +183,18 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
         t.stop("field", 1, 0);
     }
     std::vector<double2> hs((size_t)(nf * nfp)), hi((size_t)(nf * nfp));
-    c.last_phi.assign((size_t)(2 * n * nf), 0.0);
-    c.last_vn.assign((size_t)(2 * n * nf), 0.0);
-    c.last_n = n;
-    c.last_nf = nf;
     if (nfp) {
         BEM_CUDA(cudaMemcpyAsync(hs.data(), fps, sizeof(double2) * nf * nfp, cudaMemcpyDeviceToHost, c.stream));
         BEM_CUDA(cudaMemcpyAsync(hi.data(), finc, sizeof(double2) * nf * nfp, cudaMemcpyDeviceToHost, c.stream));
     }
-    BEM_CUDA(cudaMemcpyAsync(c.last_phi.data(), phi, sizeof(double2) * nf * n, cudaMemcpyDeviceToHost, c.stream));
-    BEM_CUDA(cudaMemcpyAsync(c.last_vn.data(), vn, sizeof(double2) * nf * n, cudaMemcpyDeviceToHost, c.stream));
+    BEM_CUDA(cudaMemcpyAsync(c.last_phi.data() + 2 * n * F0, phi, sizeof(double2) * nf * n, cudaMemcpyDeviceToHost,
+                             c.stream));
+    BEM_CUDA(cudaMemcpyAsync(c.last_vn.data() + 2 * n * F0, vn, sizeof(double2) * nf * n, cudaMemcpyDeviceToHost,
+                             c.stream));
     c.sync();
     double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     for (int64_t f = 0; f < nf; ++f) {
-        p.ifreq = f;
+        p.ifreq = F0 + f;
         double w = p.in.output_pressure ? p.omega() * p.in.mass_density : 0.0;
         for (int64_t i = 0; i < nfp; ++i) {
             double2 a = hs[(size_t)(f * nfp + i)], q = hi[(size_t)(f * nfp + i)];
@@ -204,11 +202,12 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
                 a = make_double2(-a.y * w, a.x * w);
                 q = make_double2(-q.y * w, q.x * w);
             }
-            if (scattered) { scattered[f * nfp + i].re = a.x; scattered[f * nfp + i].im = a.y; }
-            if (incident) { incident[f * nfp + i].re = q.x; incident[f * nfp + i].im = q.y; }
+            const int64_t o = (F0 + f) * nfp + i;
+            if (scattered) { scattered[o].re = a.x; scattered[o].im = a.y; }
+            if (incident) { incident[o].re = q.x; incident[o].im = q.y; }
         }
         if (reports) {
-            bem_solve_report& r = reports[f];
+            bem_solve_report& r = reports[F0 + f];
             r.num_mv = st[(size_t)f].num_mv;
             r.restarts = st[(size_t)f].restarts + (st[(size_t)f].converged ? 1 : 0);
             r.iterations = st[(size_t)f].iterations;
@@ -220,13 +219,36 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
         }
     }
     if (check_vs_lu && reports) {
-        for (int64_t f = 0; f < nf; ++f) {
+        for (int64_t f = F0; f < F0 + nf; ++f) {
             p.ifreq = f;
             reports[f].rel_err_vs_lu =
                 lu_reference_error(c, p, c.last_phi.data() + 2 * n * f, c.last_vn.data() + 2 * n * f);
         }
     }
     p.ifreq = saved_ifreq;
+}
+
+void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered, bem_cplx* incident,
+               bem_solve_report* reports, bool check_vs_lu, bool fp64_operator) {
+    c.stages.clear();
+    const int64_t nf = (int64_t)p.freqs.size(), n = p.n;
+    require(nf >= 1, "no frequencies");
+    c.last_phi.assign((size_t)(2 * n * nf), 0.0);
+    c.last_vn.assign((size_t)(2 * n * nf), 0.0);
+    c.last_n = n;
+    c.last_nf = nf;
+    // frequencies per batch: the operators (and the LU copy) within 60% of the
+    // device memory the context can use
+    const bool op64 = fp64_operator || (p.in.method_type == 0 && p.in.bc_type == 0);
+    const double ent = (double)p.geo.npad * (double)n;
+    const double per = ent * (op64 ? 16.0 : 8.0) + (precond == BEM_PRECOND_LU ? ent * 8.0 + 3072.0 * n : 0.0);
+    size_t fr = 0, tot = 0;
+    BEM_CUDA(cudaMemGetInfo(&fr, &tot));
+    const double budget = 0.6 * (double)(fr + c.w_mat.bytes + c.w_lu_F.bytes);
+    const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nf, (int64_t)(budget / per)));
+    for (int64_t f0 = 0; f0 < nf; f0 += chunk)
+        run_mixed_range(c, p, f0, std::min(chunk, nf - f0), precond, scattered, incident, reports, check_vs_lu,
+                        fp64_operator);
 }
 
 }  // namespace bem
