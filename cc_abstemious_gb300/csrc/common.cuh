@@ -168,6 +168,7 @@ struct Context {
     // diagonal-block inverses and panel workspace (grow-only, reused by
     // every mixed solve)
     DevBuf w_gm, w_gmz, w_lu_F, w_lu_D, w_lu_W;
+    DevBuf w_upload;  // mesh staging of problem construction
     // results of the last bem_run
     std::vector<double> last_phi, last_vn;
     int64_t last_n = 0, last_nf = 0;

@@ -107,7 +107,7 @@ void compute_collocation(Context& ctx, Problem& p) {
         if (t != 5 && t != 9) continue;
         int64_t nn = m.conn_off[(size_t)e + 1] - m.conn_off[(size_t)e];
         int need = t == 5 ? 3 : 4;
-        require(nn >= need, "VTK: element " + std::to_string(e) + " has too few nodes");
+        if (nn < need) throw Error(BEM_ERR_BAD_INPUT, "VTK: element " + std::to_string(e) + " has too few nodes");
         int64_t ids[4] = {0, 0, 0, 0};
         for (int a = 0; a < need; ++a) {
             ids[a] = m.conn[(size_t)(m.conn_off[(size_t)e] + a)];
@@ -122,18 +122,21 @@ void compute_collocation(Context& ctx, Problem& p) {
     p.geo.n = n;
     p.geo.npad = (n + 63) / 64 * 64;
     p.geo.buf.ensure(sizeof(double) * GEO_NARR * (size_t)p.geo.npad);
-    DevBuf d_nodes, d_et, d_en;
-    d_nodes.ensure(sizeof(double) * m.nodes.size());
-    d_et.ensure(sizeof(int32_t) * et.size());
-    d_en.ensure(sizeof(int64_t) * en.size());
-    BEM_CUDA(cudaMemcpyAsync(d_nodes.p, m.nodes.data(), sizeof(double) * m.nodes.size(),
-                             cudaMemcpyHostToDevice, ctx.stream));
-    BEM_CUDA(cudaMemcpyAsync(d_et.p, et.data(), sizeof(int32_t) * et.size(), cudaMemcpyHostToDevice, ctx.stream));
-    BEM_CUDA(cudaMemcpyAsync(d_en.p, en.data(), sizeof(int64_t) * en.size(), cudaMemcpyHostToDevice, ctx.stream));
+    // nodes, element types and connectivity staged in one grow-only buffer of
+    // the context (no allocation per problem)
+    const size_t b_nodes = sizeof(double) * m.nodes.size(), b_en = sizeof(int64_t) * en.size(),
+                 b_et = sizeof(int32_t) * et.size();
+    ctx.w_upload.ensure(b_nodes + b_en + b_et + 64);
+    char* up = ctx.w_upload.as<char>();
+    double* d_nodes = reinterpret_cast<double*>(up);
+    int64_t* d_en = reinterpret_cast<int64_t*>(up + b_nodes);
+    int32_t* d_et = reinterpret_cast<int32_t*>(up + b_nodes + b_en);
+    BEM_CUDA(cudaMemcpyAsync(d_nodes, m.nodes.data(), b_nodes, cudaMemcpyHostToDevice, ctx.stream));
+    BEM_CUDA(cudaMemcpyAsync(d_et, et.data(), b_et, cudaMemcpyHostToDevice, ctx.stream));
+    BEM_CUDA(cudaMemcpyAsync(d_en, en.data(), b_en, cudaMemcpyHostToDevice, ctx.stream));
     int threads = 128;
     int blocks = (int)((p.geo.npad + threads - 1) / threads);
-    collocation_kernel<<<blocks, threads, 0, ctx.stream>>>(n, d_nodes.as<double>(), d_et.as<int32_t>(),
-                                                           d_en.as<int64_t>(), p.geo.npad, p.geo.arr(0));
+    collocation_kernel<<<blocks, threads, 0, ctx.stream>>>(n, d_nodes, d_et, d_en, p.geo.npad, p.geo.arr(0));
     BEM_CHECK_LAUNCH(&ctx);
     p.geo.buf32.ensure(sizeof(float) * GEO32_NARR * (size_t)p.geo.npad);
     geometry32_kernel<<<blocks, threads, 0, ctx.stream>>>(p.geo.npad, p.geo.arr(0), p.geo.arr32(0));

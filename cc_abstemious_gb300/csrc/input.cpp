@@ -3,6 +3,9 @@
 // dialect (mesh_data.rs:96-175) and the frequency lists (preprocess.rs:155-167,
 // tools.rs:1-24).  Host C++; no JSON library is available, so a small
 // recursive-descent parser is included.
+#include <charconv>
+#include <cstdio>
+#include <type_traits>
 #include <cctype>
 #include <cmath>
 #include <cstdlib>
@@ -293,69 +296,130 @@ UserInput parse_user_input(const std::string& text) {
 
 // mesh_data.rs:96-175: line-oriented reader; POINTS rows carry 3 coordinates,
 // CELLS rows carry the body id then the node ids, CELL_TYPES one type per row.
+namespace {
+// Line-oriented cursor over a file held in memory.
+struct Lines {
+    const char* p;
+    const char* end;
+    bool next(const char*& b, const char*& e) {
+        if (p >= end) return false;
+        b = p;
+        const char* nl = static_cast<const char*>(std::memchr(p, '\n', (size_t)(end - p)));
+        e = nl ? nl : end;
+        p = nl ? nl + 1 : end;
+        return true;
+    }
+};
+
+inline const char* skip_ws(const char* s, const char* e) {
+    while (s < e && (*s == ' ' || *s == '\t' || *s == '\r')) ++s;
+    return s;
+}
+
+// One number; false at the end of the line or on a non-number.  from_chars
+// is correctly rounded like strtod; a form it rejects (a leading '+') goes
+// through strtod on a bounded copy.
+template <class T>
+inline bool parse_num(const char*& s, const char* e, T& v) {
+    s = skip_ws(s, e);
+    if (s >= e) return false;
+    auto r = std::from_chars(s, e, v);
+    if (r.ec == std::errc() && r.ptr != s) {
+        s = r.ptr;
+        return true;
+    }
+    char buf[64];
+    size_t n = 0;
+    while (s + n < e && n < sizeof(buf) - 1 && s[n] != ' ' && s[n] != '\t' && s[n] != '\r') ++n;
+    std::memcpy(buf, s, n);
+    buf[n] = 0;
+    char* q = nullptr;
+    if constexpr (std::is_floating_point<T>::value) v = (T)std::strtod(buf, &q);
+    else v = (T)std::strtoll(buf, &q, 10);
+    if (q == buf) return false;
+    s += (q - buf);
+    return true;
+}
+
+inline std::string first_word(const char* b, const char* e) {
+    b = skip_ws(b, e);
+    const char* w = b;
+    while (w < e && *w != ' ' && *w != '\t' && *w != '\r') ++w;
+    return std::string(b, w);
+}
+}  // namespace
+
 Mesh read_vtk(const std::string& path) {
-    std::ifstream f(path);
-    require(f.good(), "Mesh file not found at specified path: " + path);
-    Mesh m;
-    std::string line;
-    auto first_word = [](const std::string& l) {
-        std::istringstream is(l);
-        std::string w;
-        is >> w;
-        return w;
+    std::string text;
+    {
+        FILE* fp = std::fopen(path.c_str(), "rb");
+        require(fp != nullptr, "Mesh file not found at specified path: " + path);
+        std::fseek(fp, 0, SEEK_END);
+        const long sz = std::ftell(fp);
+        std::fseek(fp, 0, SEEK_SET);
+        text.resize(sz > 0 ? (size_t)sz : 0);
+        const size_t got = sz > 0 ? std::fread(&text[0], 1, (size_t)sz, fp) : 0;
+        std::fclose(fp);
+        require(got == text.size(), "VTK: cannot read " + path);
+    }
+    // error messages are built only on failure (they would cost an allocation
+    // per number otherwise)
+    auto fail = [](const char* what, const char* lb, const char* le) {
+        throw Error(BEM_ERR_BAD_INPUT, std::string(what) + std::string(lb, le));
     };
-    auto count_after = [&](const std::string& l) -> int64_t {
-        std::istringstream is(l);
-        std::string w;
+    Lines L{text.data(), text.data() + text.size()};
+    Mesh m;
+    const char *b, *e;
+    auto count_after = [&](const char* lb, const char* le) -> int64_t {
+        const char* s = skip_ws(lb, le);
+        while (s < le && *s != ' ' && *s != '\t') ++s;  // the keyword
         long long n = -1;
-        is >> w >> n;
-        require(is && n >= 0, "VTK: bad block header: " + l);
+        if (!parse_num(s, le, n) || n < 0) fail("VTK: bad block header: ", lb, le);
         return (int64_t)n;
     };
-    while (std::getline(f, line)) {
-        std::string w = first_word(line);
+    while (L.next(b, e)) {
+        const std::string w = first_word(b, e);
         if (w == "POINTS") {
-            int64_t n = count_after(line);
+            const int64_t n = count_after(b, e);
             m.nodes.assign((size_t)(3 * n), 0.0);
             for (int64_t i = 0; i < n; ++i) {
-                require((bool)std::getline(f, line), "VTK: unexpected end of POINTS");
-                const char* s = line.c_str();
-                char* e;
+                const char *lb, *le;
+                if (!L.next(lb, le)) fail("VTK: unexpected end of POINTS", b, b);
+                const char* s = lb;
                 for (int c = 0; c < 3; ++c) {
-                    double v = std::strtod(s, &e);
-                    require(e != s, "VTK: bad point row: " + line);
+                    double v;
+                    if (!parse_num(s, le, v)) fail("VTK: bad point row: ", lb, le);
                     m.nodes[(size_t)(3 * i + c)] = v;
-                    s = e;
                 }
             }
         } else if (w == "CELLS") {
-            int64_t n = count_after(line);
+            const int64_t n = count_after(b, e);
             m.body.assign((size_t)n, 0);
             m.etype.assign((size_t)n, 0);
             m.conn_off.assign((size_t)n + 1, 0);
             m.conn.clear();
+            m.conn.reserve((size_t)n * 4);
             for (int64_t i = 0; i < n; ++i) {
-                require((bool)std::getline(f, line), "VTK: unexpected end of CELLS");
-                const char* s = line.c_str();
-                char* e;
-                long long b = std::strtoll(s, &e, 10);
-                require(e != s, "VTK: bad cell row: " + line);
-                m.body[(size_t)i] = b;
-                s = e;
-                for (;;) {
-                    long long v = std::strtoll(s, &e, 10);
-                    if (e == s) break;
-                    m.conn.push_back(v);
-                    s = e;
-                }
+                const char *lb, *le;
+                if (!L.next(lb, le)) fail("VTK: unexpected end of CELLS", b, b);
+                const char* s = lb;
+                long long bv;
+                if (!parse_num(s, le, bv)) fail("VTK: bad cell row: ", lb, le);
+                m.body[(size_t)i] = bv;
+                long long v;
+                while (parse_num(s, le, v)) m.conn.push_back(v);
                 m.conn_off[(size_t)i + 1] = (int64_t)m.conn.size();
             }
         } else if (w == "CELL_TYPES") {
-            int64_t n = count_after(line);
+            const int64_t n = count_after(b, e);
             require(n <= m.nelem(), "VTK: CELL_TYPES longer than CELLS");
             for (int64_t i = 0; i < n; ++i) {
-                require((bool)std::getline(f, line), "VTK: unexpected end of CELL_TYPES");
-                m.etype[(size_t)i] = (int32_t)std::strtol(line.c_str(), nullptr, 10);
+                const char *lb, *le;
+                if (!L.next(lb, le)) fail("VTK: unexpected end of CELL_TYPES", b, b);
+                const char* s = lb;
+                long v = 0;
+                parse_num(s, le, v);
+                m.etype[(size_t)i] = (int32_t)v;
             }
         }
     }
