@@ -366,24 +366,29 @@ class Analysis:
         pd = PreData.from_json(self._input, self._base_dir, ctx)
         self.predata = pd
         nf, nfp = len(pd.frequencies), pd.nfp
-        sc = np.zeros((nf, max(nfp, 1)), dtype=np.complex128)
-        inc = np.zeros((nf, max(nfp, 1)), dtype=np.complex128)
-        reps = (SolveReport * max(nf, 1))()
+        R = int(pd.info["num_rhs"])  # incident_wave + additional_incident_waves
+        sc = np.zeros((R * nf, max(nfp, 1)), dtype=np.complex128)
+        inc = np.zeros((R * nf, max(nfp, 1)), dtype=np.complex128)
+        reps = (SolveReport * max(R * nf, 1))()
         f = {"plain": FORM_PLAIN_FP64, "mixed": FORM_MIXED, "refined": FORM_REFINED}[form]
         pc = {None: PRECOND_NONE, "none": PRECOND_NONE, "block_jacobi": PRECOND_BLOCK_JACOBI,
               "learned": PRECOND_LEARNED, "lu": PRECOND_LU}[precond]
         st = ctx.lib.bem_run(ctx.h, pd.h, f, pc, _ptr(sc), _ptr(inc), reps, 1 if check_vs_lu else 0)
         ctx.check(st)
-        self.results = [FPResult(float(pd.frequencies[i]), sc[i, :nfp].copy(), inc[i, :nfp].copy())
-                        for i in range(nf)]
-        self.reports = [reps[i].as_dict() for i in range(nf)]
+        # per incident wave (wave-major); results / reports are those of the
+        # first wave, as the reference's single incident_wave
+        self.results_by_rhs = [[FPResult(float(pd.frequencies[i]), sc[r * nf + i, :nfp].copy(),
+                                         inc[r * nf + i, :nfp].copy()) for i in range(nf)] for r in range(R)]
+        self.reports_by_rhs = [[reps[r * nf + i].as_dict() for i in range(nf)] for r in range(R)]
+        self.results = self.results_by_rhs[0]
+        self.reports = self.reports_by_rhs[0]
 
     def get_result(self):
         return self.results
 
     def surface_solution(self):
         pd = self.predata
-        nf = len(pd.frequencies)
+        nf = len(pd.frequencies) * int(pd.info["num_rhs"])
         phi = np.zeros((nf, pd.n), dtype=np.complex128)
         vn = np.zeros((nf, pd.n), dtype=np.complex128)
         self.ctx_or_default().check(pd.ctx.lib.bem_last_surface(pd.ctx.h, pd.h, _ptr(phi), _ptr(vn)))

@@ -47,7 +47,7 @@ class ProblemInfo(C.Structure):
                 ("bc_value", C.c_double * 2), ("hm_leaf", C.c_int64), ("hm_eta", C.c_double),
                 ("hm_aca_tol", C.c_double), ("num_eqn", C.c_int64), ("num_field_points", C.c_int64),
                 ("num_frequencies", C.c_int64), ("mesh_elements", C.c_int64), ("mesh_nodes", C.c_int64),
-                ("mesh_bodies", C.c_int64)]
+                ("mesh_bodies", C.c_int64), ("num_rhs", C.c_int64)]
 
 
 _vp, _i64, _d, _i = C.c_void_p, C.c_int64, C.c_double, C.c_int

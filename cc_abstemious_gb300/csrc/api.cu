@@ -300,6 +300,7 @@ BEM_API bem_status bem_problem_get_info(const bem_problem* pp, bem_problem_info*
     o->mesh_elements = p.mesh.nelem();
     o->mesh_nodes = p.mesh.nnodes();
     o->mesh_bodies = p.mesh.nbodies;
+    o->num_rhs = p.nrhs();
     return BEM_OK;
 }
 
@@ -656,7 +657,7 @@ BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* pp, bem_form form, bem_pre
         set_device(c);
         int64_t nf = (int64_t)p.freqs.size();
         if (reports)
-            for (int64_t f = 0; f < nf; ++f) {
+            for (int64_t f = 0; f < nf * p.nrhs(); ++f) {
                 std::memset(&reports[f], 0, sizeof(bem_solve_report));
                 reports[f].rel_err_vs_lu = -1;
             }
@@ -673,13 +674,18 @@ BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* pp, bem_form form, bem_pre
         double2* vn = phi + n;
         double2* inc = vn + n;
         double2* fps = inc + nfp;
-        c.last_phi.assign((size_t)(2 * n * nf), 0.0);
-        c.last_vn.assign((size_t)(2 * n * nf), 0.0);
+        const int64_t nrhs = p.nrhs();
+        c.last_phi.assign((size_t)(2 * n * nf * nrhs), 0.0);
+        c.last_vn.assign((size_t)(2 * n * nf * nrhs), 0.0);
         c.last_n = n;
         c.last_nf = nf;
         int64_t saved = p.ifreq;
-        for (int64_t f = 0; f < nf; ++f) {
-            p.ifreq = f;
+        // one right-hand side after the other, each as the reference would run it
+        for (int64_t r = 0; r < nrhs; ++r)
+        for (int64_t f0 = 0; f0 < nf; ++f0) {
+            p.select_rhs(r);
+            p.ifreq = f0;
+            const int64_t f = r * nf + f0;  // output slot
             auto t0 = std::chrono::steady_clock::now();
             incident_surface(c, p, rhs);
             bem_solve_report* rep = reports ? &reports[f] : nullptr;
@@ -706,6 +712,7 @@ BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* pp, bem_form form, bem_pre
                 if (incident) { incident[f * nfp + i].re = q.x; incident[f * nfp + i].im = q.y; }
             }
         }
+        p.select_rhs(0);
         p.ifreq = saved;
     });
 }

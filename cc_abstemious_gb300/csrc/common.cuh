@@ -55,6 +55,13 @@ struct UserInput {
     int incident_type = 0;
     double incident_vec[3] = {0, 0, 0};
     double incident_amp[2] = {0, 0};
+    // every right-hand side: incident_wave first, then the optional
+    // `additional_incident_waves` (the fields above hold the selected one)
+    struct Wave {
+        int type;
+        double vec[3], amp[2];
+    };
+    std::vector<Wave> waves;
     int bc_type = 1;
     double bc_value[2] = {0, 0};
     int output_total = 0, output_pressure = 1;
@@ -129,6 +136,16 @@ struct Problem {
     DevBuf d_fp32;             // field points as float-float, 6 arrays of nfp_pad
     int64_t nfp_pad = 0;
     int device = 0;
+    int64_t nrhs() const { return in.waves.empty() ? 1 : (int64_t)in.waves.size(); }
+    // makes right-hand side r the problem's incident wave
+    void select_rhs(int64_t r) {
+        if (in.waves.empty()) return;
+        const UserInput::Wave& w = in.waves[(size_t)r];
+        in.incident_type = w.type;
+        for (int k = 0; k < 3; ++k) in.incident_vec[k] = w.vec[k];
+        in.incident_amp[0] = w.amp[0];
+        in.incident_amp[1] = w.amp[1];
+    }
     double frequency() const { return freqs.empty() ? 0.0 : freqs[(size_t)ifreq]; }
     double omega() const { return 2.0 * 3.14159265358979323846 * frequency(); }
     double wavenumber() const { return omega() / in.sound_speed; }

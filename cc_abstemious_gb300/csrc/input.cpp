@@ -258,18 +258,34 @@ UserInput parse_user_input(const std::string& text) {
         }
     }
     {   // IncidentWaveInput (input_data.rs:36-46)
-        auto t = tagged(field(root, "incident_wave"), "incident_wave");
-        require(t.second != nullptr, "incident_wave must be a struct variant");
-        if (t.first == "PlaneWave") {
-            u.incident_type = 0;
-            fixed_array(field(*t.second, "direction"), u.incident_vec, 3, "direction");
-        } else if (t.first == "SphericalWave") {
-            u.incident_type = 1;
-            fixed_array(field(*t.second, "origin"), u.incident_vec, 3, "origin");
-        } else {
-            throw Error(BEM_ERR_BAD_INPUT, "unknown variant `" + t.first + "` for `incident_wave`");
+        auto wave = [](const JValue& v, const char* key) {
+            auto t = tagged(v, key);
+            require(t.second != nullptr, std::string(key) + " must be a struct variant");
+            UserInput::Wave w{};
+            if (t.first == "PlaneWave") {
+                w.type = 0;
+                fixed_array(field(*t.second, "direction"), w.vec, 3, "direction");
+            } else if (t.first == "SphericalWave") {
+                w.type = 1;
+                fixed_array(field(*t.second, "origin"), w.vec, 3, "origin");
+            } else {
+                throw Error(BEM_ERR_BAD_INPUT, "unknown variant `" + t.first + "` for `" + key + "`");
+            }
+            fixed_array(field(*t.second, "amplitude"), w.amp, 2, "amplitude");
+            return w;
+        };
+        u.waves.push_back(wave(field(root, "incident_wave"), "incident_wave"));
+        // extension: further right-hand sides solved with the same operators
+        // (unknown to the reference, whose serde ignores the key)
+        if (const JValue* extra = root.get("additional_incident_waves")) {
+            require(extra->kind == JValue::Array, "additional_incident_waves must be an array");
+            for (const JValue& v : extra->arr) u.waves.push_back(wave(v, "additional_incident_waves"));
         }
-        fixed_array(field(*t.second, "amplitude"), u.incident_amp, 2, "amplitude");
+        const UserInput::Wave& w0 = u.waves[0];
+        u.incident_type = w0.type;
+        for (int k = 0; k < 3; ++k) u.incident_vec[k] = w0.vec[k];
+        u.incident_amp[0] = w0.amp[0];
+        u.incident_amp[1] = w0.amp[1];
     }
     {   // SurfaceBoundaryCondition (input_data.rs:48-59)
         const JValue& bc = field(root, "surface_bc");

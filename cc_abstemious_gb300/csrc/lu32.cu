@@ -723,6 +723,16 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
                                                  c.w_lu_F.as<float2>());
         BEM_CHECK_LAUNCH(&c);
     }
+    // systems sharing an operator (several right-hand sides) share its factors
+    std::vector<int> owner((size_t)nsys);
+    for (int s = 0; s < nsys; ++s) {
+        owner[(size_t)s] = s;
+        for (int o = 0; o < s; ++o)
+            if (owner[(size_t)o] == o && v[(size_t)o].a == v[(size_t)s].a) {
+                owner[(size_t)s] = o;
+                break;
+            }
+    }
     d->sys.resize((size_t)nsys);
     d->maps.ensure(sizeof(CUtensorMap) * 2 * nsys);
     std::vector<CUtensorMap> maps((size_t)(2 * nsys));
@@ -730,6 +740,10 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     size_t od = 0, ow = 0;
     for (int s = 0; s < nsys; ++s) {
         LuSys& L = d->sys[(size_t)s];
+        if (owner[(size_t)s] != s) {
+            L = d->sys[(size_t)owner[(size_t)s]];
+            continue;
+        }
         L.F = c.w_lu_F.as<float2>() + v[(size_t)s].a;
         L.Dm = c.w_lu_D.as<float2>() + od;
         L.W = c.w_lu_W.as<float>() + ow;
@@ -771,7 +785,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         std::vector<std::pair<int, int64_t>> ed, eu, el, eg;
         for (int s = 0; s < nsys; ++s) {
             const LuSys& L = d->sys[(size_t)s];
-            if (L.nblk <= k) continue;
+            if (L.nblk <= k || owner[(size_t)s] != s) continue;  // factored once per operator
             ed.push_back({s, 1});
             const int64_t mt = L.n - (int64_t)(k + 1) * LB;
             if (mt > 0) {

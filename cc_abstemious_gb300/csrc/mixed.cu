@@ -79,24 +79,34 @@ double lu_reference_error(Context& c, const Problem& p, const double* phi_host, 
     return std::sqrt(num / den);
 }
 
-// Frequencies [F0, F0 + nf) of the problem as one batch.
+// out[s] = in[s / R]: the norm of each frequency's operator for its R systems.
+__global__ void repeat_norms_kernel(const double* __restrict__ in, int R, int ns, double* __restrict__ out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < ns) out[s] = in[s / R];
+}
+
+// Frequencies [F0, F0 + nf) of the problem as one batch.  With several
+// right-hand sides (R incident waves) every frequency's operator is assembled
+// once and shared by its R systems (s = f R + r) through the ragged batch
+// layout; the LU preconditioner factors it once.
 static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_precond precond,
                             bem_cplx* scattered, bem_cplx* incident, bem_solve_report* reports, bool check_vs_lu,
                             bool fp64_operator) {
-    const int64_t n = p.n, nfp = p.nfp;
+    const int64_t n = p.n, nfp = p.nfp, R = p.nrhs(), ns = nf * R, NF = (int64_t)p.freqs.size();
     const int64_t ld = p.geo.npad;  // multiple of 64: aligned float4 loads
     const size_t mstride = (size_t)ld * n;
     const int64_t saved_ifreq = p.ifreq;
     auto t_start = std::chrono::steady_clock::now();
 
     // per-frequency factors (influence_matrix.rs:130-162)
-    std::vector<double> ks(nf);
+    std::vector<double> ks(nf), ks_sys(ns);
     std::vector<cd> al(nf), be(nf), ga(nf), de(nf);
     for (int64_t f = 0; f < nf; ++f) {
         p.ifreq = F0 + f;
         ks[f] = p.wavenumber();
         lhs_factors(p, al[f], be[f]);
         rhs_factors(p, ga[f], de[f]);
+        for (int64_t r = 0; r < R; ++r) ks_sys[f * R + r] = ks[f];
     }
     const bool need_rowsum = !(p.in.bc_value[0] == 0.0 && p.in.bc_value[1] == 0.0) && p.in.bc_type != 2;
 
@@ -108,13 +118,14 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
     c.w_mat.ensure((first_kind ? sizeof(double2) : sizeof(float2)) * mstride * nf);
     float2* A32 = c.w_mat.as<float2>();
     double2* A64 = c.w_mat.as<double2>();
-    c.w_vec.ensure(sizeof(double2) * (size_t)nf * (4 * n + 2 * nfp + 2));
+    c.w_vec.ensure(sizeof(double2) * ((size_t)ns * (3 * n + 2 * nfp) + (size_t)nf * n + 2) + sizeof(double) * nf);
     double2* inc = c.w_vec.as<double2>();
-    double2* rowsum = inc + nf * n;
+    double2* rowsum = inc + ns * n;
     double2* phi = rowsum + nf * n;
-    double2* vn = phi + nf * n;
-    double2* finc = vn + nf * n;
-    double2* fps = finc + nf * nfp;
+    double2* vn = phi + ns * n;
+    double2* finc = vn + ns * n;
+    double2* fps = finc + ns * nfp;
+    double* normf = reinterpret_cast<double*>(fps + ns * nfp + 2);
 
     // solver parameters: the problem's GMRES settings, or for the direct
     // solver a tight tolerance (the mixed form always iterates)
@@ -128,8 +139,15 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
     GmWorkspace ws;
     ws.mem_pool = &c.w_gm;
     ws.z_pool = &c.w_gmz;
-    gm_prepare(c, ws, (int)nf, n, m, first_kind ? (const void*)A64 : (const void*)A32, ld, mstride, !first_kind,
-               false);
+    const void* Aop = first_kind ? (const void*)A64 : (const void*)A32;
+    if (R == 1) {
+        gm_prepare(c, ws, (int)nf, n, m, Aop, ld, mstride, !first_kind, false);
+    } else {
+        std::vector<int64_t> nsz((size_t)ns, n), lds((size_t)ns, ld);
+        std::vector<size_t> aoff((size_t)ns);
+        for (int64_t s = 0; s < ns; ++s) aoff[(size_t)s] = (size_t)(s / R) * mstride;
+        gm_prepare_ragged(c, ws, nsz, lds, aoff, m, Aop, !first_kind);
+    }
 
     if (first_kind) {
         EventTimer t(c);
@@ -144,28 +162,33 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
         // the assembly kernel also writes ||A_f||_F for the stopping test
         EventTimer t(c);
         assemble_system_fp32_body(c, p, ks.data(), al.data(), be.data(), ga.data(), de.data(), (int)nf, A32, ld,
-                                  mstride, need_rowsum ? rowsum : nullptr, (size_t)n, ws.anorm);
+                                  mstride, need_rowsum ? rowsum : nullptr, (size_t)n, R == 1 ? ws.anorm : normf);
+        if (R > 1) {
+            repeat_norms_kernel<<<(unsigned)((ns + 127) / 128), 128, 0, c.stream>>>(normf, (int)R, (int)ns, ws.anorm);
+            BEM_CHECK_LAUNCH(&c);
+        }
         t.stop("assemble_fp32", (nf + 15) / 16, 8.0 * (double)n * n * nf);
     }
     {
         EventTimer t(c);
-        for (int64_t f = 0; f < nf; ++f) {
-            p.ifreq = F0 + f;
-            incident_surface(c, p, inc + f * n);
+        for (int64_t s = 0; s < ns; ++s) {
+            p.select_rhs(s % R);
+            p.ifreq = F0 + s / R;
+            incident_surface(c, p, inc + s * n);
         }
-        t.stop("incident", nf, 0);
+        t.stop("incident", ns, 0);
     }
 
-    const double s = p.in.bc_type == 0 ? 1.0 : -1.0;
-    for (int64_t f = 0; f < nf; ++f)
-        launch_rhs_combine(c, n, s, inc + f * n, {p.in.bc_value[0], p.in.bc_value[1]},
-                           need_rowsum ? rowsum + f * n : nullptr, ws.bt.B + f * n);
+    const double sgn = p.in.bc_type == 0 ? 1.0 : -1.0;
+    for (int64_t s = 0; s < ns; ++s)
+        launch_rhs_combine(c, n, sgn, inc + s * n, {p.in.bc_value[0], p.in.bc_value[1]},
+                           need_rowsum ? rowsum + (s / R) * n : nullptr, ws.bt.B + s * n);
     std::vector<GmState> st;
     {
         EventTimer t(c);
         gm_init(c, ws, tol, restarts);
         if (precond != BEM_PRECOND_NONE)
-            precond = precond_setup(c, p, ws, precond, ks.data());
+            precond = precond_setup(c, p, ws, precond, ks_sys.data());
         gm_run(c, ws, c.profiling ? 0 : 4, restarts * (int64_t)m + 1);
         gm_read_states(c, ws, st);
         int64_t mv = 0;
@@ -174,57 +197,64 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
     }
     {
         EventTimer t(c);
-        for (int64_t f = 0; f < nf; ++f) {
-            p.ifreq = F0 + f;
-            unpack_solution(c, p, ws.bt.X + f * n, phi + f * n, vn + f * n);
-            incident_field(c, p, finc + f * nfp);
+        for (int64_t s = 0; s < ns; ++s) {
+            p.select_rhs(s % R);
+            p.ifreq = F0 + s / R;
+            unpack_solution(c, p, ws.bt.X + s * n, phi + s * n, vn + s * n);
+            incident_field(c, p, finc + s * nfp);
         }
-        evaluate_field32_batch(c, p, ks.data(), (int)nf, phi, vn, n, p.in.output_total ? finc : nullptr, fps);
+        evaluate_field32_batch(c, p, ks_sys.data(), (int)ns, phi, vn, n, p.in.output_total ? finc : nullptr, fps);
         t.stop("field", 1, 0);
     }
-    std::vector<double2> hs((size_t)(nf * nfp)), hi((size_t)(nf * nfp));
+    std::vector<double2> hs((size_t)(ns * nfp)), hi((size_t)(ns * nfp));
     if (nfp) {
-        BEM_CUDA(cudaMemcpyAsync(hs.data(), fps, sizeof(double2) * nf * nfp, cudaMemcpyDeviceToHost, c.stream));
-        BEM_CUDA(cudaMemcpyAsync(hi.data(), finc, sizeof(double2) * nf * nfp, cudaMemcpyDeviceToHost, c.stream));
+        BEM_CUDA(cudaMemcpyAsync(hs.data(), fps, sizeof(double2) * ns * nfp, cudaMemcpyDeviceToHost, c.stream));
+        BEM_CUDA(cudaMemcpyAsync(hi.data(), finc, sizeof(double2) * ns * nfp, cudaMemcpyDeviceToHost, c.stream));
     }
-    BEM_CUDA(cudaMemcpyAsync(c.last_phi.data() + 2 * n * F0, phi, sizeof(double2) * nf * n, cudaMemcpyDeviceToHost,
-                             c.stream));
-    BEM_CUDA(cudaMemcpyAsync(c.last_vn.data() + 2 * n * F0, vn, sizeof(double2) * nf * n, cudaMemcpyDeviceToHost,
-                             c.stream));
+    // output slot of system s: wave-major, then frequency
+    auto slot = [&](int64_t s) { return (s % R) * NF + F0 + s / R; };
+    for (int64_t s = 0; s < ns; ++s) {
+        BEM_CUDA(cudaMemcpyAsync(c.last_phi.data() + 2 * n * slot(s), phi + s * n, sizeof(double2) * n,
+                                 cudaMemcpyDeviceToHost, c.stream));
+        BEM_CUDA(cudaMemcpyAsync(c.last_vn.data() + 2 * n * slot(s), vn + s * n, sizeof(double2) * n,
+                                 cudaMemcpyDeviceToHost, c.stream));
+    }
     c.sync();
     double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-    for (int64_t f = 0; f < nf; ++f) {
-        p.ifreq = F0 + f;
+    for (int64_t s = 0; s < ns; ++s) {
+        p.ifreq = F0 + s / R;
         double w = p.in.output_pressure ? p.omega() * p.in.mass_density : 0.0;
         for (int64_t i = 0; i < nfp; ++i) {
-            double2 a = hs[(size_t)(f * nfp + i)], q = hi[(size_t)(f * nfp + i)];
+            double2 a = hs[(size_t)(s * nfp + i)], q = hi[(size_t)(s * nfp + i)];
             if (p.in.output_pressure) {
                 a = make_double2(-a.y * w, a.x * w);
                 q = make_double2(-q.y * w, q.x * w);
             }
-            const int64_t o = (F0 + f) * nfp + i;
+            const int64_t o = slot(s) * nfp + i;
             if (scattered) { scattered[o].re = a.x; scattered[o].im = a.y; }
             if (incident) { incident[o].re = q.x; incident[o].im = q.y; }
         }
         if (reports) {
-            bem_solve_report& r = reports[F0 + f];
-            r.num_mv = st[(size_t)f].num_mv;
-            r.restarts = st[(size_t)f].restarts + (st[(size_t)f].converged ? 1 : 0);
-            r.iterations = st[(size_t)f].iterations;
-            r.backward_error = st[(size_t)f].error;
-            r.flag = st[(size_t)f].converged ? 1 : 2;
+            bem_solve_report& r = reports[slot(s)];
+            r.num_mv = st[(size_t)s].num_mv;
+            r.restarts = st[(size_t)s].restarts + (st[(size_t)s].converged ? 1 : 0);
+            r.iterations = st[(size_t)s].iterations;
+            r.backward_error = st[(size_t)s].error;
+            r.flag = st[(size_t)s].converged ? 1 : 2;
             r.precond = (int32_t)precond;
-            r.seconds = secs / (double)nf;
+            r.seconds = secs / (double)ns;
             r.rel_err_vs_lu = -1;
         }
     }
     if (check_vs_lu && reports) {
-        for (int64_t f = F0; f < F0 + nf; ++f) {
-            p.ifreq = f;
-            reports[f].rel_err_vs_lu =
-                lu_reference_error(c, p, c.last_phi.data() + 2 * n * f, c.last_vn.data() + 2 * n * f);
+        for (int64_t s = 0; s < ns; ++s) {
+            p.select_rhs(s % R);
+            p.ifreq = F0 + s / R;
+            reports[slot(s)].rel_err_vs_lu = lu_reference_error(c, p, c.last_phi.data() + 2 * n * slot(s),
+                                                                c.last_vn.data() + 2 * n * slot(s));
         }
     }
+    p.select_rhs(0);
     p.ifreq = saved_ifreq;
 }
 
@@ -233,8 +263,8 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     c.stages.clear();
     const int64_t nf = (int64_t)p.freqs.size(), n = p.n;
     require(nf >= 1, "no frequencies");
-    c.last_phi.assign((size_t)(2 * n * nf), 0.0);
-    c.last_vn.assign((size_t)(2 * n * nf), 0.0);
+    c.last_phi.assign((size_t)(2 * n * nf * p.nrhs()), 0.0);
+    c.last_vn.assign((size_t)(2 * n * nf * p.nrhs()), 0.0);
     c.last_n = n;
     c.last_nf = nf;
     // frequencies per batch: the operators (and the LU copy) within 60% of the

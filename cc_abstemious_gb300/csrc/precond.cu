@@ -695,7 +695,7 @@ bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond k
     build_pattern(p, h->data.pat, kind != BEM_PRECOND_LEARNED);
     upload_pattern(c, h->data);
     const int nsys = ws.bt.nsys;
-    diag_inverses(c, h->data, nsys, ws.bt.A, ws.fp32, ws.bt.lda, ws.bt.mat_stride);
+    diag_inverses(c, h->data, nsys, ws.bt.A, ws.fp32, ws.bt.lda, ws.bt.mat_stride, ws.bt.sys);
     h->use_off = false;
     if (kind == BEM_PRECOND_LEARNED) {
         PairBufs pb;

@@ -122,6 +122,7 @@ typedef struct {
     int64_t mesh_elements;
     int64_t mesh_nodes;
     int64_t mesh_bodies;
+    int64_t num_rhs;         /* incident_wave + the extension key additional_incident_waves */
 } bem_problem_info;
 
 /* ---- context ---------------------------------------------------------- */
@@ -226,11 +227,15 @@ BEM_API bem_status bem_convert_to_pressure(const bem_problem* p, double frequenc
 
 /* ---- driver (analysis.rs:57-118) --------------------------------------- */
 /* Runs every frequency of the problem.  scattered and incident are
- * (num_frequencies x nfp) row-major host arrays (field point fastest) and
+ * (num_rhs x num_frequencies x nfp) row-major host arrays (field point
+ * fastest; num_rhs = 1 unless the input lists additional_incident_waves, in
+ * which case every wave is solved with the same operators: the mixed and
+ * refined forms assemble and factor each frequency once) and
  * receive the pressure (or velocity potential) as postprocess.rs:70-79
  * leaves them.  reports: num_frequencies entries or NULL.  With
  * check_vs_lu != 0 each report carries its error against an FP64 LU solve of
  * the same operator (costly; outside any timed region). */
+/* reports: num_rhs x num_frequencies entries (wave-major) or NULL. */
 BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* p, bem_form form, bem_precond precond,
                            bem_cplx* scattered, bem_cplx* incident, bem_solve_report* reports,
                            int check_vs_lu);
@@ -242,12 +247,14 @@ BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* p, bem_form form, bem_prec
  * arrays, or any entry, may be NULL).  max_operator_bytes bounds the operators
  * held at once (bodies are grouped into chunks; 0: a share of the free device
  * memory).  Bodies with a classical formulation and a pressure condition keep
- * an FP64 operator and run one by one as in bem_run. */
+ * an FP64 operator and run one by one as in bem_run.  Only the first incident
+ * wave of each body is solved (additional_incident_waves: bem_run). */
 BEM_API bem_status bem_run_batch(bem_ctx* ctx, bem_problem* const* problems, int nprob, bem_precond precond,
                                  bem_cplx* const* scattered, bem_cplx* const* incident,
                                  bem_solve_report* const* reports, int check_vs_lu,
                                  int64_t max_operator_bytes);
-/* Surface solutions of the last bem_run (n per frequency, frequency-major). */
+/* Surface solutions of the last bem_run (n per system; wave-major, then
+ * frequency: num_rhs x num_frequencies x n). */
 BEM_API bem_status bem_last_surface(bem_ctx* ctx, const bem_problem* p, bem_cplx* phi, bem_cplx* vn);
 
 /* ---- learned preconditioner (no counterpart in the reference) ------------ */
