@@ -336,6 +336,12 @@ __global__ void finish_norm_kernel(const double* __restrict__ part, int64_t npar
     if (threadIdx.x == 0) out[s] = sqrt(sh[0]);
 }
 
+// out[s] = sqrt(sum of the nparts partials of system s).
+void finish_norms(Context& ctx, const double* part, int64_t nparts, int nsys, double* out) {
+    finish_norm_kernel<<<nsys, 256, 0, ctx.stream>>>(part, nparts, out);
+    BEM_CHECK_LAUNCH(&ctx);
+}
+
 void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks, const cd* alphas, const cd* betas,
                                const cd* gammas, const cd* deltas, int nsys, float2* A, int64_t ld, size_t mat_stride,
                                double2* rowsum, size_t vec_stride, double* norms) {

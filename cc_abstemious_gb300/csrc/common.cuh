@@ -217,6 +217,12 @@ void assemble_surface_fp64(Context& ctx, const Problem& p, double2* H, double2* 
 // A = alpha H + beta G and rowsum(gamma H + delta G) partials (fused solve path)
 void assemble_system_fp64(Context& ctx, const Problem& p, double2* A, int64_t ld, cd alpha, cd beta,
                           cd gamma, cd delta, double2* rowsum /* n, may be null */);
+// A_s = alpha_s H_s + beta_s G_s in FP64 for several frequencies (refined
+// form): geometry once per pair, e^{ik r} by recurrence when the wavenumbers
+// are evenly spaced; norms[s] = ||A_s||_F.
+void assemble_system_fp64_multi(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
+                                const cd* betas, int nsys, double2* A, int64_t ld, size_t mat_stride,
+                                double* norms);
 void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
                                const cd* betas, const cd* gammas, const cd* deltas, int nsys, float2* A,
                                int64_t ld, size_t mat_stride, double2* rowsum, size_t vec_stride, double* norms);

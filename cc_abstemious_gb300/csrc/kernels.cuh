@@ -23,6 +23,7 @@ __device__ __forceinline__ void self_term64(double area, double wt, int bm, doub
 }
 
 int* device_err(Context& ctx);
+void finish_norms(Context& ctx, const double* part, int64_t nparts, int nsys, double* out);
 void check_device_err(Context& ctx);
 void launch_reduce_parts(Context& ctx, int64_t n, int64_t npad, int ntiles, const double2* part, double2* out);
 
