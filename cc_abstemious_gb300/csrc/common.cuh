@@ -184,7 +184,7 @@ struct Context {
     // batched GMRES workspace and Krylov-preconditioned basis, LU factors,
     // diagonal-block inverses and panel workspace (grow-only, reused by
     // every mixed solve)
-    DevBuf w_gm, w_gmz, w_lu_F, w_lu_D, w_lu_W;
+    DevBuf w_gm, w_gmz, w_lu_F, w_lu_D, w_lu_W, w_lu_P;
     DevBuf w_upload;  // mesh staging of problem construction
     // results of the last bem_run
     std::vector<double> last_phi, last_vn;

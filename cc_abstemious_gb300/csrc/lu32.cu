@@ -6,10 +6,14 @@
 //
 //   diag   one CTA per system: A11 = L11 U11 in shared memory (tiny pivots are
 //          replaced and counted), then L11^-1 and U11^-1 in place; the two
-//          inverses are kept per block (strict lower / upper of one tile).
-//   u12    U12 = L11^-1 A12 (row panel), CUDA cores.
-//   l21    L21 = A21 U11^-1 (column panel), CUDA cores; also writes L21 in
-//          the real embedding below, row-major, for the tensor cores.
+//          inverses are kept per block (strict lower / upper of one tile) and
+//          written in the real embedding below for the panel GEMMs.
+//   l21    the column panel A21 is embedded (memory-bound copy), then
+//          L21 = A21 U11^-1 on the tensor cores, in place (the embedding is a
+//          ring homomorphism: emb(A U) = emb(A) emb(U)); the GEMM's epilogue
+//          also writes L21 in natural form into the factors.
+//   u12    U12 = L11^-1 A12 on the tensor cores into a side buffer (the
+//          trailing update's second operand), copied into the factors after.
 //   gemm   A22 -= L21 U12 on the tensor cores (tcgen05, kind::tf32, FP32
 //          accumulation in tensor memory).  The complex product is one real
 //          GEMM: with A' the 2m x 2k real matrix holding [[ar, -ai], [ai, ar]]
@@ -61,9 +65,15 @@ constexpr uint32_t G_TMEM_COLS = 512;           // two accumulators of GN column
 struct LuSys {
     float2* F;    // factors (copy of the operator), column-major, leading dimension ld
     float2* Dm;   // per block: L11^-1 (strict lower) and U11^-1 (upper), LB x LB column-major
-    float* W;     // real embedding of the current step's L21: 2n rows x 2 LB floats, row-major
-    const CUtensorMap* tmW;  // W as 2n rows x 256 floats, 128-byte swizzled 32 x 128 boxes
+    float* W;     // real embedding of the current step's A21, then L21: 2n rows x 2 LB floats, row-major
+    float* Li;    // real embedding of L11^-1: 2 LB x 2 LB, row-major
+    float* UiT;   // transposed real embedding of U11^-1: 2 LB x 2 LB, row-major
+    float* Y;     // U12 of the current step, natural real view: column j at Y + 2 LB j
+    const CUtensorMap* tmW;  // W: 2n rows x 256 floats, 128-byte swizzled 32 x 128 boxes
     const CUtensorMap* tmF;  // F's natural real view: n columns x 2n floats, 32 x 256 boxes
+    const CUtensorMap* tmY;  // Y: n columns x 256 floats, 32 x 256 boxes
+    const CUtensorMap* tmL;  // Li: 256 rows, 32 x 128 boxes
+    const CUtensorMap* tmU;  // UiT: 256 rows, 32 x 256 boxes
     int64_t n, ld;
     int nblk, pad;
 };
@@ -186,112 +196,59 @@ __global__ void __launch_bounds__(1024) lu_diag_kernel(const LuSys* __restrict__
     float2* Dk = S.Dm + (size_t)k * LB * LB;
     for (int c = ty; c < nb; c += 32)
         for (int r = tx; r < nb; r += 32) Dk[c * LB + r] = T[c * LB + r];
-}
-
-// U12 = L11^-1 A12 for 64 columns per CTA.
-__global__ void __launch_bounds__(256) lu_u12_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
-                                                     int nw, int k) {
-    extern __shared__ float2 sm[];
-    float2* Lf = sm;            // LB x LB column-major, unit diagonal, zero above
-    float2* X = sm + LB * LB;   // LB x 64 column-major
-    int64_t tile;
-    const LuSys S = sys[lu_locate(wl, nw, blockIdx.x, tile)];
-    const int64_t k0 = (int64_t)k * LB, j0 = k0 + LB + 64 * tile;
-    const int ncol = (int)min((int64_t)64, S.n - j0);
-    const float2* Dk = S.Dm + (size_t)k * LB * LB;
+    if (nb < LB || S.n <= k0 + LB) return;  // no panels after the last block
+    // real embeddings for the panel GEMMs: Li = [[re, -im], [im, re]] of
+    // L11^-1 (unit lower), UiT = the transpose of that of U11^-1 (upper)
+    float2* Li2 = reinterpret_cast<float2*>(S.Li);
+    float2* Ui2 = reinterpret_cast<float2*>(S.UiT);
     for (int t = threadIdx.x; t < LB * LB; t += blockDim.x) {
-        const int c = t / LB, r = t % LB;
-        Lf[t] = r > c ? Dk[t] : make_float2(r == c ? 1.f : 0.f, 0.f);
-    }
-    for (int t = threadIdx.x; t < 64 * LB; t += blockDim.x) {
-        const int c = t / LB, r = t % LB;
-        X[t] = c < ncol ? S.F[(j0 + c) * S.ld + k0 + r] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;  // rows tr + 32q, columns tc * 8 + c
-    float2 acc[4][8];
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-#pragma unroll
-        for (int c = 0; c < 8; ++c) acc[q][c] = make_float2(0.f, 0.f);
-    for (int p = 0; p < LB; ++p) {
-        float2 a[4], b[8];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) a[q] = Lf[p * LB + tr + 32 * q];
-#pragma unroll
-        for (int c = 0; c < 8; ++c) b[c] = X[(tc * 8 + c) * LB + p];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-            for (int c = 0; c < 8; ++c) cfmaf_(acc[q][c], a[q], b[c]);
-    }
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        const int col = tc * 8 + c;
-        if (col >= ncol) continue;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) S.F[(j0 + col) * S.ld + k0 + tr + 32 * q] = acc[q][c];
+        const int i = t % LB, p = t / LB;  // Li: element (i, p), consecutive threads down a column of T
+        const float2 l = p < i ? T[p * LB + i] : make_float2(p == i ? 1.f : 0.f, 0.f);
+        Li2[(2 * i) * LB + p] = make_float2(l.x, -l.y);
+        Li2[(2 * i + 1) * LB + p] = make_float2(l.y, l.x);
+        const int pu = t % LB, q = t / LB;  // UiT rows 2q, 2q + 1 from U11^-1 (pu, q)
+        const float2 u = pu <= q ? T[q * LB + pu] : make_float2(0.f, 0.f);
+        Ui2[(2 * q) * LB + pu] = make_float2(u.x, u.y);
+        Ui2[(2 * q + 1) * LB + pu] = make_float2(-u.y, u.x);
     }
 }
 
-// L21 = A21 U11^-1 for 64 rows per CTA; natural form back into F and the
-// real embedding into W.
-__global__ void __launch_bounds__(256) lu_l21_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
-                                                     int nw, int k) {
-    extern __shared__ float2 sm[];
-    float2* Uf = sm;            // LB x LB column-major, zero below the diagonal
-    float2* Y = sm + LB * LB;   // 64 x LB: Y[p * 64 + i], reused for the output (row-major R[i * LB + c])
+// W <- real embedding of the column panel A21 (64 rows per CTA): rows 2i and
+// 2i + 1 of W hold [ar, -ai] and [ai, ar] for every column of A21's row i.
+__global__ void __launch_bounds__(256) lu_expand_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
+                                                        int nw, int k) {
+    extern __shared__ float2 Y[];  // 64 x LB: Y[p * 64 + i]
     int64_t tile;
     const LuSys S = sys[lu_locate(wl, nw, blockIdx.x, tile)];
     const int64_t k0 = (int64_t)k * LB, kt = k0 + LB, i0 = kt + 64 * tile;
     const int nrow = (int)min((int64_t)64, S.n - i0);
-    const float2* Dk = S.Dm + (size_t)k * LB * LB;
-    for (int t = threadIdx.x; t < LB * LB; t += blockDim.x) {
-        const int c = t / LB, r = t % LB;
-        Uf[t] = r <= c ? Dk[t] : make_float2(0.f, 0.f);
-    }
     for (int t = threadIdx.x; t < 64 * LB; t += blockDim.x) {
         const int p = t / 64, i = t % 64;
         Y[t] = i < nrow ? S.F[(k0 + p) * S.ld + i0 + i] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;  // rows tr + 32q, columns tc * 16 + c
-    float2 acc[2][16];
-#pragma unroll
-    for (int q = 0; q < 2; ++q)
-#pragma unroll
-        for (int c = 0; c < 16; ++c) acc[q][c] = make_float2(0.f, 0.f);
-    for (int p = 0; p < LB; ++p) {
-        const float2 a0 = Y[p * 64 + tr], a1 = Y[p * 64 + tr + 32];
-#pragma unroll
-        for (int c = 0; c < 16; ++c) {
-            const float2 b = Uf[(tc * 16 + c) * LB + p];
-            cfmaf_(acc[0][c], a0, b);
-            cfmaf_(acc[1][c], a1, b);
-        }
-    }
-    __syncthreads();  // Y is reused below
-    float2* R = Y;
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const int i = tr + 32 * q;
-#pragma unroll
-        for (int c = 0; c < 16; ++c) {
-            const int col = tc * 16 + c;
-            R[i * LB + col] = acc[q][c];
-            if (i < nrow) S.F[(k0 + col) * S.ld + i0 + i] = acc[q][c];
-        }
-    }
-    __syncthreads();
-    // real embedding: rows 2i and 2i + 1 of W (relative to the trailing block)
     const int64_t wr0 = 2 * (i0 - kt);
     for (int t = threadIdx.x; t < nrow * LB; t += blockDim.x) {
         const int i = t / LB, c = t % LB;
-        const float2 v = R[i * LB + c];
+        const float2 v = Y[c * 64 + i];
         float2* w0 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i) * (2 * LB));
         float2* w1 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i + 1) * (2 * LB));
         w0[c] = make_float2(v.x, -v.y);
         w1[c] = make_float2(v.y, v.x);
+    }
+}
+
+// F's row panel (rows k0 .. k0 + LB of every column j >= kt) <- Y (32 columns per CTA).
+__global__ void __launch_bounds__(256) lu_copy_u12_kernel(const LuSys* __restrict__ sys,
+                                                          const LuWork* __restrict__ wl, int nw, int k) {
+    int64_t tile;
+    const LuSys S = sys[lu_locate(wl, nw, blockIdx.x, tile)];
+    const int64_t k0 = (int64_t)k * LB, kt = k0 + LB, j0 = kt + 32 * tile;
+    const int ncol = (int)min((int64_t)32, S.n - j0);
+    for (int t = threadIdx.x; t < ncol * (LB / 2); t += blockDim.x) {
+        const int c = t / (LB / 2), q = t % (LB / 2);  // 64 float4 per column
+        const float4 v = reinterpret_cast<const float4*>(S.Y + (j0 + c) * (2 * LB))[q];
+        reinterpret_cast<float4*>(S.F + (j0 + c) * S.ld + k0)[q] = v;
     }
 }
 
@@ -341,31 +298,71 @@ __host__ __device__ constexpr uint32_t umma_idesc_tf32_f32(int M, int N) {
 // the MMAs of a stage and releases it through tcgen05.commit on its "empty"
 // barrier, and warps 2-9 drain the accumulator of the previous tile (two
 // accumulators of 256 tensor-memory columns) while the next tile's MMAs run.
+// GEMM modes of one block step (all D = A' B over K = 2 LB real):
+//   TRAIL  A22 -= W Y        tiles of 128 rows of W x 256 columns of Y
+//   U12    Y = Li U12raw     the two 128-row halves of Li x 256 columns of F's row panel
+//   L21    W = W UiT^T       128 rows of W x all 256 columns, in place; F's column panel
+//                            receives L21 in natural form
+enum { G_TRAIL = 0, G_U12 = 1, G_L21 = 2 };
+
 struct GemmTile {
-    const CUtensorMap *tmW, *tmF;
-    float* F;
-    int64_t n, rows, ld2, k0, kt, row0, col0;
+    const CUtensorMap *tmA, *tmB;
+    int ax, ay, bx, by;  // tensor-copy coordinates of chunk 0 (x advances by GK per chunk)
+    float *F, *Y, *W;
+    int64_t n, rows, ld, ld2, k0, kt, row0, col0;
 };
 
+template <int MODE>
 __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl, int nw,
                                               int k, int64_t t) {
     int64_t local;
     const LuSys S = sys[lu_locate(wl, nw, t, local)];
     GemmTile g;
-    g.tmW = S.tmW;
-    g.tmF = S.tmF;
     g.F = reinterpret_cast<float*>(S.F);
+    g.Y = S.Y;
+    g.W = S.W;
     g.n = S.n;
+    g.ld = S.ld;
     g.k0 = (int64_t)k * LB;
     g.kt = g.k0 + LB;
-    g.rows = 2 * (S.n - g.kt);
     g.ld2 = 2 * S.ld;
-    const int64_t tiles_i = (g.rows + GM - 1) / GM;
-    g.row0 = (local % tiles_i) * GM;
-    g.col0 = g.kt + (local / tiles_i) * GN;
+    const int64_t mt = S.n - g.kt;
+    if (MODE == G_TRAIL) {
+        g.rows = 2 * mt;
+        const int64_t tiles_i = (g.rows + GM - 1) / GM;
+        g.row0 = (local % tiles_i) * GM;
+        g.col0 = g.kt + (local / tiles_i) * GN;
+        g.tmA = S.tmW;
+        g.ax = 0;
+        g.ay = (int)g.row0;
+        g.tmB = S.tmY;
+        g.bx = 0;
+        g.by = (int)g.col0;
+    } else if (MODE == G_U12) {
+        g.rows = 2 * LB;
+        g.row0 = (local & 1) * GM;
+        g.col0 = g.kt + (local >> 1) * GN;
+        g.tmA = S.tmL;
+        g.ax = 0;
+        g.ay = (int)g.row0;
+        g.tmB = S.tmF;
+        g.bx = (int)(2 * g.k0);
+        g.by = (int)g.col0;
+    } else {
+        g.rows = 2 * mt;
+        g.row0 = local * GM;
+        g.col0 = 0;
+        g.tmA = S.tmW;
+        g.ax = 0;
+        g.ay = (int)g.row0;
+        g.tmB = S.tmU;
+        g.bx = 0;
+        g.by = 0;
+    }
     return g;
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __restrict__ sys,
                                                               const LuWork* __restrict__ wl, int nw, int k,
                                                               int64_t ntiles, int* __restrict__ err) {
@@ -407,7 +404,7 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
         if (lane == 0) {
             int64_t it = 0;
             for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
-                const GemmTile g = gemm_tile(sys, wl, nw, k, t);
+                const GemmTile g = gemm_tile<MODE>(sys, wl, nw, k, t);
                 for (int c = 0; c < GCHUNKS; ++c, ++it) {
                     const int st = (int)(it % GS);
                     const int64_t round = it / GS;
@@ -417,8 +414,8 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                     }
                     const uint32_t As = base + st * GSTAGE, Bs = As + GA_BYTES;
                     mbar_arrive_expect_tx(&full[st], GSTAGE);
-                    tma_load_2d(As, g.tmW, c * GK, (int)g.row0, &full[st]);
-                    tma_load_2d(Bs, g.tmF, (int)(2 * g.k0) + c * GK, (int)g.col0, &full[st]);
+                    tma_load_2d(As, g.tmA, g.ax + c * GK, g.ay, &full[st]);
+                    tma_load_2d(Bs, g.tmB, g.bx + c * GK, g.by, &full[st]);
                 }
             }
             if (*abort_flag) {
@@ -474,24 +471,49 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                 break;
             }
             tc_fence_after();
-            const GemmTile g = gemm_tile(sys, wl, nw, k, t);
+            const GemmTile g = gemm_tile<MODE>(sys, wl, nw, k, t);
             const int64_t r = g.row0 + 32 * quarter + lane;
             const bool rok = r < g.rows;
             for (int cc = half * (GN / 64); cc < (half + 1) * (GN / 64); ++cc) {
                 const int64_t jb = g.col0 + cc * 32;
-                if (jb >= g.n) break;  // uniform over the warp
+                if (MODE != G_L21 && jb >= g.n) break;  // uniform over the warp
                 float v[32];
                 tmem_ld32(tmem + lane_base + (uint32_t)(acc * GN + cc * 32), v);
-                if (!rok) continue;
-                // all 32 loads in flight before the first store
-                const int nq = (int)min((int64_t)32, g.n - jb);
-                float* p0 = g.F + jb * g.ld2 + 2 * g.kt + r;
-                float cv[32];
+                if (MODE == G_TRAIL) {
+                    if (!rok) continue;
+                    // all 32 loads in flight before the first store
+                    const int nq = (int)min((int64_t)32, g.n - jb);
+                    float* p0 = g.F + jb * g.ld2 + 2 * g.kt + r;
+                    float cv[32];
 #pragma unroll
-                for (int q = 0; q < 32; ++q) cv[q] = q < nq ? __ldcg(p0 + q * g.ld2) : 0.f;
+                    for (int q = 0; q < 32; ++q) cv[q] = q < nq ? __ldcg(p0 + q * g.ld2) : 0.f;
 #pragma unroll
-                for (int q = 0; q < 32; ++q)
-                    if (q < nq) p0[q * g.ld2] = cv[q] - v[q];
+                    for (int q = 0; q < 32; ++q)
+                        if (q < nq) p0[q * g.ld2] = cv[q] - v[q];
+                } else if (MODE == G_U12) {
+                    const int nq = (int)min((int64_t)32, g.n - jb);
+                    float* p0 = g.Y + jb * (2 * LB) + r;
+#pragma unroll
+                    for (int q = 0; q < 32; ++q)
+                        if (q < nq) p0[q * (2 * LB)] = v[q];
+                } else {
+                    // L21: the embedded row back into W, and the natural
+                    // entries (row 2i holds re, row 2i + 1 im of column 2p)
+                    float im[16];
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) im[q] = __shfl_down_sync(0xffffffffu, v[2 * q], 1);
+                    if (!rok) continue;
+                    float4* wrow = reinterpret_cast<float4*>(g.W + r * (2 * LB) + cc * 32);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) wrow[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                    if ((lane & 1) == 0) {
+                        const int64_t i = g.kt + (r >> 1);
+                        float2* F2 = reinterpret_cast<float2*>(g.F);
+#pragma unroll
+                        for (int q = 0; q < 16; ++q)
+                            F2[(g.k0 + cc * 16 + q) * g.ld + i] = make_float2(v[2 * q], im[q]);
+                    }
+                }
             }
             tc_fence_before();
             mbar_arrive(&tempty[acc]);
@@ -629,7 +651,7 @@ struct LuData {
         int count = 0;
         int64_t ctas = 0;
     };
-    std::vector<Seg> diag, u12, l21, gemm, fwd, bwd;
+    std::vector<Seg> diag, expand, u12, l21, gemm, copy, fwd, bwd;
     std::vector<LuWork> host;
     int small_pivots = 0;
 };
@@ -694,7 +716,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     auto d = std::make_shared<LuData>();
     const int nsys = ws.bt.nsys;
     std::vector<GmView> v((size_t)nsys);
-    size_t entries = 0, dm = 0, wsz = 0;
+    size_t entries = 0, dm = 0, wsz = 0, psz = 0;
     for (int s = 0; s < nsys; ++s) {
         v[(size_t)s] = ws.sys_host.empty() ? gm_view(ws.bt, s) : GmView{};
         if (!ws.sys_host.empty()) {
@@ -707,6 +729,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         const int nb = (int)((v[(size_t)s].n + LB - 1) / LB);
         dm += (size_t)nb * LB * LB;
         wsz += (size_t)2 * v[(size_t)s].n * 2 * LB;
+        psz += (size_t)2 * (2 * LB) * (2 * LB) + (size_t)(2 * LB) * v[(size_t)s].n;
         d->nblk_max = std::max(d->nblk_max, nb);
     }
     // the factors, block inverses and panel workspace live in grow-only
@@ -714,6 +737,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     c.w_lu_F.ensure(sizeof(float2) * entries);
     c.w_lu_D.ensure(sizeof(float2) * std::max<size_t>(dm, 1));
     c.w_lu_W.ensure(sizeof(float) * std::max<size_t>(wsz, 4));
+    c.w_lu_P.ensure(sizeof(float) * std::max<size_t>(psz, 4));
     if (ws.fp32) {
         BEM_CUDA(cudaMemcpyAsync(c.w_lu_F.p, ws.bt.A, sizeof(float2) * entries, cudaMemcpyDeviceToDevice, c.stream));
     } else {
@@ -734,10 +758,23 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
             }
     }
     d->sys.resize((size_t)nsys);
-    d->maps.ensure(sizeof(CUtensorMap) * 2 * nsys);
-    std::vector<CUtensorMap> maps((size_t)(2 * nsys));
+    constexpr int NMAP = 5;
+    d->maps.ensure(sizeof(CUtensorMap) * NMAP * nsys);
+    std::vector<CUtensorMap> maps((size_t)(NMAP * nsys));
     const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
-    size_t od = 0, ow = 0;
+    // a 2-D FP32 tensor map with 128-byte swizzled boxes of 32 floats x rows
+    auto map2d = [&](CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint64_t stride_floats,
+                     uint32_t box_rows, const char* what) {
+        const cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+        const cuuint64_t strides[1] = {(cuuint64_t)(stride_floats * sizeof(float))};
+        const cuuint32_t box[2] = {(cuuint32_t)GK, (cuuint32_t)box_rows};
+        const cuuint32_t es[2] = {1, 1};
+        const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box,
+                                  es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        require(r == CUDA_SUCCESS, std::string("LU: tensor map of ") + what);
+    };
+    size_t od = 0, ow = 0, op = 0;
     for (int s = 0; s < nsys; ++s) {
         LuSys& L = d->sys[(size_t)s];
         if (owner[(size_t)s] != s) {
@@ -750,54 +787,49 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         L.n = v[(size_t)s].n;
         L.ld = v[(size_t)s].lda;
         L.nblk = (int)((L.n + LB - 1) / LB);
+        L.Li = c.w_lu_P.as<float>() + op;
+        L.UiT = L.Li + (2 * LB) * (2 * LB);
+        L.Y = L.UiT + (2 * LB) * (2 * LB);
         od += (size_t)L.nblk * LB * LB;
         ow += (size_t)2 * L.n * 2 * LB;
-        // W: 2n rows of 2 LB floats; boxes of 32 floats (128 bytes) x 128 rows
-        const cuuint32_t es[2] = {1, 1};
-        {
-            const cuuint64_t dims[2] = {(cuuint64_t)(2 * LB), (cuuint64_t)(2 * L.n)};
-            const cuuint64_t strides[1] = {(cuuint64_t)(2 * LB * sizeof(float))};
-            const cuuint32_t box[2] = {(cuuint32_t)GK, (cuuint32_t)GM};
-            const CUresult r = encode(&maps[(size_t)(2 * s)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
-                                                      L.W, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                                      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-            require(r == CUDA_SUCCESS, "LU: tensor map of the panel workspace");
-        }
-        // F: n columns of 2n floats (natural real view), leading dimension 2 ld
-        {
-            const cuuint64_t dims[2] = {(cuuint64_t)(2 * L.n), (cuuint64_t)L.n};
-            const cuuint64_t strides[1] = {(cuuint64_t)(2 * L.ld * sizeof(float))};
-            const cuuint32_t box[2] = {(cuuint32_t)GK, (cuuint32_t)GN};
-            const CUresult r = encode(&maps[(size_t)(2 * s + 1)], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
-                                                      L.F, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                                      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-            require(r == CUDA_SUCCESS, "LU: tensor map of the factors");
-        }
-        L.tmW = d->maps.as<CUtensorMap>() + 2 * s;
-        L.tmF = d->maps.as<CUtensorMap>() + 2 * s + 1;
+        op += (size_t)2 * (2 * LB) * (2 * LB) + (size_t)(2 * LB) * L.n;
+        CUtensorMap* ms = maps.data() + (size_t)NMAP * s;
+        map2d(ms + 0, L.W, 2 * LB, 2 * L.n, 2 * LB, GM, "the panel workspace");        // W
+        map2d(ms + 1, L.F, 2 * L.n, L.n, 2 * L.ld, GN, "the factors");                 // F, natural real view
+        map2d(ms + 2, L.Y, 2 * LB, L.n, 2 * LB, GN, "the row panel");                  // Y
+        map2d(ms + 3, L.Li, 2 * LB, 2 * LB, 2 * LB, GM, "the lower inverse");          // Li
+        map2d(ms + 4, L.UiT, 2 * LB, 2 * LB, 2 * LB, GN, "the upper inverse");         // UiT
+        CUtensorMap* md = d->maps.as<CUtensorMap>() + (size_t)NMAP * s;
+        L.tmW = md + 0;
+        L.tmF = md + 1;
+        L.tmY = md + 2;
+        L.tmL = md + 3;
+        L.tmU = md + 4;
     }
     BEM_CUDA(cudaMemcpyAsync(d->maps.p, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice,
                              c.stream));
     // work lists of every launch
     for (int k = 0; k < d->nblk_max; ++k) {
-        std::vector<std::pair<int, int64_t>> ed, eu, el, eg;
+        std::vector<std::pair<int, int64_t>> ed, ex, eu, el, eg, ec;
         for (int s = 0; s < nsys; ++s) {
             const LuSys& L = d->sys[(size_t)s];
             if (L.nblk <= k || owner[(size_t)s] != s) continue;  // factored once per operator
             ed.push_back({s, 1});
             const int64_t mt = L.n - (int64_t)(k + 1) * LB;
             if (mt > 0) {
-                eu.push_back({s, (mt + 63) / 64});
-                el.push_back({s, (mt + 63) / 64});
+                ex.push_back({s, (mt + 63) / 64});
+                eu.push_back({s, 2 * ((mt + GN - 1) / GN)});
+                el.push_back({s, (2 * mt + GM - 1) / GM});
                 eg.push_back({s, ((2 * mt + GM - 1) / GM) * ((mt + GN - 1) / GN)});
+                ec.push_back({s, (mt + 31) / 32});
             }
         }
         d->diag.push_back(add_segment(*d, ed));
+        d->expand.push_back(add_segment(*d, ex));
         d->u12.push_back(add_segment(*d, eu));
         d->l21.push_back(add_segment(*d, el));
         d->gemm.push_back(add_segment(*d, eg));
+        d->copy.push_back(add_segment(*d, ec));
     }
     for (int k = -1; k < d->nblk_max - 1; ++k) {
         std::vector<std::pair<int, int64_t>> e;
@@ -824,11 +856,12 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     BEM_CUDA(cudaMemsetAsync(d->info.p, 0, sizeof(int), c.stream));
     int* err = device_err(c);
     BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c.stream));
-    const size_t diag_smem = sizeof(float2) * LB * LB, panel_smem = sizeof(float2) * (LB * LB + 64 * LB);
+    const size_t diag_smem = sizeof(float2) * LB * LB, expand_smem = sizeof(float2) * 64 * LB;
     BEM_CUDA(cudaFuncSetAttribute(lu_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_smem));
-    BEM_CUDA(cudaFuncSetAttribute(lu_u12_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
-    BEM_CUDA(cudaFuncSetAttribute(lu_l21_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
-    BEM_CUDA(cudaFuncSetAttribute(lu_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    BEM_CUDA(cudaFuncSetAttribute(lu_expand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)expand_smem));
+    BEM_CUDA(cudaFuncSetAttribute(lu_gemm_kernel<G_TRAIL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    BEM_CUDA(cudaFuncSetAttribute(lu_gemm_kernel<G_U12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    BEM_CUDA(cudaFuncSetAttribute(lu_gemm_kernel<G_L21>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
     const LuSys* sys = d->sysbuf.as<LuSys>();
     const LuWork* wk = d->work.as<LuWork>();
     int nsm = 0;
@@ -840,8 +873,9 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     if (c.profiling)
         for (auto& e : ev) BEM_CUDA(cudaEventCreate(&e));
     for (int k = 0; k < d->nblk_max; ++k) {
-        const auto &sd = d->diag[(size_t)k], &su = d->u12[(size_t)k], &sl = d->l21[(size_t)k],
-                   &sg = d->gemm[(size_t)k];
+        const auto &sd = d->diag[(size_t)k], &sx = d->expand[(size_t)k], &su = d->u12[(size_t)k],
+                   &sl = d->l21[(size_t)k], &sg = d->gemm[(size_t)k], &sc = d->copy[(size_t)k];
+        auto persistent = [&](int64_t ctas) { return (unsigned)std::min<int64_t>(ctas, nsm); };
         if (c.profiling) BEM_CUDA(cudaEventRecord(ev[0], c.stream));
         if (sd.ctas) {
             lu_diag_kernel<<<(unsigned)sd.ctas, 1024, diag_smem, c.stream>>>(sys, wk + sd.off, k,
@@ -849,19 +883,26 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
             BEM_CHECK_LAUNCH(&c);
         }
         if (c.profiling) BEM_CUDA(cudaEventRecord(ev[1], c.stream));
-        if (su.ctas) {
-            lu_u12_kernel<<<(unsigned)su.ctas, 256, panel_smem, c.stream>>>(sys, wk + su.off, su.count, k);
+        if (sx.ctas) {  // column panel: embed A21, then L21 = A21 U11^-1 in place
+            lu_expand_kernel<<<(unsigned)sx.ctas, 256, expand_smem, c.stream>>>(sys, wk + sx.off, sx.count, k);
+            BEM_CHECK_LAUNCH(&c);
+            lu_gemm_kernel<G_L21><<<persistent(sl.ctas), GTHREADS, G_SMEM, c.stream>>>(sys, wk + sl.off, sl.count,
+                                                                                       k, sl.ctas, err);
             BEM_CHECK_LAUNCH(&c);
         }
         if (c.profiling) BEM_CUDA(cudaEventRecord(ev[2], c.stream));
-        if (sl.ctas) {
-            lu_l21_kernel<<<(unsigned)sl.ctas, 256, panel_smem, c.stream>>>(sys, wk + sl.off, sl.count, k);
+        if (su.ctas) {  // row panel: Y = L11^-1 A12
+            lu_gemm_kernel<G_U12><<<persistent(su.ctas), GTHREADS, G_SMEM, c.stream>>>(sys, wk + su.off, su.count,
+                                                                                       k, su.ctas, err);
             BEM_CHECK_LAUNCH(&c);
         }
         if (c.profiling) BEM_CUDA(cudaEventRecord(ev[3], c.stream));
         if (sg.ctas) {
-            const unsigned grid = (unsigned)std::min<int64_t>(sg.ctas, nsm);
-            lu_gemm_kernel<<<grid, GTHREADS, G_SMEM, c.stream>>>(sys, wk + sg.off, sg.count, k, sg.ctas, err);
+            lu_gemm_kernel<G_TRAIL><<<persistent(sg.ctas), GTHREADS, G_SMEM, c.stream>>>(sys, wk + sg.off,
+                                                                                         sg.count, k, sg.ctas, err);
+            BEM_CHECK_LAUNCH(&c);
+            // U12 into the factors for the substitutions
+            lu_copy_u12_kernel<<<(unsigned)sc.ctas, 256, 0, c.stream>>>(sys, wk + sc.off, sc.count, k);
             BEM_CHECK_LAUNCH(&c);
         }
         if (c.profiling) {
@@ -875,14 +916,14 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
             for (int s = 0; s < nsys; ++s) {
                 const double mt = (double)(d->sys[(size_t)s].n - (int64_t)(k + 1) * LB);
                 if (mt <= 0) continue;
-                flops[1] += 8.0 * LB * LB * mt;
-                flops[2] += 8.0 * LB * LB * mt;
+                flops[1] += 8.0 * LB * LB * mt;  // L21 (complex flop)
+                flops[2] += 8.0 * LB * LB * mt;  // U12
                 flops[3] += 8.0 * LB * mt * mt;
             }
         }
     }
     if (c.profiling) {
-        const char* names[4] = {"lu_diag", "lu_u12", "lu_l21", "lu_gemm_tf32"};
+        const char* names[4] = {"lu_diag", "lu_l21_tf32", "lu_u12_tf32", "lu_gemm_tf32"};
         for (int q = 0; q < 4; ++q) c.stage_add(names[q], tsum[q], d->nblk_max, flops[q]);
         for (auto& e : ev) cudaEventDestroy(e);
     }
