@@ -53,6 +53,18 @@ def test_lu_small_and_block_multiples(ctx, wd, sub, method):
         assert b["iterations"] <= max(4, a["iterations"] // 2), (a["iterations"], b["iterations"])
 
 
+@pytest.mark.parametrize("ntri", [128, 130, 256, 258])
+def test_lu_block_edges(ctx, wd, ntri):
+    """Exactly one and two blocks of 128 (no panels after the last), and one
+    unknown past them (a 2-unknown last block)."""
+    inp = workloads.perturbed_sphere_input(wd, 50 + ntri, ntri, [1.5, 4.0], tol=1e-10)
+    r1 = _run(ctx, inp, "lu")
+    for b in r1:
+        assert b["flag"] == 1 and b["precond"] == bem.PRECOND_LU
+        assert 0 <= b["rel_err_vs_lu"] < 1e-6, b
+        assert b["iterations"] <= 8
+
+
 def test_lu_hard_impedance(ctx, wd):
     """Impedance condition at high ka, where unpreconditioned GMRES(32) needs
     hundreds of iterations."""
