@@ -280,11 +280,14 @@ void run_mixed_batch(Context& c, const std::vector<Problem*>& probs, bem_precond
     while (i < batched.size()) {
         std::vector<BodyPlan*> chunk;
         size_t bytes = 0;
-        // the LU preconditioner keeps a factored copy of every operator
-        const double per_op = precond == BEM_PRECOND_LU ? 2.2 : 1.0;
-        while (i < batched.size() &&
-               (chunk.empty() || (double)bytes + per_op * (double)batched[i]->op_bytes <= (double)budget_bytes)) {
-            bytes += (size_t)(per_op * (double)batched[i]->op_bytes);
+        // the LU preconditioner keeps a factored copy of every operator and,
+        // per unknown, the diagonal blocks and the panel workspaces (7 KB)
+        auto need = [&](const BodyPlan* p) {
+            return precond == BEM_PRECOND_LU ? 2.0 * (double)p->op_bytes + 7200.0 * (double)p->n * (double)p->nf
+                                             : (double)p->op_bytes;
+        };
+        while (i < batched.size() && (chunk.empty() || (double)bytes + need(batched[i]) <= (double)budget_bytes)) {
+            bytes += (size_t)need(batched[i]);
             chunk.push_back(batched[i]);
             ++i;
         }

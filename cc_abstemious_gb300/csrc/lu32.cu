@@ -54,7 +54,8 @@ namespace {
 constexpr int LB = 128;                 // block size (complex unknowns)
 constexpr int GM = 128, GN = 256;       // GEMM tile: real rows x columns
 constexpr int GK = 32;                  // real K per pipeline chunk
-constexpr int GCHUNKS = 2 * LB / GK;    // 8
+constexpr int GCHUNKS = 2 * LB / GK;    // 8 chunks: K = 256, one block step
+constexpr int WK = 4 * LB;              // panel workspace width: two block steps (K = 512)
 constexpr int GS = 4;                   // pipeline stages
 constexpr int GTHREADS = 320;           // producer warp, MMA warp, eight epilogue warps
 constexpr int GEPI = GTHREADS - 64;     // epilogue threads
@@ -65,25 +66,39 @@ constexpr uint32_t G_TMEM_COLS = 512;           // two accumulators of GN column
 struct LuSys {
     float2* F;    // factors (copy of the operator), column-major, leading dimension ld
     float2* Dm;   // per block: L11^-1 (strict lower) and U11^-1 (upper), LB x LB column-major
-    float* W;     // real embedding of the current step's A21, then L21: 2n rows x 2 LB floats, row-major
+    float* W;     // real embeddings of the step pair's column panels (A21, then L21): 2n rows x WK floats
     float* Li;    // real embedding of L11^-1: 2 LB x 2 LB, row-major
     float* UiT;   // transposed real embedding of U11^-1: 2 LB x 2 LB, row-major
-    float* Y;     // U12 of the current step, natural real view: column j at Y + 2 LB j
-    const CUtensorMap* tmW;  // W: 2n rows x 256 floats, 128-byte swizzled 32 x 128 boxes
+    float* Y;     // the step pair's U12, natural real view: column j at Y + WK j (first step's rows 0-255)
+    const CUtensorMap* tmW;  // W: 2n rows x WK floats, 128-byte swizzled 32 x 128 boxes
     const CUtensorMap* tmF;  // F's natural real view: n columns x 2n floats, 32 x 256 boxes
-    const CUtensorMap* tmY;  // Y: n columns x 256 floats, 32 x 256 boxes
+    const CUtensorMap* tmY;  // Y: n columns x WK floats, 32 x 256 boxes
     const CUtensorMap* tmL;  // Li: 256 rows, 32 x 128 boxes
     const CUtensorMap* tmU;  // UiT: 256 rows, 32 x 256 boxes
     int64_t n, ld;
     int nblk, pad;
 };
 
-// One entry per (system, launch): the system and its first CTA in the
-// flattened grid of that launch.
+// One entry per (system, launch): the system, its first CTA in the flattened
+// grid of that launch and, for the GEMMs, the region it covers (rows of the
+// panel workspace, relative to the step pair's trailing origin, and columns).
 struct LuWork {
-    int sys, pad;
+    int sys, tiles_i;
     int64_t tile0;
+    int64_t r0, r1, c0, c1;
 };
+
+// Index of the work entry holding CTA t of a launch, and t's rank in it.
+__device__ __forceinline__ int lu_entry(const LuWork* __restrict__ wl, int nw, int64_t t, int64_t& local) {
+    int lo = 0, hi = nw - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (wl[mid].tile0 <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    local = t - wl[lo].tile0;
+    return lo;
+}
 
 __device__ __forceinline__ int lu_locate(const LuWork* __restrict__ wl, int nw, int64_t t, int64_t& local) {
     int lo = 0, hi = nw - 1;
@@ -213,41 +228,44 @@ __global__ void __launch_bounds__(1024) lu_diag_kernel(const LuSys* __restrict__
     }
 }
 
-// W <- real embedding of the column panel A21 (64 rows per CTA): rows 2i and
-// 2i + 1 of W hold [ar, -ai] and [ai, ar] for every column of A21's row i.
+// W <- real embedding of step ks's column panel A21 (64 rows per CTA): rows
+// 2(i - kt_w) and 2(i - kt_w) + 1 of W, columns woff .. woff + 256, hold
+// [ar, -ai] and [ai, ar] for every column of A21's row i; kt_w = (kw + 1) LB
+// is the trailing origin of the step pair.
 __global__ void __launch_bounds__(256) lu_expand_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
-                                                        int nw, int k) {
+                                                        int nw, int ks, int kw, int woff) {
     extern __shared__ float2 Y[];  // 64 x LB: Y[p * 64 + i]
     int64_t tile;
     const LuSys S = sys[lu_locate(wl, nw, blockIdx.x, tile)];
-    const int64_t k0 = (int64_t)k * LB, kt = k0 + LB, i0 = kt + 64 * tile;
+    const int64_t k0 = (int64_t)ks * LB, kt = k0 + LB, ktw = (int64_t)(kw + 1) * LB, i0 = kt + 64 * tile;
     const int nrow = (int)min((int64_t)64, S.n - i0);
     for (int t = threadIdx.x; t < 64 * LB; t += blockDim.x) {
         const int p = t / 64, i = t % 64;
         Y[t] = i < nrow ? S.F[(k0 + p) * S.ld + i0 + i] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    const int64_t wr0 = 2 * (i0 - kt);
+    const int64_t wr0 = 2 * (i0 - ktw);
     for (int t = threadIdx.x; t < nrow * LB; t += blockDim.x) {
         const int i = t / LB, c = t % LB;
         const float2 v = Y[c * 64 + i];
-        float2* w0 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i) * (2 * LB));
-        float2* w1 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i + 1) * (2 * LB));
+        float2* w0 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i) * WK + woff);
+        float2* w1 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i + 1) * WK + woff);
         w0[c] = make_float2(v.x, -v.y);
         w1[c] = make_float2(v.y, v.x);
     }
 }
 
-// F's row panel (rows k0 .. k0 + LB of every column j >= kt) <- Y (32 columns per CTA).
+// Step ks's row panel in the factors (rows ks LB .. + LB of every column
+// j >= (ks + 1) LB) <- rows yoff .. yoff + 256 of Y (32 columns per CTA).
 __global__ void __launch_bounds__(256) lu_copy_u12_kernel(const LuSys* __restrict__ sys,
-                                                          const LuWork* __restrict__ wl, int nw, int k) {
+                                                          const LuWork* __restrict__ wl, int nw, int ks, int yoff) {
     int64_t tile;
     const LuSys S = sys[lu_locate(wl, nw, blockIdx.x, tile)];
-    const int64_t k0 = (int64_t)k * LB, kt = k0 + LB, j0 = kt + 32 * tile;
+    const int64_t k0 = (int64_t)ks * LB, kt = k0 + LB, j0 = kt + 32 * tile;
     const int ncol = (int)min((int64_t)32, S.n - j0);
     for (int t = threadIdx.x; t < ncol * (LB / 2); t += blockDim.x) {
         const int c = t / (LB / 2), q = t % (LB / 2);  // 64 float4 per column
-        const float4 v = reinterpret_cast<const float4*>(S.Y + (j0 + c) * (2 * LB))[q];
+        const float4 v = reinterpret_cast<const float4*>(S.Y + (j0 + c) * WK + yoff)[q];
         reinterpret_cast<float4*>(S.F + (j0 + c) * S.ld + k0)[q] = v;
     }
 }
@@ -298,40 +316,44 @@ __host__ __device__ constexpr uint32_t umma_idesc_tf32_f32(int M, int N) {
 // the MMAs of a stage and releases it through tcgen05.commit on its "empty"
 // barrier, and warps 2-9 drain the accumulator of the previous tile (two
 // accumulators of 256 tensor-memory columns) while the next tile's MMAs run.
-// GEMM modes of one block step (all D = A' B over K = 2 LB real):
-//   TRAIL  A22 -= W Y        tiles of 128 rows of W x 256 columns of Y
-//   U12    Y = Li U12raw     the two 128-row halves of Li x 256 columns of F's row panel
-//   L21    W = W UiT^T       128 rows of W x all 256 columns, in place; F's column panel
-//                            receives L21 in natural form
+// GEMM modes (D = A' B over K = 32 nchunks real), for block step ks of the
+// step pair starting at kw (trailing origin kt_w = (kw + 1) LB, the row origin
+// of W and of the TRAIL work regions):
+//   TRAIL  A22 -= W Y        128 rows of W x 256 columns of Y inside each work
+//                            entry's region; K = 256 (one step) or 512 (both)
+//   U12    Y = Li U12raw     the two 128-row halves of Li x 256 columns of the
+//                            step's row panel, into Y's rows yoff .. yoff + 256
+//   L21    W = W UiT^T       128 rows of W x all 256 columns at W column woff, in
+//                            place; L21 in natural form into the factors
 enum { G_TRAIL = 0, G_U12 = 1, G_L21 = 2 };
 
 struct GemmTile {
     const CUtensorMap *tmA, *tmB;
     int ax, ay, bx, by;  // tensor-copy coordinates of chunk 0 (x advances by GK per chunk)
     float *F, *Y, *W;
-    int64_t n, rows, ld, ld2, k0, kt, row0, col0;
+    int64_t n, ld, ld2, k0, ktw, row0, rows_end, col0, col_end;
 };
 
 template <int MODE>
 __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl, int nw,
-                                              int k, int64_t t) {
+                                              int64_t t, int ks, int kw, int woff) {
     int64_t local;
-    const LuSys S = sys[lu_locate(wl, nw, t, local)];
+    const LuWork& w = wl[lu_entry(wl, nw, t, local)];
+    const LuSys S = sys[w.sys];
     GemmTile g;
     g.F = reinterpret_cast<float*>(S.F);
     g.Y = S.Y;
     g.W = S.W;
     g.n = S.n;
     g.ld = S.ld;
-    g.k0 = (int64_t)k * LB;
-    g.kt = g.k0 + LB;
     g.ld2 = 2 * S.ld;
-    const int64_t mt = S.n - g.kt;
+    g.k0 = (int64_t)ks * LB;
+    g.ktw = (int64_t)(kw + 1) * LB;
     if (MODE == G_TRAIL) {
-        g.rows = 2 * mt;
-        const int64_t tiles_i = (g.rows + GM - 1) / GM;
-        g.row0 = (local % tiles_i) * GM;
-        g.col0 = g.kt + (local / tiles_i) * GN;
+        g.row0 = w.r0 + (local % w.tiles_i) * GM;
+        g.rows_end = w.r1;
+        g.col0 = w.c0 + (local / w.tiles_i) * GN;
+        g.col_end = w.c1;
         g.tmA = S.tmW;
         g.ax = 0;
         g.ay = (int)g.row0;
@@ -339,9 +361,10 @@ __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, con
         g.bx = 0;
         g.by = (int)g.col0;
     } else if (MODE == G_U12) {
-        g.rows = 2 * LB;
         g.row0 = (local & 1) * GM;
-        g.col0 = g.kt + (local >> 1) * GN;
+        g.rows_end = 2 * LB;
+        g.col0 = w.c0 + (local >> 1) * GN;
+        g.col_end = w.c1;
         g.tmA = S.tmL;
         g.ax = 0;
         g.ay = (int)g.row0;
@@ -349,11 +372,12 @@ __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, con
         g.bx = (int)(2 * g.k0);
         g.by = (int)g.col0;
     } else {
-        g.rows = 2 * mt;
-        g.row0 = local * GM;
+        g.row0 = w.r0 + local * GM;
+        g.rows_end = w.r1;
         g.col0 = 0;
+        g.col_end = 2 * LB;
         g.tmA = S.tmW;
-        g.ax = 0;
+        g.ax = woff;
         g.ay = (int)g.row0;
         g.tmB = S.tmU;
         g.bx = 0;
@@ -364,8 +388,9 @@ __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, con
 
 template <int MODE>
 __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __restrict__ sys,
-                                                              const LuWork* __restrict__ wl, int nw, int k,
-                                                              int64_t ntiles, int* __restrict__ err) {
+                                                              const LuWork* __restrict__ wl, int nw, int ks, int kw,
+                                                              int nchunks, int woff, int yoff, int64_t ntiles,
+                                                              int* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + GS * GSTAGE);
     uint64_t* empty = full + GS;
@@ -404,8 +429,8 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
         if (lane == 0) {
             int64_t it = 0;
             for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
-                const GemmTile g = gemm_tile<MODE>(sys, wl, nw, k, t);
-                for (int c = 0; c < GCHUNKS; ++c, ++it) {
+                const GemmTile g = gemm_tile<MODE>(sys, wl, nw, t, ks, kw, woff);
+                for (int c = 0; c < nchunks; ++c, ++it) {
                     const int st = (int)(it % GS);
                     const int64_t round = it / GS;
                     if (round > 0 && !mbar_wait_bounded(&empty[st], (uint32_t)((round - 1) & 1))) {
@@ -436,7 +461,7 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
             __syncwarp();
             if (*abort_flag) break;
             tc_fence_after();
-            for (int c = 0; c < GCHUNKS; ++c, ++it) {
+            for (int c = 0; c < nchunks; ++c, ++it) {
                 const int st = (int)(it % GS);
                 if (lane == 0) {
                     if (!mbar_wait_bounded(&full[st], (uint32_t)((it / GS) & 1))) fail();
@@ -471,19 +496,19 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                 break;
             }
             tc_fence_after();
-            const GemmTile g = gemm_tile<MODE>(sys, wl, nw, k, t);
+            const GemmTile g = gemm_tile<MODE>(sys, wl, nw, t, ks, kw, woff);
             const int64_t r = g.row0 + 32 * quarter + lane;
-            const bool rok = r < g.rows;
+            const bool rok = r < g.rows_end;
             for (int cc = half * (GN / 64); cc < (half + 1) * (GN / 64); ++cc) {
                 const int64_t jb = g.col0 + cc * 32;
-                if (MODE != G_L21 && jb >= g.n) break;  // uniform over the warp
+                if (jb >= g.col_end) break;  // uniform over the warp
                 float v[32];
                 tmem_ld32(tmem + lane_base + (uint32_t)(acc * GN + cc * 32), v);
                 if (MODE == G_TRAIL) {
                     if (!rok) continue;
                     // all 32 loads in flight before the first store
-                    const int nq = (int)min((int64_t)32, g.n - jb);
-                    float* p0 = g.F + jb * g.ld2 + 2 * g.kt + r;
+                    const int nq = (int)min((int64_t)32, g.col_end - jb);
+                    float* p0 = g.F + jb * g.ld2 + 2 * g.ktw + r;
                     float cv[32];
 #pragma unroll
                     for (int q = 0; q < 32; ++q) cv[q] = q < nq ? __ldcg(p0 + q * g.ld2) : 0.f;
@@ -491,11 +516,11 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                     for (int q = 0; q < 32; ++q)
                         if (q < nq) p0[q * g.ld2] = cv[q] - v[q];
                 } else if (MODE == G_U12) {
-                    const int nq = (int)min((int64_t)32, g.n - jb);
-                    float* p0 = g.Y + jb * (2 * LB) + r;
+                    const int nq = (int)min((int64_t)32, g.col_end - jb);
+                    float* p0 = g.Y + jb * WK + yoff + r;
 #pragma unroll
                     for (int q = 0; q < 32; ++q)
-                        if (q < nq) p0[q * (2 * LB)] = v[q];
+                        if (q < nq) p0[q * WK] = v[q];
                 } else {
                     // L21: the embedded row back into W, and the natural
                     // entries (row 2i holds re, row 2i + 1 im of column 2p)
@@ -503,11 +528,11 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
 #pragma unroll
                     for (int q = 0; q < 16; ++q) im[q] = __shfl_down_sync(0xffffffffu, v[2 * q], 1);
                     if (!rok) continue;
-                    float4* wrow = reinterpret_cast<float4*>(g.W + r * (2 * LB) + cc * 32);
+                    float4* wrow = reinterpret_cast<float4*>(g.W + r * WK + woff + cc * 32);
 #pragma unroll
                     for (int q = 0; q < 8; ++q) wrow[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
                     if ((lane & 1) == 0) {
-                        const int64_t i = g.kt + (r >> 1);
+                        const int64_t i = g.ktw + (r >> 1);
                         float2* F2 = reinterpret_cast<float2*>(g.F);
 #pragma unroll
                         for (int q = 0; q < 16; ++q)
@@ -651,23 +676,52 @@ struct LuData {
         int count = 0;
         int64_t ctas = 0;
     };
-    std::vector<Seg> diag, expand, u12, l21, gemm, copy, fwd, bwd;
+    // the factorization as an ordered list of launches
+    enum Kind { DIAG, EXPAND, L21, U12, COPY, TRAIL };
+    struct Launch {
+        Kind kind;
+        int ks, kw, woff, yoff, nchunks;
+        Seg seg;
+    };
+    std::vector<Launch> plan;
+    std::vector<Seg> fwd, bwd;
     std::vector<LuWork> host;
     int small_pivots = 0;
 };
 
-LuData::Seg add_segment(LuData& d, const std::vector<std::pair<int, int64_t>>& entries) {
+// A work entry: system, CTAs, and for the GEMMs the covered region.
+struct Entry {
+    int sys;
+    int64_t ctas;
+    int tiles_i;
+    int64_t r0, r1, c0, c1;
+};
+
+LuData::Seg add_segment(LuData& d, const std::vector<Entry>& entries) {
     LuData::Seg sg;
     sg.off = (int64_t)d.host.size();
     int64_t t = 0;
-    for (auto& e : entries) {
-        if (e.second <= 0) continue;
-        d.host.push_back(LuWork{e.first, 0, t});
-        t += e.second;
+    for (const Entry& e : entries) {
+        if (e.ctas <= 0) continue;
+        d.host.push_back(LuWork{e.sys, e.tiles_i, t, e.r0, e.r1, e.c0, e.c1});
+        t += e.ctas;
     }
     sg.count = (int)((int64_t)d.host.size() - sg.off);
     sg.ctas = t;
     return sg;
+}
+
+LuData::Seg add_segment(LuData& d, const std::vector<std::pair<int, int64_t>>& entries) {
+    std::vector<Entry> e;
+    for (auto& x : entries) e.push_back(Entry{x.first, x.second, 0, 0, 0, 0, 0});
+    return add_segment(d, e);
+}
+
+// A GEMM region of TRAIL mode: rows [r0, r1) of W (relative to the trailing
+// origin) x columns [c0, c1).
+Entry trail_entry(int s, int64_t r0, int64_t r1, int64_t c0, int64_t c1) {
+    const int64_t ti = (r1 - r0 + GM - 1) / GM, tj = (c1 - c0 + GN - 1) / GN;
+    return Entry{s, (r1 > r0 && c1 > c0) ? ti * tj : 0, (int)ti, r0, r1, c0, c1};
 }
 
 void lu_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
@@ -728,8 +782,8 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         entries = std::max(entries, v[(size_t)s].a + (size_t)v[(size_t)s].lda * v[(size_t)s].n);
         const int nb = (int)((v[(size_t)s].n + LB - 1) / LB);
         dm += (size_t)nb * LB * LB;
-        wsz += (size_t)2 * v[(size_t)s].n * 2 * LB;
-        psz += (size_t)2 * (2 * LB) * (2 * LB) + (size_t)(2 * LB) * v[(size_t)s].n;
+        wsz += (size_t)2 * v[(size_t)s].n * WK;
+        psz += (size_t)2 * (2 * LB) * (2 * LB) + (size_t)WK * v[(size_t)s].n;
         d->nblk_max = std::max(d->nblk_max, nb);
     }
     // the factors, block inverses and panel workspace live in grow-only
@@ -791,12 +845,12 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         L.UiT = L.Li + (2 * LB) * (2 * LB);
         L.Y = L.UiT + (2 * LB) * (2 * LB);
         od += (size_t)L.nblk * LB * LB;
-        ow += (size_t)2 * L.n * 2 * LB;
-        op += (size_t)2 * (2 * LB) * (2 * LB) + (size_t)(2 * LB) * L.n;
+        ow += (size_t)2 * L.n * WK;
+        op += (size_t)2 * (2 * LB) * (2 * LB) + (size_t)WK * L.n;
         CUtensorMap* ms = maps.data() + (size_t)NMAP * s;
-        map2d(ms + 0, L.W, 2 * LB, 2 * L.n, 2 * LB, GM, "the panel workspace");        // W
+        map2d(ms + 0, L.W, WK, 2 * L.n, WK, GM, "the panel workspace");                // W
         map2d(ms + 1, L.F, 2 * L.n, L.n, 2 * L.ld, GN, "the factors");                 // F, natural real view
-        map2d(ms + 2, L.Y, 2 * LB, L.n, 2 * LB, GN, "the row panel");                  // Y
+        map2d(ms + 2, L.Y, WK, L.n, WK, GN, "the row panel");                          // Y
         map2d(ms + 3, L.Li, 2 * LB, 2 * LB, 2 * LB, GM, "the lower inverse");          // Li
         map2d(ms + 4, L.UiT, 2 * LB, 2 * LB, 2 * LB, GN, "the upper inverse");         // UiT
         CUtensorMap* md = d->maps.as<CUtensorMap>() + (size_t)NMAP * s;
@@ -808,28 +862,55 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     }
     BEM_CUDA(cudaMemcpyAsync(d->maps.p, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice,
                              c.stream));
-    // work lists of every launch
-    for (int k = 0; k < d->nblk_max; ++k) {
-        std::vector<std::pair<int, int64_t>> ed, ex, eu, el, eg, ec;
+    // the factorization plan: block steps in pairs (k, k + 1).  Step k's panels,
+    // then its update of block column and block row k + 1 only (K = 256),
+    // step k + 1's panels, then one K = 512 update of the rest with both
+    // steps' panels: A22 is read and written once per two steps.  A system
+    // whose step k + 1 has no trailing block takes step k's full update.
+    auto plan = [&](LuData::Kind kind, int ks, int kw, int woff, int yoff, int nchunks,
+                    const std::vector<Entry>& e) {
+        LuData::Launch l{kind, ks, kw, woff, yoff, nchunks, add_segment(*d, e)};
+        if (l.seg.ctas) d->plan.push_back(l);
+    };
+    for (int k = 0; k < d->nblk_max; k += 2) {
+        std::vector<Entry> diag0, exp0, l210, u120, copy0, trail0, diag1, exp1, l211, u121, copy1, trail1;
         for (int s = 0; s < nsys; ++s) {
             const LuSys& L = d->sys[(size_t)s];
             if (L.nblk <= k || owner[(size_t)s] != s) continue;  // factored once per operator
-            ed.push_back({s, 1});
-            const int64_t mt = L.n - (int64_t)(k + 1) * LB;
-            if (mt > 0) {
-                ex.push_back({s, (mt + 63) / 64});
-                eu.push_back({s, 2 * ((mt + GN - 1) / GN)});
-                el.push_back({s, (2 * mt + GM - 1) / GM});
-                eg.push_back({s, ((2 * mt + GM - 1) / GM) * ((mt + GN - 1) / GN)});
-                ec.push_back({s, (mt + 31) / 32});
+            const int64_t kt0 = (int64_t)(k + 1) * LB, kt1 = kt0 + LB;
+            const int64_t mt0 = L.n - kt0, mt1 = L.n - kt1;
+            diag0.push_back(Entry{s, 1, 0, 0, 0, 0, 0});
+            if (mt0 <= 0) continue;
+            exp0.push_back(Entry{s, (mt0 + 63) / 64, 0, 0, 0, 0, 0});
+            l210.push_back(Entry{s, (2 * mt0 + GM - 1) / GM, 0, 0, 2 * mt0, 0, 0});
+            u120.push_back(Entry{s, 2 * ((mt0 + GN - 1) / GN), 0, 0, 0, kt0, L.n});
+            copy0.push_back(Entry{s, (mt0 + 31) / 32, 0, 0, 0, 0, 0});
+            if (mt1 <= 0) {  // block k + 1 is the last: step k's full update
+                trail0.push_back(trail_entry(s, 0, 2 * mt0, kt0, L.n));
+                if (L.nblk > k + 1) diag1.push_back(Entry{s, 1, 0, 0, 0, 0, 0});
+                continue;
             }
+            trail0.push_back(trail_entry(s, 0, 2 * mt0, kt0, kt1));     // block column k + 1
+            trail0.push_back(trail_entry(s, 0, 2 * LB, kt1, L.n));      // block row k + 1
+            diag1.push_back(Entry{s, 1, 0, 0, 0, 0, 0});
+            exp1.push_back(Entry{s, (mt1 + 63) / 64, 0, 0, 0, 0, 0});
+            l211.push_back(Entry{s, (2 * mt1 + GM - 1) / GM, 0, 2 * LB, 2 * mt0, 0, 0});
+            u121.push_back(Entry{s, 2 * ((mt1 + GN - 1) / GN), 0, 0, 0, kt1, L.n});
+            copy1.push_back(Entry{s, (mt1 + 31) / 32, 0, 0, 0, 0, 0});
+            trail1.push_back(trail_entry(s, 2 * LB, 2 * mt0, kt1, L.n));  // both steps, K = 512
         }
-        d->diag.push_back(add_segment(*d, ed));
-        d->expand.push_back(add_segment(*d, ex));
-        d->u12.push_back(add_segment(*d, eu));
-        d->l21.push_back(add_segment(*d, el));
-        d->gemm.push_back(add_segment(*d, eg));
-        d->copy.push_back(add_segment(*d, ec));
+        plan(LuData::DIAG, k, k, 0, 0, 0, diag0);
+        plan(LuData::EXPAND, k, k, 0, 0, 0, exp0);
+        plan(LuData::L21, k, k, 0, 0, GCHUNKS, l210);
+        plan(LuData::U12, k, k, 0, 0, GCHUNKS, u120);
+        plan(LuData::COPY, k, k, 0, 0, 0, copy0);
+        plan(LuData::TRAIL, k, k, 0, 0, GCHUNKS, trail0);
+        plan(LuData::DIAG, k + 1, k, 0, 0, 0, diag1);
+        plan(LuData::EXPAND, k + 1, k, 2 * LB, 0, 0, exp1);
+        plan(LuData::L21, k + 1, k, 2 * LB, 0, GCHUNKS, l211);
+        plan(LuData::U12, k + 1, k, 0, 2 * LB, GCHUNKS, u121);
+        plan(LuData::COPY, k + 1, k, 0, 2 * LB, 0, copy1);
+        plan(LuData::TRAIL, k + 1, k, 0, 0, 2 * GCHUNKS, trail1);
     }
     for (int k = -1; k < d->nblk_max - 1; ++k) {
         std::vector<std::pair<int, int64_t>> e;
@@ -865,67 +946,63 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     const LuSys* sys = d->sysbuf.as<LuSys>();
     const LuWork* wk = d->work.as<LuWork>();
     int nsm = 0;
-    BEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
-    // with profiling: CUDA events around every launch, summed per kernel
-    cudaEvent_t ev[5] = {};
-    float tsum[4] = {0, 0, 0, 0};
-    double flops[4] = {0, 0, 0, 0};
-    if (c.profiling)
-        for (auto& e : ev) BEM_CUDA(cudaEventCreate(&e));
-    for (int k = 0; k < d->nblk_max; ++k) {
-        const auto &sd = d->diag[(size_t)k], &sx = d->expand[(size_t)k], &su = d->u12[(size_t)k],
-                   &sl = d->l21[(size_t)k], &sg = d->gemm[(size_t)k], &sc = d->copy[(size_t)k];
-        auto persistent = [&](int64_t ctas) { return (unsigned)std::min<int64_t>(ctas, nsm); };
-        if (c.profiling) BEM_CUDA(cudaEventRecord(ev[0], c.stream));
-        if (sd.ctas) {
-            lu_diag_kernel<<<(unsigned)sd.ctas, 1024, diag_smem, c.stream>>>(sys, wk + sd.off, k,
-                                                                             d->info.as<int>());
-            BEM_CHECK_LAUNCH(&c);
+    BEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));  // persistent grids
+    // with profiling: CUDA events around every launch, summed per kind
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float tsum[3] = {0, 0, 0};
+    if (c.profiling) {
+        BEM_CUDA(cudaEventCreate(&ev0));
+        BEM_CUDA(cudaEventCreate(&ev1));
+    }
+    auto persistent = [&](int64_t ctas) { return (unsigned)std::min<int64_t>(ctas, nsm); };
+    for (const LuData::Launch& l : d->plan) {
+        const LuData::Seg& sg = l.seg;
+        if (c.profiling) BEM_CUDA(cudaEventRecord(ev0, c.stream));
+        switch (l.kind) {
+            case LuData::DIAG:
+                lu_diag_kernel<<<(unsigned)sg.ctas, 1024, diag_smem, c.stream>>>(sys, wk + sg.off, l.ks,
+                                                                                 d->info.as<int>());
+                break;
+            case LuData::EXPAND:
+                lu_expand_kernel<<<(unsigned)sg.ctas, 256, expand_smem, c.stream>>>(sys, wk + sg.off, sg.count, l.ks,
+                                                                                    l.kw, l.woff);
+                break;
+            case LuData::L21:
+                lu_gemm_kernel<G_L21><<<persistent(sg.ctas), GTHREADS, G_SMEM, c.stream>>>(
+                    sys, wk + sg.off, sg.count, l.ks, l.kw, l.nchunks, l.woff, l.yoff, sg.ctas, err);
+                break;
+            case LuData::U12:
+                lu_gemm_kernel<G_U12><<<persistent(sg.ctas), GTHREADS, G_SMEM, c.stream>>>(
+                    sys, wk + sg.off, sg.count, l.ks, l.kw, l.nchunks, l.woff, l.yoff, sg.ctas, err);
+                break;
+            case LuData::COPY:
+                lu_copy_u12_kernel<<<(unsigned)sg.ctas, 256, 0, c.stream>>>(sys, wk + sg.off, sg.count, l.ks,
+                                                                            l.yoff);
+                break;
+            case LuData::TRAIL:
+                lu_gemm_kernel<G_TRAIL><<<persistent(sg.ctas), GTHREADS, G_SMEM, c.stream>>>(
+                    sys, wk + sg.off, sg.count, l.ks, l.kw, l.nchunks, l.woff, l.yoff, sg.ctas, err);
+                break;
         }
-        if (c.profiling) BEM_CUDA(cudaEventRecord(ev[1], c.stream));
-        if (sx.ctas) {  // column panel: embed A21, then L21 = A21 U11^-1 in place
-            lu_expand_kernel<<<(unsigned)sx.ctas, 256, expand_smem, c.stream>>>(sys, wk + sx.off, sx.count, k);
-            BEM_CHECK_LAUNCH(&c);
-            lu_gemm_kernel<G_L21><<<persistent(sl.ctas), GTHREADS, G_SMEM, c.stream>>>(sys, wk + sl.off, sl.count,
-                                                                                       k, sl.ctas, err);
-            BEM_CHECK_LAUNCH(&c);
-        }
-        if (c.profiling) BEM_CUDA(cudaEventRecord(ev[2], c.stream));
-        if (su.ctas) {  // row panel: Y = L11^-1 A12
-            lu_gemm_kernel<G_U12><<<persistent(su.ctas), GTHREADS, G_SMEM, c.stream>>>(sys, wk + su.off, su.count,
-                                                                                       k, su.ctas, err);
-            BEM_CHECK_LAUNCH(&c);
-        }
-        if (c.profiling) BEM_CUDA(cudaEventRecord(ev[3], c.stream));
-        if (sg.ctas) {
-            lu_gemm_kernel<G_TRAIL><<<persistent(sg.ctas), GTHREADS, G_SMEM, c.stream>>>(sys, wk + sg.off,
-                                                                                         sg.count, k, sg.ctas, err);
-            BEM_CHECK_LAUNCH(&c);
-            // U12 into the factors for the substitutions
-            lu_copy_u12_kernel<<<(unsigned)sc.ctas, 256, 0, c.stream>>>(sys, wk + sc.off, sc.count, k);
-            BEM_CHECK_LAUNCH(&c);
-        }
+        BEM_CHECK_LAUNCH(&c);
         if (c.profiling) {
-            BEM_CUDA(cudaEventRecord(ev[4], c.stream));
-            BEM_CUDA(cudaEventSynchronize(ev[4]));
-            for (int q = 0; q < 4; ++q) {
-                float ms = 0;
-                BEM_CUDA(cudaEventElapsedTime(&ms, ev[q], ev[q + 1]));
-                tsum[q] += ms;
-            }
-            for (int s = 0; s < nsys; ++s) {
-                const double mt = (double)(d->sys[(size_t)s].n - (int64_t)(k + 1) * LB);
-                if (mt <= 0) continue;
-                flops[1] += 8.0 * LB * LB * mt;  // L21 (complex flop)
-                flops[2] += 8.0 * LB * LB * mt;  // U12
-                flops[3] += 8.0 * LB * mt * mt;
-            }
+            BEM_CUDA(cudaEventRecord(ev1, c.stream));
+            BEM_CUDA(cudaEventSynchronize(ev1));
+            float ms = 0;
+            BEM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+            tsum[l.kind == LuData::DIAG ? 0 : (l.kind == LuData::TRAIL ? 2 : 1)] += ms;
         }
     }
     if (c.profiling) {
-        const char* names[4] = {"lu_diag", "lu_l21_tf32", "lu_u12_tf32", "lu_gemm_tf32"};
-        for (int q = 0; q < 4; ++q) c.stage_add(names[q], tsum[q], d->nblk_max, flops[q]);
-        for (auto& e : ev) cudaEventDestroy(e);
+        // algorithmic work: 8 n^3 / 3 complex flop per factored operator
+        double fl = 0;
+        for (int s = 0; s < nsys; ++s)
+            if (owner[(size_t)s] == s) fl += 8.0 / 3.0 * std::pow((double)d->sys[(size_t)s].n, 3.0);
+        c.stage_add("lu_diag", tsum[0], d->nblk_max, 0);
+        c.stage_add("lu_panels", tsum[1], d->nblk_max, 0);
+        c.stage_add("lu_gemm_tf32", tsum[2], d->nblk_max, fl);
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
     }
     check_device_err(c);
     BEM_CUDA(cudaMemcpyAsync(&d->small_pivots, d->info.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
