@@ -128,88 +128,126 @@ __global__ void lu_round_kernel(const double2* __restrict__ A, size_t n, float2*
 }
 
 // ---------------------------------------------------------------------------
-// Diagonal block: LU without pivoting, then both triangular inverses in place.
-__global__ void __launch_bounds__(1024) lu_diag_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
-                                                       int k, int* __restrict__ small_pivots) {
-    extern __shared__ float2 T[];  // LB x LB, column-major: T[c * LB + r]
-    __shared__ float2 part[8][LB];
-    const LuSys S = sys[wl[blockIdx.x].sys];
-    const int64_t k0 = (int64_t)k * LB;
-    const int nb = (int)min((int64_t)LB, S.n - k0);
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int c = ty; c < nb; c += 32)
-        for (int r = tx; r < nb; r += 32) T[c * LB + r] = S.F[(k0 + c) * S.ld + k0 + r];
-    __syncthreads();
-    for (int j = 0; j < nb; ++j) {
-        float2 p = T[j * LB + j];
+// Diagonal block: LU without pivoting and both triangular inverses in one
+// elimination sweep.  Z starts as the block; at step j, with pivot p = Z[j][j],
+// column c_i = Z[i][j] and row r_c = Z[j][c]:
+//   Z[i][c] -= c_i r_c / p   for i != j, c != j, and (i > j or c > j)
+//   Z[i][j]  = -c_i / p (i > j),  c_i / p (i < j);   Z[j][c] = -r_c / p (c > j)
+//   Z[j][j]  = 1 / p
+// Entries with i > j and c > j follow the Schur complement, so c_i / p = L[i][j]
+// and r_c = U[j][c]; the strictly lower part then collects L^-1 by row
+// operations and the upper part U^-1 by column operations (the region i < j,
+// c < j is final).  On exit Z = L^-1 (strictly lower, unit diagonal implied)
+// + U^-1 (upper): the two inverses the triangular solves and panels use.
+// 256 threads, each holding a 4 x 16 tile of Z in registers (rows tx + 32a,
+// columns ty + 8b); one barrier per step.  The steps run in 16 groups of 8
+// columns, so the tile column (b = j / 8) and row (a = j / 32) of step j are
+// compile-time constants: the owners' stores take no register indexing, and
+// the final region i < j, c < j is skipped by whole tile blocks.
+constexpr int DIAG_THREADS = 256;
+
+template <int JB>
+__device__ __forceinline__ void lu_diag_group(float2 (&z)[4][16], int nb, int tx, int ty, float2 (*colbuf)[LB],
+                                              float2 (*rowbuf)[LB], int* __restrict__ small_pivots) {
+    constexpr int JA = JB / 4;
+#pragma unroll 1
+    for (int jc = 0; jc < 8; ++jc) {
+        const int j = 8 * JB + jc, jl = j & 31;
+        if (j >= nb) return;
+        float2* cb = colbuf[j & 1];
+        float2* rb = rowbuf[j & 1];
+        if (ty == jc)
+#pragma unroll
+            for (int a = 0; a < 4; ++a) cb[tx + 32 * a] = z[a][JB];
+        if (tx == jl)
+#pragma unroll
+            for (int b = 0; b < 16; ++b) rb[ty + 8 * b] = z[JA][b];
+        __syncthreads();  // (double-buffered: the next step writes the other pair)
+        float2 p = rb[j];
         float pn = p.x * p.x + p.y * p.y;
         const bool tiny = !(pn > 1e-30f);  // also catches NaN
         if (tiny) {
             p = make_float2(1e-15f, 0.f);
             pn = 1e-30f;
+            if (threadIdx.x == 0) atomicAdd(small_pivots, 1);
         }
-        const float2 inv = make_float2(p.x / pn, -p.y / pn);
-        __syncthreads();  // every thread has read the pivot
-        if (threadIdx.x == 0 && tiny) {
-            T[j * LB + j] = p;
-            atomicAdd(small_pivots, 1);
+        const float2 pinv = make_float2(p.x / pn, -p.y / pn);
+        // row multipliers c_i / p; row j takes 1 + 1/p, which turns its
+        // entries right of the pivot into -r_c / p through the same update
+        const bool below = tx > jl;  // row tx + 32 JA is below row j
+        float2 cvs[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            cvs[a] = cmulf(cb[tx + 32 * a], pinv);
+            if (a == JA && tx == jl) cvs[a] = make_float2(1.f + pinv.x, pinv.y);
         }
-        for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) T[j * LB + i] = cmulf(T[j * LB + i], inv);
-        __syncthreads();
-        for (int c = j + 1 + ty; c < nb; c += 32) {
-            const float2 u = T[c * LB + j];
-            for (int i = j + 1 + tx; i < nb; i += 32) {
-                float2 a = T[c * LB + i];
-                const float2 l = T[j * LB + i];
-                a.x -= l.x * u.x - l.y * u.y;
-                a.y -= l.x * u.y + l.y * u.x;
-                T[c * LB + i] = a;
+        const float2 cvb = below ? cvs[JA] : make_float2(0.f, 0.f);  // row JA, columns left of j
+#pragma unroll
+        for (int b = 0; b < 16; ++b) {
+            float2 r = rb[ty + 8 * b];
+            if (b == JB) {
+                const float2 hi = ty > jc ? r : make_float2(0.f, 0.f);  // columns right of j only
+                if (ty == jc) r = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    const float2 v = a < JA ? hi : (a > JA ? r : (below ? r : hi));
+                    cfmaf_(z[a][b], make_float2(-cvs[a].x, -cvs[a].y), v);
+                }
+            } else {
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    if (b < JB && a < JA) continue;  // final region
+                    const float2 m = (b < JB && a == JA) ? cvb : cvs[a];
+                    cfmaf_(z[a][b], make_float2(-m.x, -m.y), r);
+                }
             }
         }
-        __syncthreads();
-    }
-    const int row = threadIdx.x & (LB - 1), sub = threadIdx.x >> 7;  // 128 rows x 8 slices
-    // L^-1 (unit lower) in place, columns right to left:
-    //   Linv[i][j] = -(L[i][j] + sum_{j<p<i} Linv[i][p] L[p][j])
-    for (int j = nb - 2; j >= 0; --j) {
-        float2 acc = make_float2(0.f, 0.f);
-        if (row < nb)
-            for (int p = j + 1 + sub; p < row; p += 8) cfmaf_(acc, T[p * LB + row], T[j * LB + p]);
-        part[sub][row] = acc;
-        __syncthreads();
-        if (sub == 0 && row > j && row < nb) {
-            float2 s = T[j * LB + row];
-            for (int q = 0; q < 8; ++q) {
-                s.x += part[q][row].x;
-                s.y += part[q][row].y;
+        if (ty == jc)  // column j: -L[i][j] below, U^-1 entries above, 1/p on the diagonal
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const int r = tx + 32 * a;
+                z[a][JB] = r > j ? make_float2(-cvs[a].x, -cvs[a].y) : (r < j ? cvs[a] : pinv);
             }
-            T[j * LB + row] = make_float2(-s.x, -s.y);
-        }
-        __syncthreads();
     }
-    // U^-1 in place, columns left to right:
-    //   Uinv[i][j] = (delta_ij - sum_{i<=p<j} Uinv[i][p] U[p][j]) / U[j][j]
-    for (int j = 0; j < nb; ++j) {
-        const float2 d = T[j * LB + j];
-        const float dn = d.x * d.x + d.y * d.y;
-        const float2 dinv = make_float2(d.x / dn, -d.y / dn);
-        float2 acc = make_float2(0.f, 0.f);
-        if (row < j)
-            for (int p = row + sub; p < j; p += 8) cfmaf_(acc, T[p * LB + row], T[j * LB + p]);
-        part[sub][row] = acc;
-        __syncthreads();
-        if (sub == 0 && row <= j) {
-            float2 s = make_float2(row == j ? 1.f : 0.f, 0.f);
-            for (int q = 0; q < 8; ++q) {
-                s.x -= part[q][row].x;
-                s.y -= part[q][row].y;
-            }
-            T[j * LB + row] = cmulf(s, dinv);
-        }
-        __syncthreads();
+}
+
+template <int JB>
+__device__ __forceinline__ void lu_diag_sweep(float2 (&z)[4][16], int nb, int tx, int ty, float2 (*colbuf)[LB],
+                                              float2 (*rowbuf)[LB], int* __restrict__ small_pivots) {
+    if constexpr (JB < LB / 8) {
+        lu_diag_group<JB>(z, nb, tx, ty, colbuf, rowbuf, small_pivots);
+        lu_diag_sweep<JB + 1>(z, nb, tx, ty, colbuf, rowbuf, small_pivots);
     }
+}
+
+__global__ void __launch_bounds__(DIAG_THREADS) lu_diag_kernel(const LuSys* __restrict__ sys,
+                                                               const LuWork* __restrict__ wl, int k,
+                                                               int* __restrict__ small_pivots) {
+    extern __shared__ float2 T[];  // LB x LB, column-major: T[c * LB + r]
+    __shared__ float2 colbuf[2][LB], rowbuf[2][LB];
+    const LuSys S = sys[wl[blockIdx.x].sys];
+    const int64_t k0 = (int64_t)k * LB;
+    const int nb = (int)min((int64_t)LB, S.n - k0);
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    float2 z[4][16];
+#pragma unroll
+    for (int b = 0; b < 16; ++b) {
+        const int c = ty + 8 * b;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int r = tx + 32 * a;
+            // outside the block: identity, untouched by the sweep over j < nb
+            z[a][b] = (r < nb && c < nb) ? S.F[(k0 + c) * S.ld + k0 + r] : make_float2(r == c ? 1.f : 0.f, 0.f);
+        }
+    }
+    lu_diag_sweep<0>(z, nb, tx, ty, colbuf, rowbuf, small_pivots);
+#pragma unroll
+    for (int b = 0; b < 16; ++b)
+#pragma unroll
+        for (int a = 0; a < 4; ++a) T[(ty + 8 * b) * LB + tx + 32 * a] = z[a][b];
+    __syncthreads();
     float2* Dk = S.Dm + (size_t)k * LB * LB;
-    for (int c = ty; c < nb; c += 32)
+    for (int c = ty; c < nb; c += DIAG_THREADS / 32)
         for (int r = tx; r < nb; r += 32) Dk[c * LB + r] = T[c * LB + r];
     if (nb < LB || S.n <= k0 + LB) return;  // no panels after the last block
     // real embeddings for the panel GEMMs: Li = [[re, -im], [im, re]] of
@@ -960,7 +998,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         if (c.profiling) BEM_CUDA(cudaEventRecord(ev0, c.stream));
         switch (l.kind) {
             case LuData::DIAG:
-                lu_diag_kernel<<<(unsigned)sg.ctas, 1024, diag_smem, c.stream>>>(sys, wk + sg.off, l.ks,
+                lu_diag_kernel<<<(unsigned)sg.ctas, DIAG_THREADS, diag_smem, c.stream>>>(sys, wk + sg.off, l.ks,
                                                                                  d->info.as<int>());
                 break;
             case LuData::EXPAND:
