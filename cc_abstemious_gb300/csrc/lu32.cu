@@ -594,113 +594,174 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
 }
 
 // ---------------------------------------------------------------------------
-// Preconditioner application.  Forward: z = q, then for every block step
-// z_b -= L_bk z_k below block k, the block k + 1 finishing with
-// z_{k+1} = L^-1_{k+1} z_{k+1}.  Backward likewise with the U blocks above.
-// The substitutions run in FP32 (the factors are TF32-accurate; FP64 would
-// only slow them down on this part): z[0..nr) <- T z with T the lower (unit)
-// or upper part of a kept inverse tile.
-__device__ void lu_apply_inverse(const float2* __restrict__ Dk, int nr, bool lower, double2* __restrict__ z,
-                                 float2* xs, float2 (*red)[LB]) {
-    const int row = threadIdx.x & (LB - 1), half = threadIdx.x >> 7;
-    if (half == 0) {
-        const double2 v = row < nr ? z[row] : make_double2(0, 0);
-        xs[row] = make_float2((float)v.x, (float)v.y);
+// Preconditioner application z = U^-1 L^-1 q: both block substitutions in one
+// launch.  A ticket is one block row of one system in one direction:
+//   forward  row b:  y = q_b - sum_{k<b} L_bk z_k,    z_b = y + (L_bb^-1 - I) y
+//   backward row b:  w = z_b - sum_{k>b} U_bk z_k,    z_b = U_bb^-1 w
+// CTAs take tickets from a counter in an order where every row a ticket
+// depends on has a smaller ticket (forward rows by b, then backward rows by
+// descending b, systems interleaved), so a CTA only waits for rows that CTAs
+// already running hold.  A finished row publishes its flag; a set flag also
+// says every row it depended on is final, so a row polls only when it reaches
+// blocks past the last flag it saw.  Waits are bounded (error flag, then the
+// row carries on).  Block products run in FP32 (TF32-accurate factors),
+// accumulated over blocks in FP64.
+struct LuTicket {
+    int sys, phase, row, flags;  // flags: the system's forward flags, then its backward flags
+};
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Thread 0 waits (bounded) until flag f is set.
+__device__ __forceinline__ void lu_wait_flag(const int* f, int* err) {
+    for (uint32_t it = 0; it < (1u << 24); ++it) {
+        if (ld_acquire_gpu(f)) return;
+        __nanosleep(100);
     }
-    __syncthreads();
-    float2 acc = make_float2(0.f, 0.f);
-    if (row < nr) {
-        const int p0 = half * (LB / 2), p1 = min(p0 + LB / 2, nr);
-        for (int p = p0; p < p1; ++p) {
-            const bool use = lower ? (p < row) : (p >= row);
-            if (use) cfmaf_(acc, Dk[p * LB + row], xs[p]);
+    atomicOr(err, DEVERR_BARRIER_TIMEOUT);
+}
+
+constexpr int TS_THREADS = 256;  // 64 row pairs x 4 column quarters of a block
+
+// acc += B v for the row pair of this thread over its 32-column quarter of a
+// block: B's columns at col (stride ld, float2 entries), v in shared memory.
+__device__ __forceinline__ void lu_block_mv(const float2* __restrict__ col, int64_t ld, const float2* v, int c0,
+                                            int nc, bool rows_ok, double2 (&acc)[2]) {
+    float2 a0 = make_float2(0.f, 0.f), a1 = a0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float4 e[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int c = c0 + 16 * h + i;
+            e[i] = rows_ok && c < nc ? __ldg(reinterpret_cast<const float4*>(col + (int64_t)c * ld))
+                                     : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const float2 x = v[c0 + 16 * h + i];
+            cfmaf_(a0, make_float2(e[i].x, e[i].y), x);
+            cfmaf_(a1, make_float2(e[i].z, e[i].w), x);
         }
     }
-    red[half][row] = acc;
-    __syncthreads();
-    if (half == 0 && row < nr) {
-        float2 v = make_float2(red[0][row].x + red[1][row].x, red[0][row].y + red[1][row].y);
-        if (lower) v = make_float2(v.x + xs[row].x, v.y + xs[row].y);  // unit diagonal
-        z[row] = make_double2(v.x, v.y);
-    }
-    __syncthreads();
+    acc[0].x += a0.x;
+    acc[0].y += a0.y;
+    acc[1].x += a1.x;
+    acc[1].y += a1.y;
 }
 
-// z[r0 .. r0+nr) -= B x, B the nr x nc block of F at (r0, c0).
-__device__ void lu_block_update(const LuSys& S, int64_t r0, int nr, int64_t c0, int nc, const double2* __restrict__ x,
-                                double2* __restrict__ z, float2* xs, float2 (*red)[LB]) {
-    const int row = threadIdx.x & (LB - 1), half = threadIdx.x >> 7;
-    if (half == 0) {
-        const double2 v = row < nc ? x[row] : make_double2(0, 0);
-        xs[row] = make_float2((float)v.x, (float)v.y);
-    }
-    __syncthreads();
-    float2 acc = make_float2(0.f, 0.f);
-    if (row < nr) {
-        const int p0 = half * (LB / 2), p1 = min(p0 + LB / 2, nc);
-        const float2* col = S.F + (c0 + p0) * S.ld + r0 + row;
-#pragma unroll 8
-        for (int p = p0; p < p1; ++p, col += S.ld) cfmaf_(acc, *col, xs[p]);
-    }
-    red[half][row] = acc;
-    __syncthreads();
-    if (half == 0 && row < nr) {
-        double2 v = z[r0 + row];
-        v.x -= (double)(red[0][row].x + red[1][row].x);
-        v.y -= (double)(red[0][row].y + red[1][row].y);
-        z[r0 + row] = v;
-    }
-    __syncthreads();
-}
-
-__global__ void __launch_bounds__(256) lu_fwd_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
-                                                     int nw, int k, GmBatch bt) {
+__global__ void __launch_bounds__(TS_THREADS) lu_trsv_kernel(const LuSys* __restrict__ sys,
+                                                             const LuTicket* __restrict__ tickets, int ntickets,
+                                                             int* __restrict__ counter, int* __restrict__ flags,
+                                                             GmBatch bt, int* __restrict__ err) {
     __shared__ float2 xs[LB];
-    __shared__ float2 red[2][LB];
-    int64_t local;
-    const int s = lu_locate(wl, nw, blockIdx.x, local);
-    const GmState& st = bt.st[s];
-    if (!gm_apply_active(bt, st, MV_Q)) return;
-    const LuSys S = sys[s];
-    const GmView g = gm_view(bt, s);
-    const double2* q = bt.Q + g.q + (size_t)st.k * g.n;
-    double2* z = bt.Z + g.q + (size_t)st.k * g.n;
-    if (k < 0) {
-        // z = q for block b; block 0 then z_0 = L^-1_0 z_0
-        const int64_t b = local, r0 = b * LB;
-        const int nr = (int)min((int64_t)LB, S.n - r0);
-        for (int r = threadIdx.x; r < nr; r += blockDim.x) z[r0 + r] = q[r0 + r];
+    __shared__ double2 red[4][LB];
+    __shared__ double2 ys[LB];
+    __shared__ int tk, all_final;
+    const int rp = threadIdx.x & 63, cq = threadIdx.x >> 6;
+    for (;;) {
+        if (threadIdx.x == 0) tk = atomicAdd(counter, 1);
         __syncthreads();
-        if (b == 0) lu_apply_inverse(S.Dm, nr, true, z, xs, red);
-        return;
+        const int t = tk;
+        __syncthreads();  // every thread has read tk
+        if (t >= ntickets) return;
+        const LuTicket T = tickets[t];
+        const GmState& st = bt.st[T.sys];
+        if (!gm_apply_active(bt, st, MV_Q)) continue;
+        const LuSys S = sys[T.sys];
+        const GmView g = gm_view(bt, T.sys);
+        double2* z = bt.Z + g.q + (size_t)st.k * g.n;
+        const int b = T.row, nblk = S.nblk;
+        const int nr = (int)min((int64_t)LB, S.n - (int64_t)b * LB);
+        const bool rows_ok = 2 * rp < nr;  // nr is even or the block's last
+        const bool fwd = T.phase == 0;
+        int* fl = flags + T.flags + (fwd ? 0 : nblk);
+        double2 acc[2] = {make_double2(0, 0), make_double2(0, 0)};
+        // blocks of the row, in the order their values become final
+        const int nk = fwd ? b : nblk - 1 - b;
+        int seen = 0;  // blocks known final
+        if (!fwd && threadIdx.x == 0) lu_wait_flag(flags + T.flags + nblk - 1, err);  // forward done
+        __syncthreads();
+        for (int i = 0; i < nk; ++i) {
+            const int k = fwd ? i : nblk - 1 - i;
+            if (i >= seen) {
+                if (threadIdx.x == 0) {
+                    // the row's last dependency first: once set, all are
+                    const int ok = ld_acquire_gpu(fl + (fwd ? b - 1 : b + 1));
+                    if (!ok) lu_wait_flag(fl + k, err);
+                    all_final = ok;
+                }
+                __syncthreads();
+                seen = all_final ? nk : i + 1;
+            }
+            const int nc = (int)min((int64_t)LB, S.n - (int64_t)k * LB);
+            if (threadIdx.x < LB) {
+                const double2 v = threadIdx.x < nc ? __ldcg(z + (int64_t)k * LB + threadIdx.x) : make_double2(0, 0);
+                xs[threadIdx.x] = make_float2((float)v.x, (float)v.y);
+            }
+            __syncthreads();
+            const float2* col = S.F + (int64_t)k * LB * S.ld + (int64_t)b * LB + 2 * rp;
+            lu_block_mv(col, S.ld, xs, 32 * cq, nc, rows_ok, acc);
+            __syncthreads();  // xs reused by the next block
+        }
+        red[cq][2 * rp] = acc[0];
+        red[cq][2 * rp + 1] = acc[1];
+        __syncthreads();
+        const double2* src = fwd ? bt.Q + g.q + (size_t)st.k * g.n : z;
+        if (threadIdx.x < LB) {
+            const int r = threadIdx.x;
+            double2 y = make_double2(0, 0);
+            if (r < nr) {
+                y = fwd ? src[(int64_t)b * LB + r] : __ldcg(src + (int64_t)b * LB + r);
+                for (int q = 0; q < 4; ++q) {
+                    y.x -= red[q][r].x;
+                    y.y -= red[q][r].y;
+                }
+            }
+            ys[r] = y;
+            xs[r] = make_float2((float)y.x, (float)y.y);
+        }
+        __syncthreads();
+        // diagonal block: strictly lower part of L_bb^-1 (unit diagonal
+        // added in FP64) or the upper part of U_bb^-1 with its diagonal
+        {
+            const float2* D = S.Dm + (size_t)b * LB * LB;
+            const int r0 = 2 * rp;
+            float2 a0 = make_float2(0.f, 0.f), a1 = a0;
+#pragma unroll 8
+            for (int i = 0; i < 32; ++i) {
+                const int c = 32 * cq + i;
+                if (!rows_ok || c >= nr) continue;
+                const float4 e = __ldg(reinterpret_cast<const float4*>(D + (size_t)c * LB + r0));
+                const float2 x = xs[c];
+                const bool u0 = fwd ? c < r0 : c >= r0, u1 = fwd ? c < r0 + 1 : c >= r0 + 1;
+                if (u0) cfmaf_(a0, make_float2(e.x, e.y), x);
+                if (u1) cfmaf_(a1, make_float2(e.z, e.w), x);
+            }
+            red[cq][r0] = make_double2(a0.x, a0.y);
+            red[cq][r0 + 1] = make_double2(a1.x, a1.y);
+        }
+        __syncthreads();
+        if (threadIdx.x < LB && threadIdx.x < nr) {
+            const int r = threadIdx.x;
+            double2 v = fwd ? ys[r] : make_double2(0, 0);
+            for (int q = 0; q < 4; ++q) {
+                v.x += red[q][r].x;
+                v.y += red[q][r].y;
+            }
+            __stcg(z + (int64_t)b * LB + r, v);
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) st_release_gpu(fl + b, 1);
     }
-    const int64_t b = k + 1 + local, r0 = b * LB;
-    const int nr = (int)min((int64_t)LB, S.n - r0);
-    lu_block_update(S, r0, nr, (int64_t)k * LB, LB, z + (int64_t)k * LB, z, xs, red);
-    if (b == k + 1) lu_apply_inverse(S.Dm + (size_t)b * LB * LB, nr, true, z + r0, xs, red);
-}
-
-__global__ void __launch_bounds__(256) lu_bwd_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
-                                                     int nw, int t, GmBatch bt) {
-    __shared__ float2 xs[LB];
-    __shared__ float2 red[2][LB];
-    int64_t local;
-    const int s = lu_locate(wl, nw, blockIdx.x, local);
-    const GmState& st = bt.st[s];
-    if (!gm_apply_active(bt, st, MV_Q)) return;
-    const LuSys S = sys[s];
-    const GmView g = gm_view(bt, s);
-    double2* z = bt.Z + g.q + (size_t)st.k * g.n;
-    if (t == 0) {
-        const int64_t b = S.nblk - 1, r0 = b * LB;
-        lu_apply_inverse(S.Dm + (size_t)b * LB * LB, (int)(S.n - r0), false, z + r0, xs, red);
-        return;
-    }
-    const int64_t kk = S.nblk - t;  // block solved by the previous launch
-    const int64_t b = local, r0 = b * LB, c0 = kk * LB;
-    const int nc = (int)min((int64_t)LB, S.n - c0);
-    lu_block_update(S, r0, LB, c0, nc, z + c0, z, xs, red);
-    if (b == kk - 1) lu_apply_inverse(S.Dm + (size_t)b * LB * LB, LB, false, z + r0, xs, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -722,7 +783,9 @@ struct LuData {
         Seg seg;
     };
     std::vector<Launch> plan;
-    std::vector<Seg> fwd, bwd;
+    // preconditioner application: tickets, and a counter + row flags
+    DevBuf tickets, flags;
+    int ntickets = 0, nflags = 0, trsv_grid = 1;
     std::vector<LuWork> host;
     int small_pivots = 0;
 };
@@ -765,20 +828,12 @@ Entry trail_entry(int s, int64_t r0, int64_t r1, int64_t c0, int64_t c1) {
 void lu_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
     (void)mode;
     LuData& d = *static_cast<LuData*>(user);
-    const LuSys* sys = d.sysbuf.as<LuSys>();
-    const LuWork* wk = d.work.as<LuWork>();
-    for (int i = 0; i < (int)d.fwd.size(); ++i) {
-        const auto& sg = d.fwd[(size_t)i];
-        if (!sg.ctas) continue;
-        lu_fwd_kernel<<<(unsigned)sg.ctas, 256, 0, c.stream>>>(sys, wk + sg.off, sg.count, i - 1, ws.bt);
-        BEM_CHECK_LAUNCH(&c);
-    }
-    for (int i = 0; i < (int)d.bwd.size(); ++i) {
-        const auto& sg = d.bwd[(size_t)i];
-        if (!sg.ctas) continue;
-        lu_bwd_kernel<<<(unsigned)sg.ctas, 256, 0, c.stream>>>(sys, wk + sg.off, sg.count, i, ws.bt);
-        BEM_CHECK_LAUNCH(&c);
-    }
+    if (!d.ntickets) return;
+    BEM_CUDA(cudaMemsetAsync(d.flags.p, 0, sizeof(int) * (size_t)d.nflags, c.stream));
+    int* f = d.flags.as<int>();
+    lu_trsv_kernel<<<(unsigned)d.trsv_grid, TS_THREADS, 0, c.stream>>>(
+        d.sysbuf.as<LuSys>(), d.tickets.as<LuTicket>(), d.ntickets, f, f, ws.bt, device_err(c));
+    BEM_CHECK_LAUNCH(&c);
 }
 
 }  // namespace
@@ -950,21 +1005,32 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         plan(LuData::COPY, k + 1, k, 0, 2 * LB, 0, copy1);
         plan(LuData::TRAIL, k + 1, k, 0, 0, 2 * GCHUNKS, trail1);
     }
-    for (int k = -1; k < d->nblk_max - 1; ++k) {
-        std::vector<std::pair<int, int64_t>> e;
+    // substitution tickets: forward rows by ascending block, then backward
+    // rows by descending block, the systems interleaved
+    {
+        std::vector<int> fo((size_t)nsys);
+        int nf = 1;  // [0] is the ticket counter
         for (int s = 0; s < nsys; ++s) {
-            const LuSys& L = d->sys[(size_t)s];
-            e.push_back({s, k < 0 ? (int64_t)L.nblk : (int64_t)std::max(0, L.nblk - k - 1)});
+            fo[(size_t)s] = nf;
+            nf += 2 * d->sys[(size_t)s].nblk;
         }
-        d->fwd.push_back(add_segment(*d, e));
-    }
-    for (int t = 0; t < d->nblk_max; ++t) {
-        std::vector<std::pair<int, int64_t>> e;
-        for (int s = 0; s < nsys; ++s) {
-            const LuSys& L = d->sys[(size_t)s];
-            e.push_back({s, t == 0 ? 1 : (int64_t)std::max(0, L.nblk - t)});
-        }
-        d->bwd.push_back(add_segment(*d, e));
+        std::vector<LuTicket> tk;
+        for (int ph = 0; ph < 2; ++ph)
+            for (int t = 0; t < d->nblk_max; ++t)
+                for (int s = 0; s < nsys; ++s) {
+                    const int nb = d->sys[(size_t)s].nblk;
+                    if (t < nb) tk.push_back(LuTicket{s, ph, ph == 0 ? t : nb - 1 - t, fo[(size_t)s]});
+                }
+        d->ntickets = (int)tk.size();
+        d->nflags = nf;
+        d->tickets.ensure(sizeof(LuTicket) * std::max<size_t>(tk.size(), 1));
+        d->flags.ensure(sizeof(int) * (size_t)nf);
+        BEM_CUDA(cudaMemcpyAsync(d->tickets.p, tk.data(), sizeof(LuTicket) * tk.size(), cudaMemcpyHostToDevice,
+                                 c.stream));
+        int per_sm = 1, nsm_ = 0;
+        BEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lu_trsv_kernel, TS_THREADS, 0));
+        BEM_CUDA(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, c.device));
+        d->trsv_grid = std::max(1, std::min(d->ntickets, std::max(1, per_sm) * nsm_));
     }
     d->sysbuf.ensure(sizeof(LuSys) * nsys);
     d->work.ensure(sizeof(LuWork) * std::max<size_t>(d->host.size(), 1));
