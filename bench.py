@@ -157,6 +157,80 @@ def ncu_traffic_ratio():
     return None
 
 
+def tf32_peak():
+    """cuBLAS TF32 GEMM throughput measured in this run (8192^3, best of 5,
+    CUDA events): the denominator for the TF32 tensor-core LU update, since the
+    measured peaks file covers HBM and BF16 only."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    n = 8192
+    a = torch.randn(n, n, device="cuda")
+    b = torch.randn(n, n, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = float("inf")
+    for i in range(7):
+        e0.record()
+        c = a @ b
+        e1.record()
+        e1.synchronize()
+        if i >= 2:
+            best = min(best, e0.elapsed_time(e1))
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b, c
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def lu_traffic_ratio():
+    """DRAM traffic / algorithmic A22 bytes of one K = 512 trailing update, from
+    the committed ncu summary (profiles/)."""
+    p = os.path.join(ROOT, "profiles", "lu_gemm_tf32_pair_rigid_sphere.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_over_algorithmic:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def lu_roofline(prof, sizes, what):
+    """Roofline entry of the LU preconditioner's trailing update (the dominant
+    kernel of the LU forms): TF32 flop rate of the lu_gemm launches (event-timed
+    by the library's profiling pass; 8 n^3 / 3 complex flop per factored
+    operator) against cuBLAS TF32 measured here.  Block steps run in pairs:
+    one K = 512 launch per pair reads and writes the trailing block once, so its
+    algorithmic bytes are 16 B (FP32 complex, read + write) per trailing entry
+    (reported per operator: a launch covers every operator of a frequency
+    chunk)."""
+    lu = prof.get("lu_gemm_tf32", {})
+    achieved = lu["bytes"] / (lu["ms"] * 1e-3) / 1e12 if lu.get("ms") else None
+    peak = tf32_peak()
+    lb = 128
+    tot, cnt = 0.0, 0
+    for n in sizes:
+        nblk = (n + lb - 1) // lb
+        for k in range(0, nblk, 2):
+            m1 = n - (k + 2) * lb
+            if m1 > 0:
+                tot += 16.0 * m1 * m1
+                cnt += 1
+    alg = tot / cnt if cnt else None
+    ratio = lu_traffic_ratio()
+    return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak if achieved else None,
+            "traffic": ratio * alg if (ratio and alg) else None,
+            "kernel": "lu_gemm_kernel<TRAIL> (TF32 tcgen05 trailing update of the LU preconditioner, " + what + ")",
+            "algorithmic_bytes_per_operator_launch": alg,
+            "peak_kind": "measured in this run (cuBLAS TF32 GEMM 8192^3, burst)",
+            "traffic_note": "ncu dram read+write / algorithmic A22 bytes of one K = 512 launch "
+                            "(profiles/lu_gemm_tf32_pair_rigid_sphere.md), times the mean algorithmic bytes "
+                            "of this workload's K = 512 launches, per operator"}
+
+
 def cpu_reference(inp, nfreq_sample, threads):
     """The oracle (C restatement of the reference algorithm) on `nfreq_sample`
     frequencies of the workload; returns (solves/s, seconds, sample text)."""
@@ -494,7 +568,10 @@ def bench_perturbed_spheres(args):
     bem.run_batch(pds, precond=pc, ctx=ctx)
     prof = ctx.profile()
     ctx.set_profiling(False)
-    roofline = _roofline_from_profile(prof, "ragged batch over all bodies and frequencies")
+    if pc == "lu":
+        roofline = lu_roofline(prof, list(ns), "ragged batch over all bodies and frequencies")
+    else:
+        roofline = _roofline_from_profile(prof, "ragged batch over all bodies and frequencies")
 
     threads = max((os.cpu_count() or 2) // 2, 2)
     mid = int(order[len(order) // 2])
@@ -502,7 +579,8 @@ def bench_perturbed_spheres(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32 operator / fp64 vectors (complex)",
+        "vs_baseline": None,
+        "dtype": "fp32 operator / fp64 vectors (complex)" + ("; tf32 LU preconditioner" if pc == "lu" else ""),
         "data": "synthetic (seeded harmonic-perturbed spheres, no dataset)",
         "config": {"workload": "perturbed_spheres", "bodies": len(pds), "frequencies_per_body": 8,
                    "systems": nsys, "n_min": int(min(ns)), "n_max": int(max(ns)), "n_mean": float(np.mean(ns)),
@@ -568,8 +646,10 @@ def bench_held_out_learned(args):
         def step():
             ctx.check(ctx.lib.bem_run(ctx.h, pd.h, form, code, bem._ptr(sc), bem._ptr(inc), reps, 0))
 
+        launches0 = ctx.kernel_launches
         ms, clk = _timed_region(args, local, step, stream)
-        results[name] = {"value": nf * 1000.0 / ms, "ms_per_step": ms, "clocks": clk,
+        launches = (ctx.kernel_launches - launches0) * args.steps // (args.steps + max(args.warmup, 3))
+        results[name] = {"value": nf * 1000.0 / ms, "ms_per_step": ms, "clocks": clk, "gpu_launches": launches,
                          "iterations": [reps[i].iterations for i in range(nf)],
                          "converged": all(reps[i].flag == 1 for i in range(nf)),
                          "precond_used": [reps[i].precond for i in range(nf)]}
@@ -615,10 +695,34 @@ def bench_held_out_learned(args):
     prof = ctx.profile()
     ctx.set_profiling(False)
     value = results[best]["value"]
+    # end to end through the public API (JSON text + mesh file on the host ->
+    # results on the host), the headline form
+    text = json.dumps(held)
+    fname = {bem.FORM_MIXED: "mixed", bem.FORM_REFINED: "refined"}[form_best]
+    pname = {0: None, 1: "block_jacobi", 2: "learned", 3: "lu"}[code_best]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        a = bem.Analysis(ctx)
+        a.input_from_string(text)
+        a.run(form=fname, precond=pname)
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    if code_best == 3:
+        roofline = lu_roofline(prof, [pd.n], "12 frequencies of the held-out body, " + best)
+    else:
+        roofline = _roofline_from_profile(prof, "12 frequencies of the held-out body, " + best)
+    # CPU baseline: the oracle on one frequency of a smaller body of the same
+    # distribution (its dense FP64 LU of 20000 unknowns is not a bounded sample)
+    threads = max((os.cpu_count() or 2) // 2, 2)
+    small = workloads.perturbed_sphere_input(workdir, 777777, 2000, kas, tol=1e-8)
+    cv, cdt, sample = cpu_reference(small, 1, threads)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": results[best]["ms_per_step"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "fp32 operator / fp64 vectors (complex); bf16 network",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": ("fp64 operator / tf32 LU preconditioner (complex)" if form_best == bem.FORM_REFINED else
+                  "fp32 operator / fp64 vectors (complex)" + ("; tf32 LU preconditioner" if code_best == 3 else
+                                                             "; bf16 network" if code_best == 2 else "")),
         "data": "synthetic (seeded harmonic-perturbed spheres, no dataset)",
         "config": {"workload": "held_out_learned", "n_unknowns": pd.n, "frequencies": nf, "ka": [4.0, 16.0],
                    "solver": "GMRES tol 1e-8 (backward error; 1e-6 leaves ~1.3e-6 forward error)",
@@ -632,7 +736,13 @@ def bench_held_out_learned(args):
         "clocks": results[best]["clocks"], "by_precond": results, "plain_fp64": plain,
         "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
         "rel_err_vs_fp64_lu": errs, "max_rel_err_vs_fp64_lu": max(errs.values()),
-        "roofline": _roofline_from_profile(prof, "12 frequencies of the held-out body, " + best),
+        "e2e": {"value": world * nf * 1000.0 / e2e_ms, "unit": UNIT,
+                "h2d_bytes_per_step": 8 * 3 * pd.info["mesh_nodes"] + 8 * 5 * pd.n + 8 * 3 * pd.nfp,
+                "d2h_bytes_per_step": 16 * 2 * nf * pd.nfp, "note": "JSON text + VTK file on host -> results on host"},
+        "gpu_launches": results[best]["gpu_launches"],
+        "roofline": roofline,
+        "cpu_baseline": {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample + "; a 2000-triangle body of the same distribution and seed"},
         "stages_ms": {k: v["ms"] for k, v in prof.items()},
     }
     if rank == 0:
@@ -754,11 +864,7 @@ def bench_ellipsoid(args):
                               (bem.SolveReport * (R * nf))(), 0))
     prof = ctx.profile()
     ctx.set_profiling(False)
-    lu = prof.get("lu_gemm_tf32", {})
-    roofline = {"bound": "hbm", "kernel": "lu_gemm_kernel (TF32 tcgen05 trailing update, A22 read+write bound)",
-                "achieved_tflops": lu["bytes"] / (lu["ms"] * 1e-3) / 1e12 if lu.get("ms") else None,
-                "unit": "TFLOP/s", "note": "the dominant kernel of this workload; its DRAM-bound ceiling at "
-                                           "block size 128 is ~440 TFLOP/s (256 flop per 8 B of A22)"}
+    roofline = lu_roofline(prof, [pds[0].n], "8 frequencies of the 40960-unknown ellipsoid")
     threads = max((os.cpu_count() or 2) // 2, 2)
     coarse = workloads.ellipsoid_bm(workdir, n_lon=64, n_bands=21)[0]
     cv, cdt, sample = cpu_reference(coarse, 1, threads)
