@@ -86,7 +86,8 @@ __device__ __forceinline__ void phase32(float kh, float kl, float rh, float rl, 
     else if (quad == 3) { c0 = sn; s0 = -cs; }
 }
 
-// r = |a - b| for float-float points: returns (d_hi components, r hi/lo, 1/r).
+// r = |a - b| for float-float points: returns (the separation rounded to
+// FP32, r hi/lo, 1/r).
 struct Sep32 {
     float dx, dy, dz, rh, rl, inv;
 };
@@ -104,11 +105,17 @@ __device__ __forceinline__ Sep32 separation32(float axh, float axl, float ayh, f
     float r2l = (e1 + e2) + (ex + ey + ez) + 2.0f * (dxh * dxl + dyh * dyl + dzh * dzl);
     Sep32 o;
     o.rh = sqrtf(s2);
-    o.inv = 1.0f / o.rh;
-    o.rl = (fmaf(-o.rh, o.rh, s2) + r2l) * (0.5f * o.inv);
-    o.dx = dxh;
-    o.dy = dyh;
-    o.dz = dzh;
+    o.rl = (fmaf(-o.rh, o.rh, s2) + r2l) * (0.5f / o.rh);
+    // 1/r from r rounded once: s2 holds the squares of the hi parts only, off
+    // by ~1e-6 between neighbouring elements (the near-field terms carry 1/r
+    // up to the third power)
+    o.inv = 1.0f / (o.rh + o.rl);
+    // the direction uses the separation rounded once (hi + lo): the hi parts
+    // alone are off by the coordinates' rounding, which is ~1e-6 of the
+    // separation of neighbouring elements
+    o.dx = dxh + dxl;
+    o.dy = dyh + dyl;
+    o.dz = dzh + dzl;
     return o;
 }
 
