@@ -754,12 +754,13 @@ def bench_ellipsoid(args):
     along a seeded direction and a point source at (0, 0, 3), 8 frequencies with
     ka (a = 2) 2.5..20: 16 solves per step.  The input asks for the H-matrix
     solver at tolerance 1e-6; the forms measured here solve the dense operators
-    (8 x 40960^2) with the TF32 LU preconditioner.  FP32 operators (mixed form)
-    miss 1e-6 on this body (~2e-6), so the headline is the refined form (FP64
-    operators) at backward error 1e-8.  The error reference is the same FP64
-    operator solved to backward error 1e-12 (a dense FP64 LU of 40960 unknowns
-    per frequency is too slow for a benchmark; the refined form is checked
-    against FP64 LU at smaller sizes in the tests)."""
+    (8 x 40960^2) with the TF32 LU preconditioner, at backward error 1e-8: the
+    mixed form (FP32 operators) and the refined form (FP64 operators) are both
+    timed and the headline is the faster one whose every solve is within 1e-6.
+    The error reference is the same FP64 operator solved to backward error
+    1e-12 (a dense FP64 LU of 40960 unknowns per frequency is too slow for a
+    benchmark; both forms are checked against FP64 LU at smaller sizes in the
+    tests)."""
     import numpy as np
     import torch
     import cc_abstemious_gb300 as bem
@@ -800,20 +801,18 @@ def bench_ellipsoid(args):
     outs = [out2[:nf], out2[nf:]]
     reps = [[reps2[i] for i in range(nf)], [reps2[nf + i] for i in range(nf)]]
 
-    launches0 = ctx.kernel_launches
-    ms, clk = _timed_region(args, local, step, stream)
-    gpu_launches = (ctx.kernel_launches - launches0) * args.steps // (args.steps + max(args.warmup, 3))
-    value = world * nsolve * 1000.0 / ms
-    iters = [reps2[i].iterations for i in range(R * nf)]
-    refined_fields = [o.copy() for o in outs]
-
-    # mixed form (FP32 operators), one step, for comparison
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    step(bem.FORM_MIXED)
-    torch.cuda.synchronize()
-    mixed_ms = (time.perf_counter() - t0) * 1000.0
-    mixed_fields = [o.copy() for o in outs]
+    # both forms timed: refined (FP64 operators) and mixed (FP32 operators)
+    timed = {}
+    for fname, form in (("refined", bem.FORM_REFINED), ("mixed", bem.FORM_MIXED)):
+        launches0 = ctx.kernel_launches
+        fms, fclk = _timed_region(args, local, lambda: step(form), stream)
+        timed[fname] = {"ms": fms, "clocks": fclk,
+                        "gpu_launches": (ctx.kernel_launches - launches0) * args.steps //
+                                        (args.steps + max(args.warmup, 3)),
+                        "iterations": [reps2[i].iterations for i in range(R * nf)],
+                        "fields": [o.copy() for o in outs]}
+    refined_fields = timed["refined"]["fields"]
+    mixed_fields = timed["mixed"]["fields"]
 
     # reference: the FP64 operators solved to backward error 1e-12, each wave
     # as its own input
@@ -831,6 +830,13 @@ def bench_ellipsoid(args):
 
     err_refined = rel(refined_fields[0], ref_fields[0]) + rel(refined_fields[1], ref_fields[1])
     err_mixed = rel(mixed_fields[0], ref_fields[0]) + rel(mixed_fields[1], ref_fields[1])
+    # the headline: the faster form whose every solve is within 1e-6
+    best = "mixed" if (max(err_mixed) <= 1e-6 and timed["mixed"]["ms"] < timed["refined"]["ms"]) else "refined"
+    ms, clk = timed[best]["ms"], timed[best]["clocks"]
+    gpu_launches = timed[best]["gpu_launches"]
+    iters = timed[best]["iterations"]
+    value = world * nsolve * 1000.0 / ms
+    errs_best = err_mixed if best == "mixed" else err_refined
 
     # end to end through the public API (JSON text + mesh file on the host)
     torch.cuda.synchronize()
@@ -838,7 +844,7 @@ def bench_ellipsoid(args):
     for t in texts:
         a = bem.Analysis(ctx)
         a.input_from_string(t)
-        a.run(form="refined", precond="lu")
+        a.run(form=best, precond="lu")
     e2e_ms = (time.perf_counter() - t0) * 1000.0
 
     # plain FP64 drop-in form (the reference's H-matrix solver), plane wave only
@@ -860,8 +866,8 @@ def bench_ellipsoid(args):
         del p1
 
     ctx.set_profiling(True)
-    ctx.check(ctx.lib.bem_run(ctx.h, pds[0].h, bem.FORM_REFINED, 3, bem._ptr(out2), bem._ptr(inc),
-                              (bem.SolveReport * (R * nf))(), 0))
+    ctx.check(ctx.lib.bem_run(ctx.h, pds[0].h, bem.FORM_REFINED if best == "refined" else bem.FORM_MIXED, 3,
+                              bem._ptr(out2), bem._ptr(inc), (bem.SolveReport * (R * nf))(), 0))
     prof = ctx.profile()
     ctx.set_profiling(False)
     roofline = lu_roofline(prof, [pds[0].n], "8 frequencies of the 40960-unknown ellipsoid")
@@ -871,11 +877,14 @@ def bench_ellipsoid(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp64 operator / tf32 LU preconditioner (complex)",
+        "vs_baseline": None,
+        "dtype": ("fp64" if best == "refined" else "fp32") + " operator / tf32 LU preconditioner (complex)",
         "data": "synthetic (UV ellipsoid mesh, seeded wave direction, no dataset)",
         "config": {"workload": "ellipsoid_bm", "n_unknowns": pds[0].n, "frequencies": nf, "rhs": 2,
-                   "ka_a2": [2.5, 20.0], "form": "refined (FP64 operators) + LU preconditioner, both waves "
-                                                  "per operator (additional_incident_waves)",
+                   "ka_a2": [2.5, 20.0],
+                   "form": ("refined (FP64 operators)" if best == "refined" else "mixed (FP32 operators)") +
+                           " + LU preconditioner, both waves per operator (additional_incident_waves); the faster "
+                           "of mixed and refined whose every solve is within 1e-6",
                    "solver": "GMRES tol 1e-8 (input: Hierarchical tol 1e-6)", "parallelism": "replicas only"},
         "e2e": {"value": world * nsolve * 1000.0 / e2e_ms, "unit": UNIT,
                 "h2d_bytes_per_step": sum(8 * 3 * pd.info["mesh_nodes"] + 8 * 5 * pd.n + 8 * 3 * pd.nfp for pd in pds),
@@ -885,11 +894,12 @@ def bench_ellipsoid(args):
                          "sample": sample + "; a 2560-triangle ellipsoid of the same shape (the oracle's H-matrix "
                                             "solve of 40960 unknowns does not fit a bounded sample)"},
         "clocks": clk,
-        "mixed_fp32_operators": {"value": nsolve * 1000.0 / mixed_ms, "unit": UNIT, "ms_per_step": mixed_ms,
-                                 "max_rel_err": max(err_mixed)},
+        "by_form": {f: {"value": nsolve * 1000.0 / timed[f]["ms"], "unit": UNIT, "ms_per_step": timed[f]["ms"],
+                        "max_rel_err": max(err_mixed if f == "mixed" else err_refined),
+                        "iterations": timed[f]["iterations"]} for f in timed},
         "plain_fp64": plain,
         "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
-        "rel_err_vs_fp64_reference": err_refined, "max_rel_err_vs_fp64_reference": max(err_refined),
+        "rel_err_vs_fp64_reference": errs_best, "max_rel_err_vs_fp64_reference": max(errs_best),
         "error_reference": "field values of the FP64 operators solved to backward error 1e-12",
         "gmres_iterations": iters,
         "stages_ms": {k: v["ms"] for k, v in prof.items()},

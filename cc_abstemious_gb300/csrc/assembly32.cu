@@ -34,7 +34,9 @@ struct Asm32Params {
 
 struct TileGeo32 {
     float cxh[TILE], cxl[TILE], cyh[TILE], cyl[TILE], czh[TILE], czl[TILE], cex[TILE], cey[TILE], cez[TILE], cwa[TILE];
+    float cexl[TILE], ceyl[TILE], cezl[TILE];
     float rxh[TILE], rxl[TILE], ryh[TILE], ryl[TILE], rzh[TILE], rzl[TILE], rex[TILE], rey[TILE], rez[TILE];
+    float rexl[TILE], reyl[TILE], rezl[TILE];
 };
 
 // a - b as float-float (hi, lo) given float-float inputs.
@@ -86,11 +88,27 @@ __device__ __forceinline__ void phase32(float kh, float kl, float rh, float rl, 
     else if (quad == 3) { c0 = sn; s0 = -cs; }
 }
 
-// r = |a - b| for float-float points: returns (the separation rounded to
-// FP32, r hi/lo, 1/r).
+// r = |a - b| for float-float points: returns the separation (float-float),
+// r hi/lo and 1/r.
 struct Sep32 {
-    float dx, dy, dz, rh, rl, inv;
+    float dxh, dxl, dyh, dyl, dzh, dzl, rh, rl, inv;
 };
+
+// d . n for a float-float separation d and a float-float unit normal n,
+// rounded once (exact products and sums of the hi parts, first-order terms of
+// the lo parts).  Between neighbouring elements d is nearly tangent and the
+// plain FP32 dot product loses most of its digits to cancellation.
+__device__ __forceinline__ float dot_ff(const Sep32& d, float nxh, float nxl, float nyh, float nyl, float nzh,
+                                        float nzl) {
+    const float p1 = d.dxh * nxh, p2 = d.dyh * nyh, p3 = d.dzh * nzh;
+    const float e1 = fmaf(d.dxh, nxh, -p1), e2 = fmaf(d.dyh, nyh, -p2), e3 = fmaf(d.dzh, nzh, -p3);
+    float s1, t1, s2, t2;
+    two_sum32(p1, p2, s1, t1);
+    two_sum32(s1, p3, s2, t2);
+    const float lo = (t1 + t2) + (e1 + e2 + e3) + (fmaf(d.dxh, nxl, d.dxl * nxh) + fmaf(d.dyh, nyl, d.dyl * nyh) +
+                                                    fmaf(d.dzh, nzl, d.dzl * nzh));
+    return s2 + lo;
+}
 __device__ __forceinline__ Sep32 separation32(float axh, float axl, float ayh, float ayl, float azh, float azl,
                                               float bxh, float bxl, float byh, float byl, float bzh, float bzl) {
     float dxh, dxl, dyh, dyl, dzh, dzl;
@@ -110,12 +128,12 @@ __device__ __forceinline__ Sep32 separation32(float axh, float axl, float ayh, f
     // by ~1e-6 between neighbouring elements (the near-field terms carry 1/r
     // up to the third power)
     o.inv = 1.0f / (o.rh + o.rl);
-    // the direction uses the separation rounded once (hi + lo): the hi parts
-    // alone are off by the coordinates' rounding, which is ~1e-6 of the
-    // separation of neighbouring elements
-    o.dx = dxh + dxl;
-    o.dy = dyh + dyl;
-    o.dz = dzh + dzl;
+    o.dxh = dxh;
+    o.dxl = dxl;
+    o.dyh = dyh;
+    o.dyl = dyl;
+    o.dzh = dzh;
+    o.dzl = dzl;
     return o;
 }
 
@@ -147,11 +165,12 @@ __device__ __forceinline__ void assemble32_tile(int64_t n, int64_t npad, const f
     __syncthreads();
     const uint32_t B = TILE * sizeof(float);
     if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(&bar, 19 * B);
-        float* cdst[10] = {t.cxh, t.cxl, t.cyh, t.cyl, t.czh, t.czl, t.cex, t.cey, t.cez, t.cwa};
-        for (int a = 0; a < 10; ++a) bulk_g2s(cdst[a], g32 + a * npad + J0, B, &bar);
-        float* rdst[9] = {t.rxh, t.rxl, t.ryh, t.ryl, t.rzh, t.rzl, t.rex, t.rey, t.rez};
-        for (int a = 0; a < 9; ++a) bulk_g2s(rdst[a], g32 + a * npad + I0, B, &bar);
+        mbar_arrive_expect_tx(&bar, 25 * B);
+        float* cdst[13] = {t.cxh, t.cxl, t.cyh, t.cyl, t.czh, t.czl, t.cex, t.cey, t.cez, t.cwa, t.cexl, t.ceyl, t.cezl};
+        for (int a = 0; a < 13; ++a) bulk_g2s(cdst[a], g32 + a * npad + J0, B, &bar);
+        float* rdst[13] = {t.rxh, t.rxl, t.ryh, t.ryl, t.rzh, t.rzl, t.rex, t.rey, t.rez, nullptr, t.rexl, t.reyl, t.rezl};
+        for (int a = 0; a < 13; ++a)
+            if (rdst[a]) bulk_g2s(rdst[a], g32 + a * npad + I0, B, &bar);
     }
     if (!mbar_wait_bounded(&bar, 0)) {
         if (threadIdx.x == 0) atomicOr(err, DEVERR_MBAR_TIMEOUT);
@@ -163,7 +182,7 @@ __device__ __forceinline__ void assemble32_tile(int64_t n, int64_t npad, const f
     const float yxh = t.rxh[tx], yxl = t.rxl[tx], yyh = t.ryh[tx], yyl = t.ryl[tx], yzh = t.rzh[tx],
                 yzl = t.rzl[tx];
     const float eyx = t.rex[tx], eyy = t.rey[tx], eyz = t.rez[tx];
-    const float inv4pi = (float)(1.0 / (4.0 * PI_D));
+    const float eyxl = t.rexl[tx], eyyl = t.reyl[tx], eyzl = t.rezl[tx];
     float nrm[MAX_SYS32];
     float2 acc[MAX_SYS32];
 #pragma unroll
@@ -205,11 +224,10 @@ __device__ __forceinline__ void assemble32_tile(int64_t n, int64_t npad, const f
         const Sep32 sp = separation32(t.cxh[jj], t.cxl[jj], t.cyh[jj], t.cyl[jj], t.czh[jj], t.czl[jj], yxh, yxl, yyh,
                                       yyl, yzh, yzl);
         const float inv = sp.inv;
-        const float erx = sp.dx * inv, ery = sp.dy * inv, erz = sp.dz * inv;
-        const float rdoty = erx * eyx + ery * eyy + erz * eyz;
-        const float rdotx = erx * t.cex[jj] + ery * t.cey[jj] + erz * t.cez[jj];
+        const float rdoty = dot_ff(sp, eyx, eyxl, eyy, eyyl, eyz, eyzl) * inv;
+        const float rdotx = dot_ff(sp, t.cex[jj], t.cexl[jj], t.cey[jj], t.ceyl[jj], t.cez[jj], t.cezl[jj]) * inv;
         const float nxy = eyx * t.cex[jj] + eyy * t.cey[jj] + eyz * t.cez[jj];
-        const float q = inv * inv4pi * t.cwa[jj];
+        const float q = inv * t.cwa[jj];  // wt * area / (4 pi r)
 #pragma unroll
         for (int s = 0; s < MAX_SYS32; ++s) {
             if (s >= prm.nsys) break;
@@ -538,7 +556,6 @@ __global__ void __launch_bounds__(F32_THREADS) field32_kernel(
                 pzh = fp32[4 * fpad + i], pzl = fp32[5 * fpad + i];
     const double2* ph = phi + (size_t)f * vstride;
     const double2* vv = vn + (size_t)f * vstride;
-    const float inv4pi = (float)(1.0 / (4.0 * PI_D));
     double ax = 0, ay = 0;
     float bx = 0, by = 0;
     int cnt = 0;
@@ -548,8 +565,9 @@ __global__ void __launch_bounds__(F32_THREADS) field32_kernel(
                                       g32[FZL * npad + j]);
         // r = x - y with x the field point, y the element: e_r . n_y
         const float rdoty =
-            (sp.dx * g32[FEX * npad + j] + sp.dy * g32[FEY * npad + j] + sp.dz * g32[FEZ * npad + j]) * sp.inv;
-        const float q = sp.inv * inv4pi * g32[FWA * npad + j];
+            dot_ff(sp, g32[FEX * npad + j], g32[FEXL * npad + j], g32[FEY * npad + j], g32[FEYL * npad + j],
+                   g32[FEZ * npad + j], g32[FEZL * npad + j]) * sp.inv;
+        const float q = sp.inv * g32[FWA * npad + j];  // wt * area / (4 pi r)
         float c0, s0;
         phase32(S.kh, S.kl, sp.rh, sp.rl, prm, c0, s0);
         float2 g = make_float2(c0 * q, s0 * q);

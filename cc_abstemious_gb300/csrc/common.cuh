@@ -122,7 +122,9 @@ struct DevGeometry {
 // per pair; the result only depends on the point); wa = wt * area.
 enum GeoArr { GX = 0, GY, GZ, GNX, GNY, GNZ, GAREA, GWT, GWA, GEX, GEY, GEZ, GEO_NARR };
 // Single-precision copy for the mixed form: coordinates split hi + lo.
-enum Geo32Arr { FXH = 0, FXL, FYH, FYL, FZH, FZL, FEX, FEY, FEZ, FWA, GEO32_NARR };
+// FP32 geometry: float-float coordinates, the unit normal as float-float
+// (hi in FEX.., lo in FEXL..), and wt * area / (4 pi) rounded once.
+enum Geo32Arr { FXH = 0, FXL, FYH, FYL, FZH, FZL, FEX, FEY, FEZ, FWA, FEXL, FEYL, FEZL, GEO32_NARR };
 
 struct Problem {
     UserInput in;

@@ -87,10 +87,14 @@ __global__ void geometry32_kernel(int64_t npad, const double* __restrict__ geo, 
         g32[(2 * c) * npad + t] = hi;
         g32[(2 * c + 1) * npad + t] = (float)(v - (double)hi);
     }
-    g32[FEX * npad + t] = (float)geo[GEX * npad + t];
-    g32[FEY * npad + t] = (float)geo[GEY * npad + t];
-    g32[FEZ * npad + t] = (float)geo[GEZ * npad + t];
-    g32[FWA * npad + t] = (float)geo[GWA * npad + t];
+    const int nsrc[3] = {GEX, GEY, GEZ}, nhi[3] = {FEX, FEY, FEZ}, nlo[3] = {FEXL, FEYL, FEZL};
+    for (int c = 0; c < 3; ++c) {
+        double v = geo[nsrc[c] * npad + t];
+        float hi = (float)v;
+        g32[nhi[c] * npad + t] = hi;
+        g32[nlo[c] * npad + t] = (float)(v - (double)hi);
+    }
+    g32[FWA * npad + t] = (float)(geo[GWA * npad + t] * (0.25 / 3.14159265358979323846));
 }
 
 void compute_collocation(Context& ctx, Problem& p) {
