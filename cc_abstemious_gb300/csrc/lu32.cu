@@ -2,12 +2,14 @@
 //
 // Every operator of the batch (FP32 complex, column-major) is copied and
 // factored A = L U without pivoting, in blocks of LB = 128 unknowns, all
-// systems of a (possibly ragged) batch advancing block step k together:
+// systems of a (possibly ragged) batch advancing block step k together, the
+// trailing updates delayed over groups of LU_GROUP steps:
 //
-//   diag   one CTA per system: A11 = L11 U11 in shared memory (tiny pivots are
-//          replaced and counted), then L11^-1 and U11^-1 in place; the two
-//          inverses are kept per block (strict lower / upper of one tile) and
-//          written in the real embedding below for the panel GEMMs.
+//   diag   one CTA per system: L11^-1 and U11^-1 of the diagonal block in one
+//          register-tiled elimination sweep (tiny pivots are replaced and
+//          counted); the two inverses are kept per block (strict lower /
+//          upper of one tile) and written in the real embedding below for
+//          the panel GEMMs.
 //   l21    the column panel A21 is embedded (memory-bound copy), then
 //          L21 = A21 U11^-1 on the tensor cores, in place (the embedding is a
 //          ring homomorphism: emb(A U) = emb(A) emb(U)); the GEMM's epilogue
@@ -21,7 +23,8 @@
 //          (2k x n, re/im interleaved along the rows, which is how the
 //          column-major complex storage reads as floats) gives the natural
 //          real view of the product.  Tiles of 128 real rows x 256 columns,
-//          K = 256 in chunks of 32 staged by 2-D tensor copies (TMA) in the
+//          K = 256 per step of the group in chunks of 32 (up to 1024: the
+//          group's panels side by side) staged by 2-D tensor copies (TMA) in the
 //          128-byte swizzled K-major layout; a persistent warp-specialised kernel
 //          (producer warp, MMA warp, eight epilogue warps, a four-stage operand
 //          ring and two tensor-memory accumulators) so that operand loads, MMAs
@@ -29,8 +32,8 @@
 //
 // Applying M = U^-1 L^-1 to a Krylov vector (flexible right preconditioning:
 // Z[:, k] = M Q[:, k]) is a blocked forward and back substitution with the
-// kept diagonal-block inverses, one launch per block step, FP32 factors and
-// arithmetic (the Krylov vectors stay FP64).  The factorization is TF32-accurate, which is plenty for a
+// kept diagonal-block inverses in one launch (row tickets, flags), FP32
+// factors and arithmetic (the Krylov vectors stay FP64).  The factorization is TF32-accurate, which is plenty for a
 // preconditioner: the FP64 outer GMRES with exact residuals decides the
 // answer, the factors only decide the iteration count.
 #include <cuda.h>
@@ -55,7 +58,8 @@ constexpr int LB = 128;                 // block size (complex unknowns)
 constexpr int GM = 128, GN = 256;       // GEMM tile: real rows x columns
 constexpr int GK = 32;                  // real K per pipeline chunk
 constexpr int GCHUNKS = 2 * LB / GK;    // 8 chunks: K = 256, one block step
-constexpr int WK = 4 * LB;              // panel workspace width: two block steps (K = 512)
+constexpr int LU_GROUP = 4;             // block steps per delayed trailing update
+constexpr int WK = 2 * LB * LU_GROUP;   // panel workspace width: K = 1024 (the group's steps)
 constexpr int GS = 4;                   // pipeline stages
 constexpr int GTHREADS = 320;           // producer warp, MMA warp, eight epilogue warps
 constexpr int GEPI = GTHREADS - 64;     // epilogue threads
@@ -66,10 +70,10 @@ constexpr uint32_t G_TMEM_COLS = 512;           // two accumulators of GN column
 struct LuSys {
     float2* F;    // factors (copy of the operator), column-major, leading dimension ld
     float2* Dm;   // per block: L11^-1 (strict lower) and U11^-1 (upper), LB x LB column-major
-    float* W;     // real embeddings of the step pair's column panels (A21, then L21): 2n rows x WK floats
+    float* W;     // real embeddings of the group's column panels (A21, then L21): 2n rows x WK floats
     float* Li;    // real embedding of L11^-1: 2 LB x 2 LB, row-major
     float* UiT;   // transposed real embedding of U11^-1: 2 LB x 2 LB, row-major
-    float* Y;     // the step pair's U12, natural real view: column j at Y + WK j (first step's rows 0-255)
+    float* Y;     // the group's U12, natural real view: column j at Y + WK j (step k + j at rows 256 j ..)
     const CUtensorMap* tmW;  // W: 2n rows x WK floats, 128-byte swizzled 32 x 128 boxes
     const CUtensorMap* tmF;  // F's natural real view: n columns x 2n floats, 32 x 256 boxes
     const CUtensorMap* tmY;  // Y: n columns x WK floats, 32 x 256 boxes
@@ -81,7 +85,7 @@ struct LuSys {
 
 // One entry per (system, launch): the system, its first CTA in the flattened
 // grid of that launch and, for the GEMMs, the region it covers (rows of the
-// panel workspace, relative to the step pair's trailing origin, and columns).
+// panel workspace, relative to the step group's trailing origin, and columns).
 struct LuWork {
     int sys, tiles_i;
     int64_t tile0;
@@ -269,7 +273,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) lu_diag_kernel(const LuSys* __re
 // W <- real embedding of step ks's column panel A21 (64 rows per CTA): rows
 // 2(i - kt_w) and 2(i - kt_w) + 1 of W, columns woff .. woff + 256, hold
 // [ar, -ai] and [ai, ar] for every column of A21's row i; kt_w = (kw + 1) LB
-// is the trailing origin of the step pair.
+// is the trailing origin of the step group.
 __global__ void __launch_bounds__(256) lu_expand_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
                                                         int nw, int ks, int kw, int woff) {
     extern __shared__ float2 Y[];  // 64 x LB: Y[p * 64 + i]
@@ -355,7 +359,7 @@ __host__ __device__ constexpr uint32_t umma_idesc_tf32_f32(int M, int N) {
 // barrier, and warps 2-9 drain the accumulator of the previous tile (two
 // accumulators of 256 tensor-memory columns) while the next tile's MMAs run.
 // GEMM modes (D = A' B over K = 32 nchunks real), for block step ks of the
-// step pair starting at kw (trailing origin kt_w = (kw + 1) LB, the row origin
+// step group starting at kw (trailing origin kt_w = (kw + 1) LB, the row origin
 // of W and of the TRAIL work regions):
 //   TRAIL  A22 -= W Y        128 rows of W x 256 columns of Y inside each work
 //                            entry's region; K = 256 (one step) or 512 (both)
@@ -955,55 +959,53 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     }
     BEM_CUDA(cudaMemcpyAsync(d->maps.p, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice,
                              c.stream));
-    // the factorization plan: block steps in pairs (k, k + 1).  Step k's panels,
-    // then its update of block column and block row k + 1 only (K = 256),
-    // step k + 1's panels, then one K = 512 update of the rest with both
-    // steps' panels: A22 is read and written once per two steps.  A system
-    // whose step k + 1 has no trailing block takes step k's full update.
+    // the factorization plan: block steps in groups of LU_GROUP (delayed
+    // update).  Before step k + j of the group (j > 0) its block column (from
+    // the diagonal block down) and block row receive the updates of steps
+    // k .. k + j - 1 at once (K = 256 j); then its diagonal block and panels.
+    // After the group, one K = 256 LU_GROUP update of the rest with every
+    // step's panels side by side: A22 is read and written once per group.
     auto plan = [&](LuData::Kind kind, int ks, int kw, int woff, int yoff, int nchunks,
                     const std::vector<Entry>& e) {
         LuData::Launch l{kind, ks, kw, woff, yoff, nchunks, add_segment(*d, e)};
         if (l.seg.ctas) d->plan.push_back(l);
     };
-    for (int k = 0; k < d->nblk_max; k += 2) {
-        std::vector<Entry> diag0, exp0, l210, u120, copy0, trail0, diag1, exp1, l211, u121, copy1, trail1;
+    for (int k = 0; k < d->nblk_max; k += LU_GROUP) {
+        const int64_t ktw = (int64_t)(k + 1) * LB;  // trailing origin of the group: W row 0
+        for (int j = 0; j < LU_GROUP; ++j) {
+            const int st = k + j;
+            std::vector<Entry> thin, diag, expd, l21, u12, copy;
+            for (int s = 0; s < nsys; ++s) {
+                const LuSys& L = d->sys[(size_t)s];
+                if (L.nblk <= st || owner[(size_t)s] != s) continue;  // factored once per operator
+                const int64_t kts = (int64_t)(st + 1) * LB, mts = L.n - kts, mtw = L.n - ktw;
+                if (j > 0) {
+                    const int64_t c0 = (int64_t)st * LB;
+                    thin.push_back(trail_entry(s, 2 * (j - 1) * LB, 2 * mtw, c0, std::min<int64_t>(c0 + LB, L.n)));
+                    thin.push_back(trail_entry(s, 2 * (j - 1) * LB, 2 * j * LB, c0 + LB, L.n));
+                }
+                diag.push_back(Entry{s, 1, 0, 0, 0, 0, 0});
+                if (mts <= 0) continue;  // the system's last block
+                expd.push_back(Entry{s, (mts + 63) / 64, 0, 0, 0, 0, 0});
+                l21.push_back(Entry{s, (2 * mts + GM - 1) / GM, 0, 2 * j * LB, 2 * mtw, 0, 0});
+                u12.push_back(Entry{s, 2 * ((mts + GN - 1) / GN), 0, 0, 0, kts, L.n});
+                copy.push_back(Entry{s, (mts + 31) / 32, 0, 0, 0, 0, 0});
+            }
+            plan(LuData::TRAIL, st, k, 0, 0, GCHUNKS * j, thin);
+            plan(LuData::DIAG, st, k, 0, 0, 0, diag);
+            plan(LuData::EXPAND, st, k, 2 * LB * j, 0, 0, expd);
+            plan(LuData::L21, st, k, 2 * LB * j, 0, GCHUNKS, l21);
+            plan(LuData::U12, st, k, 0, 2 * LB * j, GCHUNKS, u12);
+            plan(LuData::COPY, st, k, 0, 2 * LB * j, 0, copy);
+        }
+        std::vector<Entry> rest;
         for (int s = 0; s < nsys; ++s) {
             const LuSys& L = d->sys[(size_t)s];
-            if (L.nblk <= k || owner[(size_t)s] != s) continue;  // factored once per operator
-            const int64_t kt0 = (int64_t)(k + 1) * LB, kt1 = kt0 + LB;
-            const int64_t mt0 = L.n - kt0, mt1 = L.n - kt1;
-            diag0.push_back(Entry{s, 1, 0, 0, 0, 0, 0});
-            if (mt0 <= 0) continue;
-            exp0.push_back(Entry{s, (mt0 + 63) / 64, 0, 0, 0, 0, 0});
-            l210.push_back(Entry{s, (2 * mt0 + GM - 1) / GM, 0, 0, 2 * mt0, 0, 0});
-            u120.push_back(Entry{s, 2 * ((mt0 + GN - 1) / GN), 0, 0, 0, kt0, L.n});
-            copy0.push_back(Entry{s, (mt0 + 31) / 32, 0, 0, 0, 0, 0});
-            if (mt1 <= 0) {  // block k + 1 is the last: step k's full update
-                trail0.push_back(trail_entry(s, 0, 2 * mt0, kt0, L.n));
-                if (L.nblk > k + 1) diag1.push_back(Entry{s, 1, 0, 0, 0, 0, 0});
-                continue;
-            }
-            trail0.push_back(trail_entry(s, 0, 2 * mt0, kt0, kt1));     // block column k + 1
-            trail0.push_back(trail_entry(s, 0, 2 * LB, kt1, L.n));      // block row k + 1
-            diag1.push_back(Entry{s, 1, 0, 0, 0, 0, 0});
-            exp1.push_back(Entry{s, (mt1 + 63) / 64, 0, 0, 0, 0, 0});
-            l211.push_back(Entry{s, (2 * mt1 + GM - 1) / GM, 0, 2 * LB, 2 * mt0, 0, 0});
-            u121.push_back(Entry{s, 2 * ((mt1 + GN - 1) / GN), 0, 0, 0, kt1, L.n});
-            copy1.push_back(Entry{s, (mt1 + 31) / 32, 0, 0, 0, 0, 0});
-            trail1.push_back(trail_entry(s, 2 * LB, 2 * mt0, kt1, L.n));  // both steps, K = 512
+            const int64_t c0 = (int64_t)(k + LU_GROUP) * LB;
+            if (owner[(size_t)s] != s || c0 >= L.n) continue;
+            rest.push_back(trail_entry(s, 2 * (LU_GROUP - 1) * LB, 2 * (L.n - ktw), c0, L.n));
         }
-        plan(LuData::DIAG, k, k, 0, 0, 0, diag0);
-        plan(LuData::EXPAND, k, k, 0, 0, 0, exp0);
-        plan(LuData::L21, k, k, 0, 0, GCHUNKS, l210);
-        plan(LuData::U12, k, k, 0, 0, GCHUNKS, u120);
-        plan(LuData::COPY, k, k, 0, 0, 0, copy0);
-        plan(LuData::TRAIL, k, k, 0, 0, GCHUNKS, trail0);
-        plan(LuData::DIAG, k + 1, k, 0, 0, 0, diag1);
-        plan(LuData::EXPAND, k + 1, k, 2 * LB, 0, 0, exp1);
-        plan(LuData::L21, k + 1, k, 2 * LB, 0, GCHUNKS, l211);
-        plan(LuData::U12, k + 1, k, 0, 2 * LB, GCHUNKS, u121);
-        plan(LuData::COPY, k + 1, k, 0, 2 * LB, 0, copy1);
-        plan(LuData::TRAIL, k + 1, k, 0, 0, 2 * GCHUNKS, trail1);
+        plan(LuData::TRAIL, k + LU_GROUP - 1, k, 0, 0, GCHUNKS * LU_GROUP, rest);
     }
     // substitution tickets: forward rows by ascending block, then backward
     // rows by descending block, the systems interleaved
@@ -1053,7 +1055,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     BEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));  // persistent grids
     // with profiling: CUDA events around every launch, summed per kind
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    float tsum[3] = {0, 0, 0};
+    float tsum[6] = {0, 0, 0, 0, 0, 0};  // per launch kind
     if (c.profiling) {
         BEM_CUDA(cudaEventCreate(&ev0));
         BEM_CUDA(cudaEventCreate(&ev1));
@@ -1094,7 +1096,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
             BEM_CUDA(cudaEventSynchronize(ev1));
             float ms = 0;
             BEM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-            tsum[l.kind == LuData::DIAG ? 0 : (l.kind == LuData::TRAIL ? 2 : 1)] += ms;
+            tsum[(int)l.kind] += ms;
         }
     }
     if (c.profiling) {
@@ -1102,9 +1104,12 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         double fl = 0;
         for (int s = 0; s < nsys; ++s)
             if (owner[(size_t)s] == s) fl += 8.0 / 3.0 * std::pow((double)d->sys[(size_t)s].n, 3.0);
-        c.stage_add("lu_diag", tsum[0], d->nblk_max, 0);
-        c.stage_add("lu_panels", tsum[1], d->nblk_max, 0);
-        c.stage_add("lu_gemm_tf32", tsum[2], d->nblk_max, fl);
+        c.stage_add("lu_diag", tsum[LuData::DIAG], d->nblk_max, 0);
+        c.stage_add("lu_panel_expand", tsum[LuData::EXPAND], d->nblk_max, 0);
+        c.stage_add("lu_panel_l21", tsum[LuData::L21], d->nblk_max, 0);
+        c.stage_add("lu_panel_u12", tsum[LuData::U12], d->nblk_max, 0);
+        c.stage_add("lu_panel_copy", tsum[LuData::COPY], d->nblk_max, 0);
+        c.stage_add("lu_gemm_tf32", tsum[LuData::TRAIL], d->nblk_max, fl);
         cudaEventDestroy(ev0);
         cudaEventDestroy(ev1);
     }

@@ -118,3 +118,15 @@ def test_refined_form(ctx, wd):
         assert 0 <= r["rel_err_vs_lu"] < 1e-8, r
         assert r["rel_err_vs_lu"] < rm["rel_err_vs_lu"]
         assert r["iterations"] <= 12
+
+
+@pytest.mark.parametrize("ntri", [700, 1030, 1300])
+def test_lu_partial_step_groups(ctx, wd, ntri):
+    """Block counts that end inside a group of four delayed steps: 6, 9 and
+    11 blocks of 128 (the last group has 2, 1 and 3 steps)."""
+    inps = [workloads.perturbed_sphere_input(wd, 90 + ntri, ntri, [2.5, 7.0], tol=1e-10)]
+    r1 = _run(ctx, inps[0], "lu")
+    for b in r1:
+        assert b["flag"] == 1 and b["precond"] == bem.PRECOND_LU
+        assert 0 <= b["rel_err_vs_lu"] < 1e-6, b
+        assert b["iterations"] <= 8
