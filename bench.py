@@ -183,9 +183,9 @@ def tf32_peak():
 
 
 def lu_traffic_ratio():
-    """DRAM traffic / algorithmic A22 bytes of one K = 512 trailing update, from
+    """DRAM traffic / algorithmic A22 bytes of one K = 1024 trailing update, from
     the committed ncu summary (profiles/)."""
-    p = os.path.join(ROOT, "profiles", "lu_gemm_tf32_pair_rigid_sphere.md")
+    p = os.path.join(ROOT, "profiles", "lu_gemm_tf32_group_rigid_sphere.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -201,20 +201,20 @@ def lu_roofline(prof, sizes, what):
     """Roofline entry of the LU preconditioner's trailing update (the dominant
     kernel of the LU forms): TF32 flop rate of the lu_gemm launches (event-timed
     by the library's profiling pass; 8 n^3 / 3 complex flop per factored
-    operator) against cuBLAS TF32 measured here.  Block steps run in pairs:
-    one K = 512 launch per pair reads and writes the trailing block once, so its
-    algorithmic bytes are 16 B (FP32 complex, read + write) per trailing entry
-    (reported per operator: a launch covers every operator of a frequency
-    chunk)."""
+    operator) against cuBLAS TF32 measured here.  Block steps run in groups of
+    four: one K = 1024 launch per group reads and writes the rest of the
+    trailing block once, so its algorithmic bytes are 16 B (FP32 complex, read
+    + write) per entry of that block (reported per operator: a launch covers
+    every operator of a frequency chunk)."""
     lu = prof.get("lu_gemm_tf32", {})
     achieved = lu["bytes"] / (lu["ms"] * 1e-3) / 1e12 if lu.get("ms") else None
     peak = tf32_peak()
-    lb = 128
+    lb, group = 128, 4
     tot, cnt = 0.0, 0
     for n in sizes:
         nblk = (n + lb - 1) // lb
-        for k in range(0, nblk, 2):
-            m1 = n - (k + 2) * lb
+        for k in range(0, nblk, group):
+            m1 = n - (k + group) * lb
             if m1 > 0:
                 tot += 16.0 * m1 * m1
                 cnt += 1
@@ -226,9 +226,9 @@ def lu_roofline(prof, sizes, what):
             "kernel": "lu_gemm_kernel<TRAIL> (TF32 tcgen05 trailing update of the LU preconditioner, " + what + ")",
             "algorithmic_bytes_per_operator_launch": alg,
             "peak_kind": "measured in this run (cuBLAS TF32 GEMM 8192^3, burst)",
-            "traffic_note": "ncu dram read+write / algorithmic A22 bytes of one K = 512 launch "
-                            "(profiles/lu_gemm_tf32_pair_rigid_sphere.md), times the mean algorithmic bytes "
-                            "of this workload's K = 512 launches, per operator"}
+            "traffic_note": "ncu dram read+write / algorithmic A22 bytes of one K = 1024 launch "
+                            "(profiles/lu_gemm_tf32_group_rigid_sphere.md), times the mean algorithmic bytes "
+                            "of this workload's K = 1024 launches, per operator"}
 
 
 def cpu_reference(inp, nfreq_sample, threads):
