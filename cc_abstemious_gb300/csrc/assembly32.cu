@@ -16,14 +16,43 @@
 
 namespace bem {
 
+// Per-frequency constants.  Those that scale every off-diagonal entry carry a
+// lo part: the diagonal (self term) is formed in FP64, so a rounded constant
+// would perturb the off-diagonal part of the operator coherently, an error the
+// solve amplifies by the condition number (unlike independent roundings).
 struct Sys32 {
-    float kh, kl;        // wavenumber hi + lo
-    float beta_im;       // 1/k (Burton-Miller) or 0
-    float k2;            // k^2
-    float2 alpha, beta;  // LHS factors
-    float2 gamma, delta; // RHS factors
+    float kh, kl;             // wavenumber hi + lo
+    float bih, bil;           // 1/k hi + lo (Burton-Miller) or 0
+    float k2;                 // k^2
+    float2 alpha, beta;       // LHS factors, hi
+    float2 alpha_l, beta_l;   // LHS factors, lo
+    float2 gamma, delta;      // RHS factors
     double kd, gdiag_im;
 };
+
+// The frequency-dependent constants of one system.
+static void set_sys32(Sys32& S, double k, bool bm, cd alpha, cd beta) {
+    S.kh = (float)k;
+    S.kl = (float)(k - (double)S.kh);
+    S.kd = k;
+    S.k2 = (float)(k * k);
+    const double bi = bm ? 1.0 / k : 0.0;
+    S.bih = (float)bi;
+    S.bil = (float)(bi - (double)S.bih);
+    S.gdiag_im = bm ? 0.5 * (1.0 / k) : 0.0;
+    S.alpha = make_float2((float)alpha.re, (float)alpha.im);
+    S.beta = make_float2((float)beta.re, (float)beta.im);
+    S.alpha_l = make_float2((float)(alpha.re - (double)S.alpha.x), (float)(alpha.im - (double)S.alpha.y));
+    S.beta_l = make_float2((float)(beta.re - (double)S.beta.x), (float)(beta.im - (double)S.beta.y));
+}
+
+// c * x for a float-float constant (ch + cl) and a float x: rounded once.
+__device__ __forceinline__ float ffmul(float ch, float cl, float x) { return fmaf(ch, x, cl * x); }
+// (ch + cl) * z for float-float complex constant parts and a complex z.
+__device__ __forceinline__ float2 ffcmul(float2 ch, float2 cl, float2 z) {
+    return make_float2(fmaf(ch.x, z.x, fmaf(-ch.y, z.y, cl.x * z.x - cl.y * z.y)),
+                       fmaf(ch.x, z.y, fmaf(ch.y, z.x, cl.x * z.y + cl.y * z.x)));
+}
 constexpr int MAX_SYS32 = 16;
 struct Asm32Params {
     int nsys, bm;
@@ -34,7 +63,7 @@ struct Asm32Params {
 
 struct TileGeo32 {
     float cxh[TILE], cxl[TILE], cyh[TILE], cyl[TILE], czh[TILE], czl[TILE], cex[TILE], cey[TILE], cez[TILE], cwa[TILE];
-    float cexl[TILE], ceyl[TILE], cezl[TILE];
+    float cexl[TILE], ceyl[TILE], cezl[TILE], cwal[TILE];
     float rxh[TILE], rxl[TILE], ryh[TILE], ryl[TILE], rzh[TILE], rzl[TILE], rex[TILE], rey[TILE], rez[TILE];
     float rexl[TILE], reyl[TILE], rezl[TILE];
 };
@@ -165,9 +194,10 @@ __device__ __forceinline__ void assemble32_tile(int64_t n, int64_t npad, const f
     __syncthreads();
     const uint32_t B = TILE * sizeof(float);
     if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(&bar, 25 * B);
-        float* cdst[13] = {t.cxh, t.cxl, t.cyh, t.cyl, t.czh, t.czl, t.cex, t.cey, t.cez, t.cwa, t.cexl, t.ceyl, t.cezl};
-        for (int a = 0; a < 13; ++a) bulk_g2s(cdst[a], g32 + a * npad + J0, B, &bar);
+        mbar_arrive_expect_tx(&bar, 26 * B);
+        float* cdst[14] = {t.cxh,  t.cxl, t.cyh,  t.cyl,  t.czh,  t.czl,  t.cex,
+                           t.cey,  t.cez, t.cwa,  t.cexl, t.ceyl, t.cezl, t.cwal};
+        for (int a = 0; a < 14; ++a) bulk_g2s(cdst[a], g32 + a * npad + J0, B, &bar);
         float* rdst[13] = {t.rxh, t.rxl, t.ryh, t.ryl, t.rzh, t.rzl, t.rex, t.rey, t.rez, nullptr, t.rexl, t.reyl, t.rezl};
         for (int a = 0; a < 13; ++a)
             if (rdst[a]) bulk_g2s(rdst[a], g32 + a * npad + I0, B, &bar);
@@ -227,7 +257,7 @@ __device__ __forceinline__ void assemble32_tile(int64_t n, int64_t npad, const f
         const float rdoty = dot_ff(sp, eyx, eyxl, eyy, eyyl, eyz, eyzl) * inv;
         const float rdotx = dot_ff(sp, t.cex[jj], t.cexl[jj], t.cey[jj], t.ceyl[jj], t.cez[jj], t.cezl[jj]) * inv;
         const float nxy = eyx * t.cex[jj] + eyy * t.cey[jj] + eyz * t.cez[jj];
-        const float q = inv * t.cwa[jj];  // wt * area / (4 pi r)
+        const float q = fmaf(inv, t.cwa[jj], inv * t.cwal[jj]);  // wt * area / (4 pi r)
 #pragma unroll
         for (int s = 0; s < MAX_SYS32; ++s) {
             if (s >= prm.nsys) break;
@@ -235,20 +265,20 @@ __device__ __forceinline__ void assemble32_tile(int64_t n, int64_t npad, const f
             float c0, s0;
             phase32(S.kh, S.kl, sp.rh, sp.rl, prm, c0, s0);
             float2 g = make_float2(c0 * q, s0 * q);  // g * wt * area
-            float2 f1 = make_float2(-inv, S.kh);
-            float2 gf1 = fmul(g, f1);
+            // g f1 with f1 = i k - 1/r
+            float2 gf1 = make_float2(-fmaf(g.x, inv, ffmul(S.kh, S.kl, g.y)), fmaf(-g.y, inv, ffmul(S.kh, S.kl, g.x)));
             float2 h = fscale(gf1, -rdoty);
             if (prm.bm) {
                 float2 dg = fscale(gf1, rdotx);
-                float2 t1 = make_float2(inv * nxy, -S.kh * nxy);  // (-f1) * nxy
-                float2 t2 = fscale(make_float2(S.k2 * sp.rh + 3.0f * f1.x, 3.0f * f1.y), rdotx * rdoty);
+                float2 t1 = make_float2(inv * nxy, -ffmul(S.kh, S.kl, nxy));  // (-f1) * nxy
+                float2 t2 = fscale(make_float2(S.k2 * sp.rh - 3.0f * inv, 3.0f * S.kh), rdotx * rdoty);
                 float2 dh = fmul(fscale(g, inv), make_float2(t1.x - t2.x, t1.y - t2.y));
-                g = make_float2(g.x - S.beta_im * dg.y, g.y + S.beta_im * dg.x);
-                h = make_float2(h.x - S.beta_im * dh.y, h.y + S.beta_im * dh.x);
+                g = make_float2(g.x - ffmul(S.bih, S.bil, dg.y), g.y + ffmul(S.bih, S.bil, dg.x));
+                h = make_float2(h.x - ffmul(S.bih, S.bil, dh.y), h.y + ffmul(S.bih, S.bil, dh.x));
             }
             if (store) {
-                float2 a = fmul(S.alpha, h);
-                float2 b2 = fmul(S.beta, g);
+                float2 a = ffcmul(S.alpha, S.alpha_l, h);
+                float2 b2 = ffcmul(S.beta, S.beta_l, g);
                 float2 af = make_float2(a.x + b2.x, a.y + b2.y);
                 A[s * mat_stride + j * ld + i] = af;
                 nrm[s] += af.x * af.x + af.y * af.y;
@@ -392,14 +422,7 @@ void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks,
         for (int s = 0; s < prm.nsys; ++s) {
             double k = ks[s0 + s];
             Sys32& S = prm.s[s];
-            S.kh = (float)k;
-            S.kl = (float)(k - (double)S.kh);
-            S.kd = k;
-            S.k2 = (float)(k * k);
-            S.beta_im = prm.bm ? (float)(1.0 / k) : 0.f;
-            S.gdiag_im = prm.bm ? 0.5 * (1.0 / k) : 0.0;
-            S.alpha = make_float2((float)alphas[s0 + s].re, (float)alphas[s0 + s].im);
-            S.beta = make_float2((float)betas[s0 + s].re, (float)betas[s0 + s].im);
+            set_sys32(S, k, prm.bm, alphas[s0 + s], betas[s0 + s]);
             S.gamma = make_float2((float)gammas[s0 + s].re, (float)gammas[s0 + s].im);
             S.delta = make_float2((float)deltas[s0 + s].re, (float)deltas[s0 + s].im);
         }
@@ -461,14 +484,7 @@ static void fill_params(const Problem& p, const double* ks, const cd* alphas, co
     for (int s = 0; s < nsys; ++s) {
         const double k = ks[s];
         Sys32& S = prm.s[s];
-        S.kh = (float)k;
-        S.kl = (float)(k - (double)S.kh);
-        S.kd = k;
-        S.k2 = (float)(k * k);
-        S.beta_im = prm.bm ? (float)(1.0 / k) : 0.f;
-        S.gdiag_im = prm.bm ? 0.5 * (1.0 / k) : 0.0;
-        S.alpha = make_float2((float)alphas[s].re, (float)alphas[s].im);
-        S.beta = make_float2((float)betas[s].re, (float)betas[s].im);
+        set_sys32(S, k, prm.bm, alphas[s], betas[s]);
         if (gammas) S.gamma = make_float2((float)gammas[s].re, (float)gammas[s].im);
         if (deltas) S.delta = make_float2((float)deltas[s].re, (float)deltas[s].im);
     }
@@ -567,7 +583,7 @@ __global__ void __launch_bounds__(F32_THREADS) field32_kernel(
         const float rdoty =
             dot_ff(sp, g32[FEX * npad + j], g32[FEXL * npad + j], g32[FEY * npad + j], g32[FEYL * npad + j],
                    g32[FEZ * npad + j], g32[FEZL * npad + j]) * sp.inv;
-        const float q = sp.inv * g32[FWA * npad + j];  // wt * area / (4 pi r)
+        const float q = fmaf(sp.inv, g32[FWA * npad + j], sp.inv * g32[FWAL * npad + j]);  // wt * area / (4 pi r)
         float c0, s0;
         phase32(S.kh, S.kl, sp.rh, sp.rl, prm, c0, s0);
         float2 g = make_float2(c0 * q, s0 * q);

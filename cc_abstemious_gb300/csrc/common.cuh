@@ -123,8 +123,10 @@ struct DevGeometry {
 enum GeoArr { GX = 0, GY, GZ, GNX, GNY, GNZ, GAREA, GWT, GWA, GEX, GEY, GEZ, GEO_NARR };
 // Single-precision copy for the mixed form: coordinates split hi + lo.
 // FP32 geometry: float-float coordinates, the unit normal as float-float
-// (hi in FEX.., lo in FEXL..), and wt * area / (4 pi) rounded once.
-enum Geo32Arr { FXH = 0, FXL, FYH, FYL, FZH, FZL, FEX, FEY, FEZ, FWA, FEXL, FEYL, FEZL, GEO32_NARR };
+// (hi in FEX.., lo in FEXL..), and wt * area / (4 pi) as float-float (FWA,
+// FWAL): a per-element rounding of that weight would scale the off-diagonal
+// part of each column and not its diagonal, an error the solve amplifies.
+enum Geo32Arr { FXH = 0, FXL, FYH, FYL, FZH, FZL, FEX, FEY, FEZ, FWA, FEXL, FEYL, FEZL, FWAL, GEO32_NARR };
 
 struct Problem {
     UserInput in;

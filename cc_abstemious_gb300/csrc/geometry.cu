@@ -94,7 +94,10 @@ __global__ void geometry32_kernel(int64_t npad, const double* __restrict__ geo, 
         g32[nhi[c] * npad + t] = hi;
         g32[nlo[c] * npad + t] = (float)(v - (double)hi);
     }
-    g32[FWA * npad + t] = (float)(geo[GWA * npad + t] * (0.25 / 3.14159265358979323846));
+    const double wa = geo[GWA * npad + t] * (0.25 / 3.14159265358979323846);
+    const float wh = (float)wa;
+    g32[FWA * npad + t] = wh;
+    g32[FWAL * npad + t] = (float)(wa - (double)wh);
 }
 
 void compute_collocation(Context& ctx, Problem& p) {

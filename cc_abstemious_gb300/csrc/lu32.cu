@@ -175,7 +175,8 @@ __device__ __forceinline__ void lu_diag_group(float2 (&z)[4][16], int nb, int tx
             pn = 1e-30f;
             if (threadIdx.x == 0) atomicAdd(small_pivots, 1);
         }
-        const float2 pinv = make_float2(p.x / pn, -p.y / pn);
+        const float rn = __frcp_rn(pn);  // one reciprocal for both parts
+        const float2 pinv = make_float2(p.x * rn, -p.y * rn);
         // row multipliers c_i / p; row j takes 1 + 1/p, which turns its
         // entries right of the pivot into -r_c / p through the same update
         const bool below = tx > jl;  // row tx + 32 JA is below row j
