@@ -28,6 +28,7 @@ struct Sys32 {
     float2 alpha_l, beta_l;   // LHS factors, lo
     float2 gamma, delta;      // RHS factors
     double kd, gdiag_im;
+    int alpha_one, beta_zero; // alpha = 1 and beta = 0 exactly (most boundary conditions)
 };
 
 // The frequency-dependent constants of one system.
@@ -44,6 +45,8 @@ static void set_sys32(Sys32& S, double k, bool bm, cd alpha, cd beta) {
     S.beta = make_float2((float)beta.re, (float)beta.im);
     S.alpha_l = make_float2((float)(alpha.re - (double)S.alpha.x), (float)(alpha.im - (double)S.alpha.y));
     S.beta_l = make_float2((float)(beta.re - (double)S.beta.x), (float)(beta.im - (double)S.beta.y));
+    S.alpha_one = alpha.re == 1.0 && alpha.im == 0.0;
+    S.beta_zero = beta.re == 0.0 && beta.im == 0.0;
 }
 
 // c * x for a float-float constant (ch + cl) and a float x: rounded once.
@@ -277,9 +280,13 @@ __device__ __forceinline__ void assemble32_tile(int64_t n, int64_t npad, const f
                 h = make_float2(h.x - ffmul(S.bih, S.bil, dh.y), h.y + ffmul(S.bih, S.bil, dh.x));
             }
             if (store) {
-                float2 a = ffcmul(S.alpha, S.alpha_l, h);
-                float2 b2 = ffcmul(S.beta, S.beta_l, g);
-                float2 af = make_float2(a.x + b2.x, a.y + b2.y);
+                // alpha h + beta g (uniform branches: alpha is 1 for every
+                // boundary condition but pressure, beta is 0 for velocity)
+                float2 af = S.alpha_one ? h : ffcmul(S.alpha, S.alpha_l, h);
+                if (!S.beta_zero) {
+                    const float2 b2 = ffcmul(S.beta, S.beta_l, g);
+                    af = make_float2(af.x + b2.x, af.y + b2.y);
+                }
                 A[s * mat_stride + j * ld + i] = af;
                 nrm[s] += af.x * af.x + af.y * af.y;
                 if (WITH_RHS) {
@@ -326,7 +333,7 @@ __device__ __forceinline__ void assemble32_tile(int64_t n, int64_t npad, const f
 }
 
 template <int WITH_RHS>
-__global__ void __launch_bounds__(ASM_THREADS) assemble32_kernel(
+__global__ void __launch_bounds__(ASM_THREADS, 3) assemble32_kernel(
     int64_t n, int64_t npad, const float* __restrict__ g32, const double* __restrict__ geo, Asm32Params prm,
     float2* __restrict__ A, int64_t ld, size_t mat_stride, double2* __restrict__ part, size_t part_stride,
     double* __restrict__ norm_part, int* __restrict__ err) {
