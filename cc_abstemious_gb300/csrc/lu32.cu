@@ -817,12 +817,6 @@ LuData::Seg add_segment(LuData& d, const std::vector<Entry>& entries) {
     return sg;
 }
 
-LuData::Seg add_segment(LuData& d, const std::vector<std::pair<int, int64_t>>& entries) {
-    std::vector<Entry> e;
-    for (auto& x : entries) e.push_back(Entry{x.first, x.second, 0, 0, 0, 0, 0});
-    return add_segment(d, e);
-}
-
 // A GEMM region of TRAIL mode: rows [r0, r1) of W (relative to the trailing
 // origin) x columns [c0, c1).
 Entry trail_entry(int s, int64_t r0, int64_t r1, int64_t c0, int64_t c1) {
