@@ -143,20 +143,23 @@ __global__ void lu_round_kernel(const double2* __restrict__ A, size_t n, float2*
 // operations and the upper part U^-1 by column operations (the region i < j,
 // c < j is final).  On exit Z = L^-1 (strictly lower, unit diagonal implied)
 // + U^-1 (upper): the two inverses the triangular solves and panels use.
-// 256 threads, each holding a 4 x 16 tile of Z in registers (rows tx + 32a,
-// columns ty + 8b); one barrier per step.  The steps run in 16 groups of 8
-// columns, so the tile column (b = j / 8) and row (a = j / 32) of step j are
-// compile-time constants: the owners' stores take no register indexing, and
-// the final region i < j, c < j is skipped by whole tile blocks.
-constexpr int DIAG_THREADS = 256;
+// DIAG_THREADS threads (DW warps), each holding a 4 x DB tile of Z in
+// registers (rows tx + 32a, columns ty + DW b); one barrier per step.  The
+// steps run in groups of DW columns, so the tile column (b = j / DW) and row
+// (a = j / 32) of step j are compile-time constants: the owners' stores take
+// no register indexing, and the final region i < j, c < j is skipped by whole
+// tile blocks.
+constexpr int DIAG_THREADS = 512;
+constexpr int DW = DIAG_THREADS / 32, DB = LB / DW;  // warps (column stride), columns per thread
+static_assert(32 % DW == 0 || DW % 32 == 0, "a group of DW columns lies in one 32-row tile block");
 
 template <int JB>
-__device__ __forceinline__ void lu_diag_group(float2 (&z)[4][16], int nb, int tx, int ty, float2 (*colbuf)[LB],
+__device__ __forceinline__ void lu_diag_group(float2 (&z)[4][DB], int nb, int tx, int ty, float2 (*colbuf)[LB],
                                               float2 (*rowbuf)[LB], int* __restrict__ small_pivots) {
-    constexpr int JA = JB / 4;
+    constexpr int JA = DW * JB / 32;
 #pragma unroll 1
-    for (int jc = 0; jc < 8; ++jc) {
-        const int j = 8 * JB + jc, jl = j & 31;
+    for (int jc = 0; jc < DW; ++jc) {
+        const int j = DW * JB + jc, jl = j & 31;
         if (j >= nb) return;
         float2* cb = colbuf[j & 1];
         float2* rb = rowbuf[j & 1];
@@ -165,7 +168,7 @@ __device__ __forceinline__ void lu_diag_group(float2 (&z)[4][16], int nb, int tx
             for (int a = 0; a < 4; ++a) cb[tx + 32 * a] = z[a][JB];
         if (tx == jl)
 #pragma unroll
-            for (int b = 0; b < 16; ++b) rb[ty + 8 * b] = z[JA][b];
+            for (int b = 0; b < DB; ++b) rb[ty + DW * b] = z[JA][b];
         __syncthreads();  // (double-buffered: the next step writes the other pair)
         float2 p = rb[j];
         float pn = p.x * p.x + p.y * p.y;
@@ -188,8 +191,8 @@ __device__ __forceinline__ void lu_diag_group(float2 (&z)[4][16], int nb, int tx
         }
         const float2 cvb = below ? cvs[JA] : make_float2(0.f, 0.f);  // row JA, columns left of j
 #pragma unroll
-        for (int b = 0; b < 16; ++b) {
-            float2 r = rb[ty + 8 * b];
+        for (int b = 0; b < DB; ++b) {
+            float2 r = rb[ty + DW * b];
             if (b == JB) {
                 const float2 hi = ty > jc ? r : make_float2(0.f, 0.f);  // columns right of j only
                 if (ty == jc) r = make_float2(0.f, 0.f);
@@ -217,9 +220,9 @@ __device__ __forceinline__ void lu_diag_group(float2 (&z)[4][16], int nb, int tx
 }
 
 template <int JB>
-__device__ __forceinline__ void lu_diag_sweep(float2 (&z)[4][16], int nb, int tx, int ty, float2 (*colbuf)[LB],
+__device__ __forceinline__ void lu_diag_sweep(float2 (&z)[4][DB], int nb, int tx, int ty, float2 (*colbuf)[LB],
                                               float2 (*rowbuf)[LB], int* __restrict__ small_pivots) {
-    if constexpr (JB < LB / 8) {
+    if constexpr (JB < LB / DW) {
         lu_diag_group<JB>(z, nb, tx, ty, colbuf, rowbuf, small_pivots);
         lu_diag_sweep<JB + 1>(z, nb, tx, ty, colbuf, rowbuf, small_pivots);
     }
@@ -234,10 +237,10 @@ __global__ void __launch_bounds__(DIAG_THREADS) lu_diag_kernel(const LuSys* __re
     const int64_t k0 = (int64_t)k * LB;
     const int nb = (int)min((int64_t)LB, S.n - k0);
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    float2 z[4][16];
+    float2 z[4][DB];
 #pragma unroll
-    for (int b = 0; b < 16; ++b) {
-        const int c = ty + 8 * b;
+    for (int b = 0; b < DB; ++b) {
+        const int c = ty + DW * b;
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             const int r = tx + 32 * a;
@@ -247,9 +250,9 @@ __global__ void __launch_bounds__(DIAG_THREADS) lu_diag_kernel(const LuSys* __re
     }
     lu_diag_sweep<0>(z, nb, tx, ty, colbuf, rowbuf, small_pivots);
 #pragma unroll
-    for (int b = 0; b < 16; ++b)
+    for (int b = 0; b < DB; ++b)
 #pragma unroll
-        for (int a = 0; a < 4; ++a) T[(ty + 8 * b) * LB + tx + 32 * a] = z[a][b];
+        for (int a = 0; a < 4; ++a) T[(ty + DW * b) * LB + tx + 32 * a] = z[a][b];
     __syncthreads();
     float2* Dk = S.Dm + (size_t)k * LB * LB;
     for (int c = ty; c < nb; c += DIAG_THREADS / 32)
