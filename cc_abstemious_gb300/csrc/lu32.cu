@@ -280,20 +280,20 @@ __global__ void __launch_bounds__(DIAG_THREADS) lu_diag_kernel(const LuSys* __re
 // is the trailing origin of the step group.
 __global__ void __launch_bounds__(256) lu_expand_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
                                                         int nw, int ks, int kw, int woff) {
-    extern __shared__ float2 Y[];  // 64 x LB: Y[p * 64 + i]
+    extern __shared__ float2 Y[];  // 64 x LB, column stride 65: Y[p * 65 + i] (no bank conflicts either way)
     int64_t tile;
     const LuSys S = sys[lu_locate(wl, nw, blockIdx.x, tile)];
     const int64_t k0 = (int64_t)ks * LB, kt = k0 + LB, ktw = (int64_t)(kw + 1) * LB, i0 = kt + 64 * tile;
     const int nrow = (int)min((int64_t)64, S.n - i0);
     for (int t = threadIdx.x; t < 64 * LB; t += blockDim.x) {
         const int p = t / 64, i = t % 64;
-        Y[t] = i < nrow ? S.F[(k0 + p) * S.ld + i0 + i] : make_float2(0.f, 0.f);
+        Y[p * 65 + i] = i < nrow ? S.F[(k0 + p) * S.ld + i0 + i] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     const int64_t wr0 = 2 * (i0 - ktw);
     for (int t = threadIdx.x; t < nrow * LB; t += blockDim.x) {
         const int i = t / LB, c = t % LB;
-        const float2 v = Y[c * 64 + i];
+        const float2 v = Y[c * 65 + i];
         float2* w0 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i) * WK + woff);
         float2* w1 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i + 1) * WK + woff);
         w0[c] = make_float2(v.x, -v.y);
@@ -1041,7 +1041,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     BEM_CUDA(cudaMemsetAsync(d->info.p, 0, sizeof(int), c.stream));
     int* err = device_err(c);
     BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c.stream));
-    const size_t diag_smem = sizeof(float2) * LB * LB, expand_smem = sizeof(float2) * 64 * LB;
+    const size_t diag_smem = sizeof(float2) * LB * LB, expand_smem = sizeof(float2) * 65 * LB;
     BEM_CUDA(cudaFuncSetAttribute(lu_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_smem));
     BEM_CUDA(cudaFuncSetAttribute(lu_expand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)expand_smem));
     BEM_CUDA(cudaFuncSetAttribute(lu_gemm_kernel<G_TRAIL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
