@@ -366,7 +366,8 @@ __host__ __device__ constexpr uint32_t umma_idesc_tf32_f32(int M, int N) {
 // step group starting at kw (trailing origin kt_w = (kw + 1) LB, the row origin
 // of W and of the TRAIL work regions):
 //   TRAIL  A22 -= W Y        128 rows of W x 256 columns of Y inside each work
-//                            entry's region; K = 256 (one step) or 512 (both)
+//                            entry's region; K = 256 per step of the group
+//                            applied (up to 1024 for the rest of A22)
 //   U12    Y = Li U12raw     the two 128-row halves of Li x 256 columns of the
 //                            step's row panel, into Y's rows yoff .. yoff + 256
 //   L21    W = W UiT^T       128 rows of W x all 256 columns at W column woff, in
