@@ -14,6 +14,13 @@
 #include <map>
 #include <memory>
 #include <sstream>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include <unistd.h>
 
 #include "common.cuh"
 
@@ -327,6 +334,104 @@ struct Lines {
     }
 };
 
+// Host threads for parsing large mesh blocks, created on first use and kept
+// for the life of the process (the pool is never destroyed; its threads wait
+// on a condition variable).  A process forked after creation has no workers
+// and parses on the calling thread.
+class RowPool {
+  public:
+    static RowPool& get() {
+        static RowPool* p = new RowPool();
+        return *p;
+    }
+    int size() const { return getpid() == owner_ ? (int)threads_.size() + 1 : 1; }
+    // f(t) for t in [0, n), n <= size(), t = 0 on the calling thread; returns
+    // when all are done
+    void run(int n, const std::function<void(int)>& f) {
+        if (n <= 1) {
+            if (n == 1) f(0);
+            return;
+        }
+        std::lock_guard<std::mutex> serial(serial_);
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            job_ = &f;
+            n_ = n;
+            next_ = 1;
+            pending_ = n - 1;
+            ++gen_;
+        }
+        cv_.notify_all();
+        f(0);
+        std::unique_lock<std::mutex> lk(m_);
+        done_.wait(lk, [&] { return pending_ == 0; });
+        job_ = nullptr;
+    }
+
+  private:
+    RowPool() : owner_(getpid()) {
+        const unsigned hw = std::thread::hardware_concurrency();
+        const unsigned nw = std::min(7u, hw > 1 ? hw - 1 : 0u);
+        for (unsigned i = 0; i < nw; ++i) threads_.emplace_back([this] { loop(); });
+    }
+    void loop() {
+        uint64_t seen = 0;
+        std::unique_lock<std::mutex> lk(m_);
+        for (;;) {
+            cv_.wait(lk, [&] { return gen_ != seen; });
+            seen = gen_;
+            while (next_ < n_) {
+                const int t = next_++;
+                const std::function<void(int)>* f = job_;
+                lk.unlock();
+                (*f)(t);
+                lk.lock();
+                if (--pending_ == 0) done_.notify_one();
+            }
+        }
+    }
+    pid_t owner_;
+    std::vector<std::thread> threads_;
+    std::mutex m_, serial_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)>* job_ = nullptr;
+    int n_ = 0, next_ = 0, pending_ = 0;
+    uint64_t gen_ = 0;
+};
+
+// The next n rows of a block: their [begin, end) spans, the cursor moved past
+// them.  False if the text ends first.
+bool take_rows(Lines& L, int64_t n, std::vector<const char*>& lb, std::vector<const char*>& le) {
+    lb.resize((size_t)n);
+    le.resize((size_t)n);
+    for (int64_t i = 0; i < n; ++i)
+        if (!L.next(lb[(size_t)i], le[(size_t)i])) return false;
+    return true;
+}
+
+// Splits rows [0, n) into contiguous chunks over the pool (one chunk per
+// ~1024 rows); row(chunk, i) parses row i and returns false on a bad row.
+// Returns the first bad row, or -1.  The results do not depend on the split.
+template <class F>
+int64_t parallel_rows(int64_t n, int nt, F row) {
+    std::vector<int64_t> bad((size_t)nt, -1);
+    RowPool::get().run(nt, [&](int t) {
+        const int64_t i0 = n * t / nt, i1 = n * (t + 1) / nt;
+        for (int64_t i = i0; i < i1; ++i)
+            if (!row(t, i)) {
+                bad[(size_t)t] = i;
+                return;
+            }
+    });
+    for (int64_t b : bad)
+        if (b >= 0) return b;
+    return -1;
+}
+
+int chunks_for(int64_t n) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>(RowPool::get().size(), n / 1024));
+}
+
 inline const char* skip_ws(const char* s, const char* e) {
     while (s < e && (*s == ' ' || *s == '\t' || *s == '\r')) ++s;
     return s;
@@ -386,6 +491,7 @@ Mesh read_vtk(const std::string& path) {
     Lines L{text.data(), text.data() + text.size()};
     Mesh m;
     const char *b, *e;
+    std::vector<const char*> lb, le;  // rows of the current block
     auto count_after = [&](const char* lb, const char* le) -> int64_t {
         const char* s = skip_ws(lb, le);
         while (s < le && *s != ' ' && *s != '\t') ++s;  // the keyword
@@ -398,34 +504,45 @@ Mesh read_vtk(const std::string& path) {
         if (w == "POINTS") {
             const int64_t n = count_after(b, e);
             m.nodes.assign((size_t)(3 * n), 0.0);
-            for (int64_t i = 0; i < n; ++i) {
-                const char *lb, *le;
-                if (!L.next(lb, le)) fail("VTK: unexpected end of POINTS", b, b);
-                const char* s = lb;
-                for (int c = 0; c < 3; ++c) {
-                    double v;
-                    if (!parse_num(s, le, v)) fail("VTK: bad point row: ", lb, le);
-                    m.nodes[(size_t)(3 * i + c)] = v;
-                }
-            }
+            if (!take_rows(L, n, lb, le)) fail("VTK: unexpected end of POINTS", b, b);
+            const int64_t bad = parallel_rows(n, chunks_for(n), [&](int, int64_t i) {
+                const char* s = lb[(size_t)i];
+                for (int c = 0; c < 3; ++c)
+                    if (!parse_num(s, le[(size_t)i], m.nodes[(size_t)(3 * i + c)])) return false;
+                return true;
+            });
+            if (bad >= 0) fail("VTK: bad point row: ", lb[(size_t)bad], le[(size_t)bad]);
         } else if (w == "CELLS") {
             const int64_t n = count_after(b, e);
             m.body.assign((size_t)n, 0);
             m.etype.assign((size_t)n, 0);
             m.conn_off.assign((size_t)n + 1, 0);
             m.conn.clear();
-            m.conn.reserve((size_t)n * 4);
-            for (int64_t i = 0; i < n; ++i) {
-                const char *lb, *le;
-                if (!L.next(lb, le)) fail("VTK: unexpected end of CELLS", b, b);
-                const char* s = lb;
+            if (!take_rows(L, n, lb, le)) fail("VTK: unexpected end of CELLS", b, b);
+            // node ids per chunk, then concatenated in row order
+            const int nt = chunks_for(n);
+            struct alignas(64) Part {  // one cache line per chunk's vector header
+                std::vector<int64_t> v;
+            };
+            std::vector<Part> part((size_t)nt);
+            for (auto& q : part) q.v.reserve((size_t)(4 * n / nt + 16));
+            std::vector<int64_t> cnt((size_t)n, 0);
+            const int64_t bad = parallel_rows(n, nt, [&](int t, int64_t i) {
+                const char* s = lb[(size_t)i];
                 long long bv;
-                if (!parse_num(s, le, bv)) fail("VTK: bad cell row: ", lb, le);
+                if (!parse_num(s, le[(size_t)i], bv)) return false;
                 m.body[(size_t)i] = bv;
                 long long v;
-                while (parse_num(s, le, v)) m.conn.push_back(v);
-                m.conn_off[(size_t)i + 1] = (int64_t)m.conn.size();
-            }
+                std::vector<int64_t>& out = part[(size_t)t].v;
+                const size_t before = out.size();
+                while (parse_num(s, le[(size_t)i], v)) out.push_back(v);
+                cnt[(size_t)i] = (int64_t)(out.size() - before);
+                return true;
+            });
+            if (bad >= 0) fail("VTK: bad cell row: ", lb[(size_t)bad], le[(size_t)bad]);
+            for (int64_t i = 0; i < n; ++i) m.conn_off[(size_t)i + 1] = m.conn_off[(size_t)i] + cnt[(size_t)i];
+            m.conn.reserve((size_t)m.conn_off[(size_t)n]);
+            for (auto& q : part) m.conn.insert(m.conn.end(), q.v.begin(), q.v.end());
         } else if (w == "CELL_TYPES") {
             const int64_t n = count_after(b, e);
             require(n <= m.nelem(), "VTK: CELL_TYPES longer than CELLS");

@@ -271,3 +271,33 @@ def test_input_1_json_parses(ctx):
     pd = bem.PreData.from_dict(d, ctx=ctx)
     assert pd.info["body_index"] == 3
     assert pd.info["mesh_elements"] == 336
+
+
+def test_vtk_reader_large_and_malformed(ctx, tmp_path):
+    """The VTK reader parses blocks of more than ~1024 rows in chunks on host
+    threads: a large mesh must give the oracle's collocation bit for bit, and a
+    bad row anywhere (here in the middle of a block) must be reported as bad
+    input with that row's text."""
+    from cc_abstemious_gb300 import meshgen
+    nodes, tris = meshgen.icosphere(5)
+    path = tmp_path / "ico5.vtk"
+    meshgen.write_vtk(str(path), nodes, tris, 5)
+    d = sphere_input(mesh_file=str(path), body_index=1)
+    pd = bem.PreData.from_dict(d, ctx=ctx)
+    assert np.array_equal(pd.get_cpts(), O.Problem(d).cpts)
+    lines = path.read_text().splitlines()
+    p0 = next(i for i, l in enumerate(lines) if l.startswith("POINTS")) + 1
+    c0 = next(i for i, l in enumerate(lines) if l.startswith("CELLS")) + 1
+    for row, text in ((p0 + 7000, "0.5 abc 0.25"), (c0 + 15000, "x 2 3 4")):
+        bad = list(lines)
+        bad[row] = text
+        bpath = tmp_path / "bad.vtk"
+        bpath.write_text("\n".join(bad) + "\n")
+        with pytest.raises(bem.BemError) as e:
+            bem.PreData.from_dict(sphere_input(mesh_file=str(bpath), body_index=1), ctx=ctx)
+        assert e.value.status == 1 and text in str(e.value)
+    short = tmp_path / "short.vtk"
+    short.write_text("\n".join(lines[:p0 + 5000]) + "\n")
+    with pytest.raises(bem.BemError) as e:
+        bem.PreData.from_dict(sphere_input(mesh_file=str(short), body_index=1), ctx=ctx)
+    assert e.value.status == 1
