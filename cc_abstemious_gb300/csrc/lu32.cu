@@ -616,7 +616,9 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
 // row carries on).  Block products run in FP32 (TF32-accurate factors),
 // accumulated over blocks in FP64.
 struct LuTicket {
-    int sys, phase, row, flags;  // flags: the system's forward flags, then its backward flags
+    int sys, nrhs;   // systems sys .. sys + nrhs - 1 share one operator (several right-hand sides)
+    int phase, row;  // 0 forward / 1 backward, block row
+    int flags;       // the group's forward flags, then its backward flags
 };
 
 __device__ __forceinline__ int ld_acquire_gpu(const int* p) {
@@ -638,12 +640,17 @@ __device__ __forceinline__ void lu_wait_flag(const int* f, int* err) {
 }
 
 constexpr int TS_THREADS = 256;  // 64 row pairs x 4 column quarters of a block
+constexpr int TS_MAXR = 4;       // right-hand sides per ticket (systems sharing one operator)
 
-// acc += B v for the row pair of this thread over its 32-column quarter of a
-// block: B's columns at col (stride ld, float2 entries), v in shared memory.
-__device__ __forceinline__ void lu_block_mv(const float2* __restrict__ col, int64_t ld, const float2* v, int c0,
-                                            int nc, bool rows_ok, double2 (&acc)[2]) {
-    float2 a0 = make_float2(0.f, 0.f), a1 = a0;
+// acc[r] += B v[r] for the row pair of this thread over its 32-column quarter
+// of a block, every right-hand side r < R sharing the loads of B: B's columns
+// at col (stride ld, float2 entries), v[r] in shared memory.
+template <int R>
+__device__ __forceinline__ void lu_block_mv(const float2* __restrict__ col, int64_t ld, const float2 (*v)[LB],
+                                            int c0, int nc, bool rows_ok, double2 (&acc)[R][2]) {
+    float2 a0[R], a1[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) a0[r] = a1[r] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         float4 e[16];
@@ -654,25 +661,33 @@ __device__ __forceinline__ void lu_block_mv(const float2* __restrict__ col, int6
                                      : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            const float2 x = v[c0 + 16 * h + i];
-            cfmaf_(a0, make_float2(e[i].x, e[i].y), x);
-            cfmaf_(a1, make_float2(e[i].z, e[i].w), x);
-        }
+        for (int i = 0; i < 16; ++i)
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const float2 x = v[r][c0 + 16 * h + i];
+                cfmaf_(a0[r], make_float2(e[i].x, e[i].y), x);
+                cfmaf_(a1[r], make_float2(e[i].z, e[i].w), x);
+            }
     }
-    acc[0].x += a0.x;
-    acc[0].y += a0.y;
-    acc[1].x += a1.x;
-    acc[1].y += a1.y;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        acc[r][0].x += a0[r].x;
+        acc[r][0].y += a0[r].y;
+        acc[r][1].x += a1[r].x;
+        acc[r][1].y += a1[r].y;
+    }
 }
 
+// R = the largest group of right-hand sides in the ticket list (1, 2 or 4):
+// smaller groups leave their unused vectors at zero.
+template <int R>
 __global__ void __launch_bounds__(TS_THREADS) lu_trsv_kernel(const LuSys* __restrict__ sys,
                                                              const LuTicket* __restrict__ tickets, int ntickets,
                                                              int* __restrict__ counter, int* __restrict__ flags,
                                                              GmBatch bt, int* __restrict__ err) {
-    __shared__ float2 xs[LB];
+    __shared__ float2 xs[R][LB];
     __shared__ double2 red[4][LB];
-    __shared__ double2 ys[LB];
+    __shared__ double2 ys[R][LB];
     __shared__ int tk, all_final;
     const int rp = threadIdx.x & 63, cq = threadIdx.x >> 6;
     for (;;) {
@@ -682,17 +697,36 @@ __global__ void __launch_bounds__(TS_THREADS) lu_trsv_kernel(const LuSys* __rest
         __syncthreads();  // every thread has read tk
         if (t >= ntickets) return;
         const LuTicket T = tickets[t];
-        const GmState& st = bt.st[T.sys];
-        if (!gm_apply_active(bt, st, MV_Q)) continue;
+        // the group's vectors: inactive systems (converged, or at another
+        // stage) keep zero vectors and are not written
+        bool act[R];
+        double2* zr[R];
+        const double2* qr[R];
+        bool any = false;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            act[r] = false;
+            zr[r] = nullptr;
+            qr[r] = nullptr;
+            if (r < T.nrhs) {
+                const GmState& st = bt.st[T.sys + r];
+                act[r] = gm_apply_active(bt, st, MV_Q);
+                const GmView g = gm_view(bt, T.sys + r);
+                zr[r] = bt.Z + g.q + (size_t)st.k * g.n;
+                qr[r] = bt.Q + g.q + (size_t)st.k * g.n;
+                any = any || act[r];
+            }
+        }
+        if (!any) continue;
         const LuSys S = sys[T.sys];
-        const GmView g = gm_view(bt, T.sys);
-        double2* z = bt.Z + g.q + (size_t)st.k * g.n;
         const int b = T.row, nblk = S.nblk;
         const int nr = (int)min((int64_t)LB, S.n - (int64_t)b * LB);
         const bool rows_ok = 2 * rp < nr;  // nr is even or the block's last
         const bool fwd = T.phase == 0;
         int* fl = flags + T.flags + (fwd ? 0 : nblk);
-        double2 acc[2] = {make_double2(0, 0), make_double2(0, 0)};
+        double2 acc[R][2];
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r][0] = acc[r][1] = make_double2(0, 0);
         // blocks of the row, in the order their values become final
         const int nk = fwd ? b : nblk - 1 - b;
         int seen = 0;  // blocks known final
@@ -711,61 +745,77 @@ __global__ void __launch_bounds__(TS_THREADS) lu_trsv_kernel(const LuSys* __rest
                 seen = all_final ? nk : i + 1;
             }
             const int nc = (int)min((int64_t)LB, S.n - (int64_t)k * LB);
-            if (threadIdx.x < LB) {
-                const double2 v = threadIdx.x < nc ? __ldcg(z + (int64_t)k * LB + threadIdx.x) : make_double2(0, 0);
-                xs[threadIdx.x] = make_float2((float)v.x, (float)v.y);
+            for (int u = threadIdx.x; u < R * LB; u += TS_THREADS) {
+                const int r = u / LB, c = u % LB;
+                double2 v = make_double2(0, 0);
+#pragma unroll
+                for (int q = 0; q < R; ++q)
+                    if (q == r && act[q] && c < nc) v = __ldcg(zr[q] + (int64_t)k * LB + c);
+                xs[r][c] = make_float2((float)v.x, (float)v.y);
             }
             __syncthreads();
             const float2* col = S.F + (int64_t)k * LB * S.ld + (int64_t)b * LB + 2 * rp;
-            lu_block_mv(col, S.ld, xs, 32 * cq, nc, rows_ok, acc);
+            lu_block_mv<R>(col, S.ld, xs, 32 * cq, nc, rows_ok, acc);
             __syncthreads();  // xs reused by the next block
         }
-        red[cq][2 * rp] = acc[0];
-        red[cq][2 * rp + 1] = acc[1];
-        __syncthreads();
-        const double2* src = fwd ? bt.Q + g.q + (size_t)st.k * g.n : z;
-        if (threadIdx.x < LB) {
-            const int r = threadIdx.x;
-            double2 y = make_double2(0, 0);
-            if (r < nr) {
-                y = fwd ? src[(int64_t)b * LB + r] : __ldcg(src + (int64_t)b * LB + r);
-                for (int q = 0; q < 4; ++q) {
-                    y.x -= red[q][r].x;
-                    y.y -= red[q][r].y;
+        // y = source - sum, per right-hand side
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            red[cq][2 * rp] = acc[r][0];
+            red[cq][2 * rp + 1] = acc[r][1];
+            __syncthreads();
+            if (threadIdx.x < LB) {
+                const int i = threadIdx.x;
+                double2 y = make_double2(0, 0);
+                if (i < nr && act[r]) {
+                    y = fwd ? qr[r][(int64_t)b * LB + i] : __ldcg(zr[r] + (int64_t)b * LB + i);
+                    for (int q = 0; q < 4; ++q) {
+                        y.x -= red[q][i].x;
+                        y.y -= red[q][i].y;
+                    }
                 }
+                ys[r][i] = y;
+                xs[r][i] = make_float2((float)y.x, (float)y.y);
             }
-            ys[r] = y;
-            xs[r] = make_float2((float)y.x, (float)y.y);
+            __syncthreads();
         }
-        __syncthreads();
         // diagonal block: strictly lower part of L_bb^-1 (unit diagonal
         // added in FP64) or the upper part of U_bb^-1 with its diagonal
+        float2 d0[R], d1[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) d0[r] = d1[r] = make_float2(0.f, 0.f);
         {
             const float2* D = S.Dm + (size_t)b * LB * LB;
             const int r0 = 2 * rp;
-            float2 a0 = make_float2(0.f, 0.f), a1 = a0;
 #pragma unroll 8
             for (int i = 0; i < 32; ++i) {
                 const int c = 32 * cq + i;
                 if (!rows_ok || c >= nr) continue;
                 const float4 e = __ldg(reinterpret_cast<const float4*>(D + (size_t)c * LB + r0));
-                const float2 x = xs[c];
                 const bool u0 = fwd ? c < r0 : c >= r0, u1 = fwd ? c < r0 + 1 : c >= r0 + 1;
-                if (u0) cfmaf_(a0, make_float2(e.x, e.y), x);
-                if (u1) cfmaf_(a1, make_float2(e.z, e.w), x);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const float2 x = xs[r][c];
+                    if (u0) cfmaf_(d0[r], make_float2(e.x, e.y), x);
+                    if (u1) cfmaf_(d1[r], make_float2(e.z, e.w), x);
+                }
             }
-            red[cq][r0] = make_double2(a0.x, a0.y);
-            red[cq][r0 + 1] = make_double2(a1.x, a1.y);
         }
-        __syncthreads();
-        if (threadIdx.x < LB && threadIdx.x < nr) {
-            const int r = threadIdx.x;
-            double2 v = fwd ? ys[r] : make_double2(0, 0);
-            for (int q = 0; q < 4; ++q) {
-                v.x += red[q][r].x;
-                v.y += red[q][r].y;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            red[cq][2 * rp] = make_double2(d0[r].x, d0[r].y);
+            red[cq][2 * rp + 1] = make_double2(d1[r].x, d1[r].y);
+            __syncthreads();
+            if (threadIdx.x < LB && threadIdx.x < nr && act[r]) {
+                const int i = threadIdx.x;
+                double2 v = fwd ? ys[r][i] : make_double2(0, 0);
+                for (int q = 0; q < 4; ++q) {
+                    v.x += red[q][i].x;
+                    v.y += red[q][i].y;
+                }
+                __stcg(zr[r] + (int64_t)b * LB + i, v);
             }
-            __stcg(z + (int64_t)b * LB + r, v);
+            __syncthreads();
         }
         __threadfence();
         __syncthreads();
@@ -794,7 +844,7 @@ struct LuData {
     std::vector<Launch> plan;
     // preconditioner application: tickets, and a counter + row flags
     DevBuf tickets, flags;
-    int ntickets = 0, nflags = 0, trsv_grid = 1;
+    int ntickets = 0, nflags = 0, trsv_grid = 1, trsv_r = 1;  // trsv_r: right-hand sides per ticket
     std::vector<LuWork> host;
     int small_pivots = 0;
 };
@@ -834,8 +884,17 @@ void lu_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
     if (!d.ntickets) return;
     BEM_CUDA(cudaMemsetAsync(d.flags.p, 0, sizeof(int) * (size_t)d.nflags, c.stream));
     int* f = d.flags.as<int>();
-    lu_trsv_kernel<<<(unsigned)d.trsv_grid, TS_THREADS, 0, c.stream>>>(
-        d.sysbuf.as<LuSys>(), d.tickets.as<LuTicket>(), d.ntickets, f, f, ws.bt, device_err(c));
+    const LuSys* sys = d.sysbuf.as<LuSys>();
+    const LuTicket* tk = d.tickets.as<LuTicket>();
+    if (d.trsv_r == 1)
+        lu_trsv_kernel<1><<<(unsigned)d.trsv_grid, TS_THREADS, 0, c.stream>>>(sys, tk, d.ntickets, f, f, ws.bt,
+                                                                              device_err(c));
+    else if (d.trsv_r == 2)
+        lu_trsv_kernel<2><<<(unsigned)d.trsv_grid, TS_THREADS, 0, c.stream>>>(sys, tk, d.ntickets, f, f, ws.bt,
+                                                                              device_err(c));
+    else
+        lu_trsv_kernel<TS_MAXR><<<(unsigned)d.trsv_grid, TS_THREADS, 0, c.stream>>>(sys, tk, d.ntickets, f, f,
+                                                                                    ws.bt, device_err(c));
     BEM_CHECK_LAUNCH(&c);
 }
 
@@ -1007,20 +1066,29 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         plan(LuData::TRAIL, k + LU_GROUP - 1, k, 0, 0, GCHUNKS * LU_GROUP, rest);
     }
     // substitution tickets: forward rows by ascending block, then backward
-    // rows by descending block, the systems interleaved
+    // rows by descending block, the groups interleaved.  A group is up to
+    // TS_MAXR consecutive systems sharing one operator (several right-hand
+    // sides): one ticket streams the factors once for all of them.
     {
-        std::vector<int> fo((size_t)nsys);
-        int nf = 1;  // [0] is the ticket counter
-        for (int s = 0; s < nsys; ++s) {
-            fo[(size_t)s] = nf;
+        std::vector<int> gs, gn, fo;  // group: first system, systems, flag offset
+        int nf = 1;                   // [0] is the ticket counter
+        for (int s = 0; s < nsys;) {
+            int r = 1;
+            while (r < TS_MAXR && s + r < nsys && owner[(size_t)(s + r)] == owner[(size_t)s]) ++r;
+            gs.push_back(s);
+            gn.push_back(r);
+            fo.push_back(nf);
             nf += 2 * d->sys[(size_t)s].nblk;
+            d->trsv_r = std::max(d->trsv_r, r);
+            s += r;
         }
+        if (d->trsv_r == 3) d->trsv_r = TS_MAXR;
         std::vector<LuTicket> tk;
         for (int ph = 0; ph < 2; ++ph)
             for (int t = 0; t < d->nblk_max; ++t)
-                for (int s = 0; s < nsys; ++s) {
-                    const int nb = d->sys[(size_t)s].nblk;
-                    if (t < nb) tk.push_back(LuTicket{s, ph, ph == 0 ? t : nb - 1 - t, fo[(size_t)s]});
+                for (size_t q = 0; q < gs.size(); ++q) {
+                    const int nb = d->sys[(size_t)gs[q]].nblk;
+                    if (t < nb) tk.push_back(LuTicket{gs[q], gn[q], ph, ph == 0 ? t : nb - 1 - t, fo[q]});
                 }
         d->ntickets = (int)tk.size();
         d->nflags = nf;
@@ -1029,7 +1097,10 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         BEM_CUDA(cudaMemcpyAsync(d->tickets.p, tk.data(), sizeof(LuTicket) * tk.size(), cudaMemcpyHostToDevice,
                                  c.stream));
         int per_sm = 1, nsm_ = 0;
-        BEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lu_trsv_kernel, TS_THREADS, 0));
+        const void* kfn = d->trsv_r == 1   ? (const void*)lu_trsv_kernel<1>
+                          : d->trsv_r == 2 ? (const void*)lu_trsv_kernel<2>
+                                           : (const void*)lu_trsv_kernel<TS_MAXR>;
+        BEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, TS_THREADS, 0));
         BEM_CUDA(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, c.device));
         d->trsv_grid = std::max(1, std::min(d->ntickets, std::max(1, per_sm) * nsm_));
     }
