@@ -48,6 +48,24 @@ __device__ __forceinline__ void ff_acc(float& hi, float& lo, float a, float b) {
     lo += err + e;
 }
 
+// (h, l) += a b for float-float a and b: the hi product exactly (FMA), the
+// cross terms to first order, renormalised.
+__device__ __forceinline__ void ff_madd(float& h, float& l, float ah, float al, float bh, float bl) {
+    const float p = ah * bh;
+    const float pe = fmaf(ah, bh, -p) + fmaf(ah, bl, al * bh);
+    float s, e;
+    two_sum(h, p, s, e);
+    e += l + pe;
+    h = s + e;
+    l = e - (h - s);
+}
+
+// A complex FP64 value as float-float parts (re hi, re lo, im hi, im lo).
+__device__ __forceinline__ float4 ff_split(double2 x) {
+    const float rh = (float)x.x, ih = (float)x.y;
+    return make_float4(rh, (float)(x.x - (double)rh), ih, (float)(x.y - (double)ih));
+}
+
 // Batched operator application W_s = A_s v_s, v_s = x_s (START/CHECK) or
 // Q_s[:, k] (Q).  Grid (row blocks, column chunks, systems); partial sums of
 // the column chunks are reduced in a fixed order by the last CTA of each row
@@ -275,9 +293,11 @@ __global__ void __launch_bounds__(AR_THREADS) gm_start_kernel(GmBatch bt) {
         acc += r.x * r.x + r.y * r.y;
     }
     double rn = sqrt(block_sum(acc, sh));
+    float4* Qf = (bt.Qf && !bt.ref_dotc) ? bt.Qf + g.q : nullptr;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
         double2 r = Q[i];
         Q[i] = make_double2(r.x / rn, r.y / rn);
+        if (Qf) Qf[i] = ff_split(Q[i]);
     }
     double xn = vec_norm(bt.X + g.v, n, sh);
     if (threadIdx.x == 0) {
@@ -313,33 +333,86 @@ __global__ void __launch_bounds__(AR_THREADS) gm_arnoldi_kernel(GmBatch bt, int 
     double2* Q = bt.Q + g.q;
     double2* Wg = bt.W + g.v;
     double2* w = w_in_smem ? wsh : Wg;
-    if (w_in_smem)
-        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) w[i] = Wg[i];
-    __syncthreads();
     GmSmall sm = gm_small(bt, s);
-    // modified Gram-Schmidt
-    for (int i = 0; i <= k; ++i) {
-        const double2* qi = Q + (size_t)i * n;
-        double2 acc = make_double2(0, 0);
-        for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
-            double2 a = w[l], q = qi[l];
-            if (bt.ref_dotc) cfma(acc, cconj(a), q);  // nalgebra dotc(qk1, q_i) = sum conj(qk1) q_i
-            else cfma(acc, cconj(q), a);             // q_i^H w
-        }
-        double2 h = block_sum2(acc, sh);
-        for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
-            double2 a = w[l];
-            cfma(a, cneg(h), qi[l]);
-            w[l] = a;
-        }
-        if (threadIdx.x == 0) sm.hk1[i] = h;
-        __syncthreads();
-    }
-    double hn = vec_norm(w, n, sh);
     double2* qk1 = Q + (size_t)(k + 1) * n;
-    // scale = 1 / hk1[k+1] as a complex division (gmres.rs:172)
-    double2 scale = cdiv(make_double2(1.0, 0.0), make_double2(hn, 0.0));
-    for (int64_t l = threadIdx.x; l < n; l += blockDim.x) qk1[l] = cmul(w[l], scale);
+    double hn;
+    if (bt.Qf && !bt.ref_dotc && w_in_smem) {
+        // modified Gram-Schmidt in float-float on the FP32 pipes (GB300's FP64
+        // rate is ~1/60 of its FP32 rate; this loop was bound by it), against
+        // the float-float copy of the basis; ~1e-14 relative
+        float4* wf = reinterpret_cast<float4*>(wsh);
+        const float4* Qf = bt.Qf + g.q;
+        for (int64_t l = threadIdx.x; l < n; l += blockDim.x) wf[l] = ff_split(Wg[l]);
+        __syncthreads();
+        for (int i = 0; i <= k; ++i) {
+            const float4* qi = Qf + (size_t)i * n;
+            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;  // q_i^H w
+            for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
+                const float4 q = qi[l], a = wf[l];
+                ff_madd(rh, rl, q.x, q.y, a.x, a.y);
+                ff_madd(rh, rl, q.z, q.w, a.z, a.w);
+                ff_madd(ih, il, q.x, q.y, a.z, a.w);
+                ff_madd(ih, il, -q.z, -q.w, a.x, a.y);
+            }
+            const double2 h = block_sum2(make_double2((double)rh + (double)rl, (double)ih + (double)il), sh);
+            const float4 hf = ff_split(h);
+            for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
+                float4 a = wf[l];
+                const float4 q = qi[l];
+                ff_madd(a.x, a.y, -hf.x, -hf.y, q.x, q.y);  // re -= hr qr - hi qi
+                ff_madd(a.x, a.y, hf.z, hf.w, q.z, q.w);
+                ff_madd(a.z, a.w, -hf.x, -hf.y, q.z, q.w);  // im -= hr qi + hi qr
+                ff_madd(a.z, a.w, -hf.z, -hf.w, q.x, q.y);
+                wf[l] = a;
+            }
+            if (threadIdx.x == 0) sm.hk1[i] = h;
+            __syncthreads();
+        }
+        float nh = 0.f, nl = 0.f;
+        for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
+            const float4 a = wf[l];
+            ff_madd(nh, nl, a.x, a.y, a.x, a.y);
+            ff_madd(nh, nl, a.z, a.w, a.z, a.w);
+        }
+        hn = sqrt(block_sum((double)nh + (double)nl, sh));
+        const double sc = 1.0 / hn;
+        const float sch = (float)sc, scl = (float)(sc - (double)sch);
+        float4* qf1 = bt.Qf + g.q + (size_t)(k + 1) * n;
+        for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
+            const float4 a = wf[l];
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            ff_madd(q.x, q.y, a.x, a.y, sch, scl);
+            ff_madd(q.z, q.w, a.z, a.w, sch, scl);
+            qf1[l] = q;
+            qk1[l] = make_double2((double)q.x + (double)q.y, (double)q.z + (double)q.w);
+        }
+    } else {
+        if (w_in_smem)
+            for (int64_t i = threadIdx.x; i < n; i += blockDim.x) w[i] = Wg[i];
+        __syncthreads();
+        // modified Gram-Schmidt
+        for (int i = 0; i <= k; ++i) {
+            const double2* qi = Q + (size_t)i * n;
+            double2 acc = make_double2(0, 0);
+            for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
+                double2 a = w[l], q = qi[l];
+                if (bt.ref_dotc) cfma(acc, cconj(a), q);  // nalgebra dotc(qk1, q_i) = sum conj(qk1) q_i
+                else cfma(acc, cconj(q), a);             // q_i^H w
+            }
+            double2 h = block_sum2(acc, sh);
+            for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
+                double2 a = w[l];
+                cfma(a, cneg(h), qi[l]);
+                w[l] = a;
+            }
+            if (threadIdx.x == 0) sm.hk1[i] = h;
+            __syncthreads();
+        }
+        hn = vec_norm(w, n, sh);
+        // scale = 1 / hk1[k+1] as a complex division (gmres.rs:172)
+        double2 scale = cdiv(make_double2(1.0, 0.0), make_double2(hn, 0.0));
+        for (int64_t l = threadIdx.x; l < n; l += blockDim.x) qk1[l] = cmul(w[l], scale);
+    }
     if (threadIdx.x == 0) {
         sm.hk1[k + 1] = make_double2(hn, 0.0);
         // apply previous rotations
@@ -529,11 +602,16 @@ void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const
     size_t oP = carve(sizeof(double2) * nsys * cb * bt.n_pad), oT = carve(sizeof(int) * nsys * rb);
     size_t oS = carve(sizeof(double2) * nsys * small), oSt = carve(sizeof(GmState) * nsys);
     size_t oN = carve(sizeof(double) * nsys * 1024 + sizeof(double) * nsys);
+    ws.w_in_smem = (n * sizeof(double2) <= 200 * 1024);
+    // float-float basis copy for the Gram-Schmidt on the FP32 pipes
+    const bool qf = !ref_dotc && ws.w_in_smem;
+    size_t oQf = qf ? carve(sizeof(float4) * nsys * bt.qstride) : 0;
     ws.memb().ensure(bytes);
     char* base = ws.memb().as<char>();
     bt.X = reinterpret_cast<double2*>(base + oX);
     bt.B = reinterpret_cast<double2*>(base + oB);
     bt.Q = reinterpret_cast<double2*>(base + oQ);
+    bt.Qf = qf ? reinterpret_cast<float4*>(base + oQf) : nullptr;
     bt.W = reinterpret_cast<double2*>(base + oW);
     bt.part = reinterpret_cast<double2*>(base + oP);
     bt.tickets = reinterpret_cast<int*>(base + oT);
@@ -543,7 +621,6 @@ void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const
     ws.norm_part = reinterpret_cast<double*>(base + oN);
     ws.anorm = ws.norm_part + (size_t)nsys * 1024;
     BEM_CUDA(cudaMemsetAsync(bt.tickets, 0, sizeof(int) * nsys * rb, ctx.stream));
-    ws.w_in_smem = (n * sizeof(double2) <= 200 * 1024);
     if (ws.w_in_smem) {
         BEM_CUDA(cudaFuncSetAttribute(gm_arnoldi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(n * sizeof(double2))));
@@ -593,6 +670,7 @@ size_t gm_prepare_external(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, i
     bt.X = reinterpret_cast<double2*>(base + oX);
     bt.B = reinterpret_cast<double2*>(base + oB);
     bt.Q = reinterpret_cast<double2*>(base + oQ);
+    bt.Qf = nullptr;  // caller memory: the FP64 Gram-Schmidt
     bt.W = reinterpret_cast<double2*>(base + oW);
     bt.part = reinterpret_cast<double2*>(base + oP);
     bt.tickets = reinterpret_cast<int*>(base + oT);
@@ -666,11 +744,15 @@ void gm_prepare_ragged(Context& ctx, GmWorkspace& ws, const std::vector<int64_t>
     size_t oS = carve(sizeof(double2) * nsys * small), oSt = carve(sizeof(GmState) * nsys);
     size_t oN = carve(sizeof(double) * nsys * 1024 + sizeof(double) * nsys);
     size_t oD = carve(sizeof(GmSys) * nsys);
+    ws.w_in_smem = (nmax * sizeof(double2) <= 200 * 1024);
+    // float-float basis copy for the Gram-Schmidt on the FP32 pipes
+    size_t oQf = ws.w_in_smem ? carve(sizeof(float4) * q) : 0;
     ws.memb().ensure(bytes);
     char* base = ws.memb().as<char>();
     bt.X = reinterpret_cast<double2*>(base + oX);
     bt.B = reinterpret_cast<double2*>(base + oB);
     bt.Q = reinterpret_cast<double2*>(base + oQ);
+    bt.Qf = ws.w_in_smem ? reinterpret_cast<float4*>(base + oQf) : nullptr;
     bt.W = reinterpret_cast<double2*>(base + oW);
     bt.part = reinterpret_cast<double2*>(base + oP);
     bt.tickets = reinterpret_cast<int*>(base + oT);
@@ -683,7 +765,6 @@ void gm_prepare_ragged(Context& ctx, GmWorkspace& ws, const std::vector<int64_t>
     BEM_CUDA(cudaMemcpyAsync(dsys, sys.data(), sizeof(GmSys) * nsys, cudaMemcpyHostToDevice, ctx.stream));
     bt.sys = dsys;
     BEM_CUDA(cudaMemsetAsync(bt.tickets, 0, sizeof(int) * t, ctx.stream));
-    ws.w_in_smem = (nmax * sizeof(double2) <= 200 * 1024);
     if (ws.w_in_smem) {
         BEM_CUDA(cudaFuncSetAttribute(gm_arnoldi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(nmax * sizeof(double2))));

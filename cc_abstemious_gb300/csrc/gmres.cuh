@@ -41,6 +41,8 @@ struct GmBatch {
     double2* small;     // per-system Hessenberg / rotations
     GmState* st;
     double2* Z;         // flexible right preconditioning: Z[:, k] = M Q[:, k] (nullptr: none)
+    float4* Qf = nullptr;  // float-float copy of Q (re hi, re lo, im hi, im lo) for the
+                           // Gram-Schmidt of the mixed / refined forms (nullptr: FP64)
 };
 
 // Whether the operator application of `mode` has work for a system.
