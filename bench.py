@@ -43,7 +43,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--lu-check", type=int, default=4,
                     help="frequencies checked against an FP64 LU (evenly spread; 0 = all)")
-    ap.add_argument("--cpu-sample", type=int, default=1, help="frequencies solved by the CPU baseline")
+    ap.add_argument("--cpu-sample", type=int, default=2,
+                    help="frequencies solved by the CPU baseline per step (evenly spread: 2 = lowest and highest ka)")
     ap.add_argument("--precond", default="none", choices=["none", "block_jacobi", "learned", "lu"])
     ap.add_argument("--mesh-m", type=int, default=32, help="cube-sphere subdivisions (6 m^2 quads)")
     ap.add_argument("--nfreq", type=int, default=16)
@@ -253,8 +254,8 @@ def run_reference_arm(args, inp):
         return
     threads = max((os.cpu_count() or 2) // 2, 2)  # preprocess.rs:12-17
     vals = []
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        pass
+    for _ in range(args.warmup):
+        cpu_reference(inp, args.cpu_sample, threads)
     t_total = 0.0
     for _ in range(max(args.steps, 1)):
         v, dt, sample = cpu_reference(inp, args.cpu_sample, threads)

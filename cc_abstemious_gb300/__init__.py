@@ -11,7 +11,6 @@ library's CUDA kernels; this module only marshals arguments.
     a.run()
     a.write_results_at_frequency(0)
 """
-import csv
 import ctypes as C
 import json
 import os
@@ -307,31 +306,30 @@ def convert_results(pd, results):
             pd.ctx.check(pd.ctx.lib.bem_convert_to_pressure(pd.h, r.frequency, _ptr(v), len(v)))
 
 
-def _field_name(pd):
-    return "pre" if pd.info["output_pressure"] else "vpo"
+def write_results_at_frequency(pd, result, path=None):
+    """postprocess.rs:15-44 through bem_write_results_at_frequency (path None:
+    the input's output.file)."""
+    sc = np.ascontiguousarray(result.scattered, dtype=np.complex128)
+    inc = np.ascontiguousarray(result.incident, dtype=np.complex128)
+    pd.ctx.check(pd.ctx.lib.bem_write_results_at_frequency(pd.ctx.h, pd.h, path.encode() if path else None,
+                                                           _ptr(sc), _ptr(inc)))
 
 
-def write_results_at_frequency(pd, result, path):
-    """postprocess.rs:15-44"""
-    on = _field_name(pd)
-    pts = pd.field_points
-    with open(path, "w", newline="") as f:
-        w = csv.writer(f)
-        w.writerow(["index", "x", "y", "z", on + "_re", on + "_im", "inc_re", "inc_im"])
-        for i in range(len(result.scattered)):
-            w.writerow([i, repr(pts[i][0]), repr(pts[i][1]), repr(pts[i][2]), repr(result.scattered[i].real),
-                        repr(result.scattered[i].imag), repr(result.incident[i].real), repr(result.incident[i].imag)])
+def write_results_at_point(pd, results, index, path=None):
+    """postprocess.rs:47-67 through bem_write_results_at_point."""
+    sc = np.ascontiguousarray(np.stack([r.scattered for r in results]), dtype=np.complex128)
+    inc = np.ascontiguousarray(np.stack([r.incident for r in results]), dtype=np.complex128)
+    pd.ctx.check(pd.ctx.lib.bem_write_results_at_point(pd.ctx.h, pd.h, path.encode() if path else None, index,
+                                                       _ptr(sc), _ptr(inc)))
 
 
-def write_results_at_point(pd, results, index, path):
-    """postprocess.rs:47-67"""
-    on = _field_name(pd)
-    with open(path, "w", newline="") as f:
-        w = csv.writer(f)
-        w.writerow(["freq", on + "_re", on + "_im", "inc_re", "inc_im"])
-        for r in results:
-            w.writerow([repr(r.frequency), repr(r.scattered[index].real), repr(r.scattered[index].imag),
-                        repr(r.incident[index].real), repr(r.incident[index].imag)])
+def format_f64(v):
+    """Rust's f64 Display as the CSV writers print numbers (bem_format_f64)."""
+    buf = C.create_string_buffer(512)
+    n = _lib.load().bem_format_f64(float(v), buf, len(buf))
+    if n < 0:
+        raise BemError(6, "formatting failed")
+    return buf.value.decode()
 
 
 # ---- analysis.rs -----------------------------------------------------------------
@@ -398,12 +396,12 @@ class Analysis:
         return self.ctx or Context.default()
 
     def write_results_at_frequency(self, ifreq, path=None):
-        out = path or json.loads(self._input)["output"]["file"]
-        write_results_at_frequency(self.predata, self.results[ifreq], out)
+        """analysis.rs:121-123"""
+        write_results_at_frequency(self.predata, self.results[ifreq], path)
 
     def write_results_at_point(self, index, path=None):
-        out = path or json.loads(self._input)["output"]["file"]
-        write_results_at_point(self.predata, self.results, index, out)
+        """analysis.rs:124-126"""
+        write_results_at_point(self.predata, self.results, index, path)
 
 
 _PRECONDS = {None: PRECOND_NONE, "none": PRECOND_NONE, "block_jacobi": PRECOND_BLOCK_JACOBI,

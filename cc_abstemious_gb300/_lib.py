@@ -80,6 +80,9 @@ SIGNATURES = {
     "bem_get_field": (_i, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i]),
     "bem_evaluate_field": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "bem_convert_to_pressure": (_i, [_vp, _d, _vp, _i64]),
+    "bem_write_results_at_frequency": (_i, [_vp, _vp, C.c_char_p, _vp, _vp]),
+    "bem_write_results_at_point": (_i, [_vp, _vp, C.c_char_p, _i64, _vp, _vp]),
+    "bem_format_f64": (_i64, [_d, C.c_char_p, _i64]),
     "bem_run": (_i, [_vp, _vp, _i, _i, _vp, _vp, C.POINTER(SolveReport), _i]),
     "bem_last_surface": (_i, [_vp, _vp, _vp, _vp]),
     "bem_run_batch": (_i, [_vp, _PP, _i, _i, _PP, _PP, _PP, _i, _i64]),
@@ -89,6 +92,7 @@ SIGNATURES = {
     "bem_learned_set_weights": (_i, [_vp, _vp]),
     "bem_learned_mlp_eval": (_i, [_vp, _i64, _vp, _vp, _vp, _vp]),
     "bem_learned_mlp_infer": (_i, [_vp, _i64, _vp, _vp]),
+    "bem_lu32_factor_apply": (_i, [_vp, _i, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
     "bem_hmatrix_build": (_i, [_vp, _vp, _i, _PP]),
     "bem_hmatrix_destroy": (None, [_vp]),
     "bem_hmatrix_gemv": (_i, [_vp, _vp, Cplx, _vp, Cplx, _vp]),

@@ -13,6 +13,8 @@
 // to summation order) or FP32 matrix with FP64 vectors and compensated
 // products/sums (mixed form).  Arnoldi (modified Gram-Schmidt), Givens
 // rotations, the small triangular solve and the stopping test are FP64.
+#include <mutex>
+
 #include "common.cuh"
 #include "complex.cuh"
 #include "gmres.cuh"
@@ -24,6 +26,8 @@ constexpr int MV_THREADS = 256;
 constexpr int MV_ROWS = MV_ROWS_PER_THREAD * MV_THREADS;  // 512
 constexpr int MV_COLS = 512;
 constexpr int AR_THREADS = 1024;
+// largest Krylov vector kept in the Arnoldi kernel's shared memory (n <= 12800)
+constexpr size_t AR_SMEM_CAP = 200 * 1024;
 
 __device__ __forceinline__ bool mv_active(const GmState& s, int mode) {
     if (s.done) return false;
@@ -569,6 +573,28 @@ __global__ void finish_norms_kernel(const double* part, int nb, int nsys, double
 }
 
 // ---------------------------------------------------------------------------
+// The Arnoldi kernel keeps w in dynamic shared memory when it fits
+// (n * 16 B <= AR_SMEM_CAP).  The kernel attribute is process-wide, so it is
+// raised once per device to the cap and never lowered: a smaller solve on
+// another thread cannot shrink the limit under a larger one's launch or graph.
+namespace {
+constexpr int AR_MAX_DEVICES = 64;
+std::once_flag g_ar_smem_once[AR_MAX_DEVICES];
+}  // namespace
+
+void arnoldi_allow_smem(int device) {
+    require(device >= 0 && device < AR_MAX_DEVICES, "device index out of range");
+    // a failed set throws out of call_once, which leaves the flag unset so the
+    // next call tries again
+    std::call_once(g_ar_smem_once[device], [] {
+        cudaError_t err = cudaFuncSetAttribute(gm_arnoldi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)AR_SMEM_CAP);
+        if (err != cudaSuccess)
+            throw Error(BEM_ERR_CUDA,
+                        std::string("cudaFuncSetAttribute(gm_arnoldi_kernel): ") + cudaGetErrorString(err));
+    });
+}
+
 GmWorkspace::~GmWorkspace() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
 }
@@ -602,7 +628,7 @@ void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const
     size_t oP = carve(sizeof(double2) * nsys * cb * bt.n_pad), oT = carve(sizeof(int) * nsys * rb);
     size_t oS = carve(sizeof(double2) * nsys * small), oSt = carve(sizeof(GmState) * nsys);
     size_t oN = carve(sizeof(double) * nsys * 1024 + sizeof(double) * nsys);
-    ws.w_in_smem = (n * sizeof(double2) <= 200 * 1024);
+    ws.w_in_smem = (n * sizeof(double2) <= AR_SMEM_CAP);
     // float-float basis copy for the Gram-Schmidt on the FP32 pipes
     const bool qf = !ref_dotc && ws.w_in_smem;
     size_t oQf = qf ? carve(sizeof(float4) * nsys * bt.qstride) : 0;
@@ -621,10 +647,7 @@ void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const
     ws.norm_part = reinterpret_cast<double*>(base + oN);
     ws.anorm = ws.norm_part + (size_t)nsys * 1024;
     BEM_CUDA(cudaMemsetAsync(bt.tickets, 0, sizeof(int) * nsys * rb, ctx.stream));
-    if (ws.w_in_smem) {
-        BEM_CUDA(cudaFuncSetAttribute(gm_arnoldi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(n * sizeof(double2))));
-    }
+    if (ws.w_in_smem) arnoldi_allow_smem(ctx.device);
     if (ws.graph_exec) {
         cudaGraphExecDestroy(ws.graph_exec);
         ws.graph_exec = nullptr;
@@ -682,11 +705,8 @@ size_t gm_prepare_external(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, i
     // the last-CTA tickets must start at zero; every other region is written
     // before it is read
     BEM_CUDA(cudaMemsetAsync(bt.tickets, 0, sizeof(int) * nsys * rb, ctx.stream));
-    ws.w_in_smem = (n * sizeof(double2) <= 200 * 1024);
-    if (ws.w_in_smem) {
-        BEM_CUDA(cudaFuncSetAttribute(gm_arnoldi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(n * sizeof(double2))));
-    }
+    ws.w_in_smem = (n * sizeof(double2) <= AR_SMEM_CAP);
+    if (ws.w_in_smem) arnoldi_allow_smem(ctx.device);
     return bytes;
 }
 
@@ -744,7 +764,7 @@ void gm_prepare_ragged(Context& ctx, GmWorkspace& ws, const std::vector<int64_t>
     size_t oS = carve(sizeof(double2) * nsys * small), oSt = carve(sizeof(GmState) * nsys);
     size_t oN = carve(sizeof(double) * nsys * 1024 + sizeof(double) * nsys);
     size_t oD = carve(sizeof(GmSys) * nsys);
-    ws.w_in_smem = (nmax * sizeof(double2) <= 200 * 1024);
+    ws.w_in_smem = (nmax * sizeof(double2) <= AR_SMEM_CAP);
     // float-float basis copy for the Gram-Schmidt on the FP32 pipes
     size_t oQf = ws.w_in_smem ? carve(sizeof(float4) * q) : 0;
     ws.memb().ensure(bytes);
@@ -765,10 +785,7 @@ void gm_prepare_ragged(Context& ctx, GmWorkspace& ws, const std::vector<int64_t>
     BEM_CUDA(cudaMemcpyAsync(dsys, sys.data(), sizeof(GmSys) * nsys, cudaMemcpyHostToDevice, ctx.stream));
     bt.sys = dsys;
     BEM_CUDA(cudaMemsetAsync(bt.tickets, 0, sizeof(int) * t, ctx.stream));
-    if (ws.w_in_smem) {
-        BEM_CUDA(cudaFuncSetAttribute(gm_arnoldi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(nmax * sizeof(double2))));
-    }
+    if (ws.w_in_smem) arnoldi_allow_smem(ctx.device);
     if (ws.graph_exec) {
         cudaGraphExecDestroy(ws.graph_exec);
         ws.graph_exec = nullptr;

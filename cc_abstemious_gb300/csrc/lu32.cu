@@ -1203,3 +1203,89 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
 }
 
 }  // namespace bem
+
+// ---------------------------------------------------------------------------
+// Instrumentation: the preconditioner's factorization and one application on
+// caller-given FP32 operators, with the factors read back, so that the device
+// kernels can be compared entry by entry with an FP64 LU.
+using namespace bem;
+
+extern "C" BEM_API bem_status bem_lu32_factor_apply(bem_ctx* ctx, int nsys, const int64_t* n, const int64_t* ld,
+                                                    const int64_t* a_off, int64_t a_entries, const float* A,
+                                                    float* F, float* D, int64_t d_entries, const bem_cplx* q,
+                                                    bem_cplx* z, int* small_pivots) {
+    if (!ctx || nsys < 1 || !n || !ld || !a_off || !A || a_entries <= 0) return BEM_ERR_BAD_INPUT;
+    Context& c = ctx->c;
+    try {
+        BEM_CUDA(cudaSetDevice(c.device));
+        std::vector<int64_t> ns(n, n + nsys), lds(ld, ld + nsys);
+        std::vector<size_t> offs((size_t)nsys);
+        int64_t dneed = 0;
+        for (int s = 0; s < nsys; ++s) {
+            require(ns[(size_t)s] >= 1 && lds[(size_t)s] >= ns[(size_t)s], "lu32: bad system size");
+            // the production layout: leading dimension and offset multiples
+            // of 64 entries (16-byte aligned tensor copies and vector loads)
+            require(lds[(size_t)s] % 64 == 0 && a_off[s] % 64 == 0 && a_off[s] >= 0,
+                    "lu32: leading dimensions and offsets must be multiples of 64");
+            require(a_off[s] + lds[(size_t)s] * ns[(size_t)s] <= a_entries, "lu32: operator outside A");
+            offs[(size_t)s] = (size_t)a_off[s];
+            bool owner = true;
+            for (int o = 0; o < s; ++o)
+                if (a_off[o] == a_off[s]) {
+                    require(ns[(size_t)o] == ns[(size_t)s] && lds[(size_t)o] == lds[(size_t)s],
+                            "lu32: systems sharing an operator must have the same size");
+                    owner = false;
+                    break;
+                }
+            if (owner) dneed += (int64_t)((ns[(size_t)s] + LB - 1) / LB) * LB * LB;
+        }
+        require(!D || d_entries == dneed,
+                "lu32: D must hold " + std::to_string(dneed) + " complex entries (128 x 128 per block)");
+        DevBuf dA;
+        dA.ensure(sizeof(float2) * (size_t)a_entries);
+        BEM_CUDA(cudaMemcpyAsync(dA.p, A, sizeof(float2) * (size_t)a_entries, cudaMemcpyHostToDevice, c.stream));
+        GmWorkspace ws;
+        gm_prepare_ragged(c, ws, ns, lds, offs, 1, dA.p, true);
+        // every system active at Krylov step 0 (the state the application reads)
+        BEM_CUDA(cudaMemsetAsync(ws.bt.st, 0, sizeof(GmState) * (size_t)nsys, c.stream));
+        if (q) {
+            size_t v = 0;
+            for (int s = 0; s < nsys; ++s) {
+                BEM_CUDA(cudaMemcpyAsync(ws.bt.Q + ws.sys_host[(size_t)s].q_off, q + v,
+                                         sizeof(double2) * (size_t)ns[(size_t)s], cudaMemcpyHostToDevice, c.stream));
+                v += (size_t)ns[(size_t)s];
+            }
+        }
+        lu_precond_setup(c, ws);
+        LuData& d = *static_cast<LuData*>(ws.precond_user);
+        if (q && z) {
+            ws.precond(c, ws, MV_Q, ws.precond_user);
+            check_device_err(c);
+            size_t v = 0;
+            for (int s = 0; s < nsys; ++s) {
+                BEM_CUDA(cudaMemcpyAsync(z + v, ws.bt.Z + ws.sys_host[(size_t)s].q_off,
+                                         sizeof(double2) * (size_t)ns[(size_t)s], cudaMemcpyDeviceToHost, c.stream));
+                v += (size_t)ns[(size_t)s];
+            }
+        }
+        if (F) {
+            size_t fent = 0;
+            for (int s = 0; s < nsys; ++s)
+                fent = std::max(fent, offs[(size_t)s] + (size_t)lds[(size_t)s] * (size_t)ns[(size_t)s]);
+            BEM_CUDA(cudaMemcpyAsync(F, c.w_lu_F.p, sizeof(float2) * fent, cudaMemcpyDeviceToHost, c.stream));
+        }
+        if (D)
+            BEM_CUDA(cudaMemcpyAsync(D, c.w_lu_D.p, sizeof(float2) * (size_t)dneed, cudaMemcpyDeviceToHost,
+                                     c.stream));
+        c.sync();
+        if (small_pivots) *small_pivots = d.small_pivots;
+        return BEM_OK;
+    } catch (const Error& e) {
+        c.last_error = e.what();
+        return e.status;
+    } catch (const std::exception& e) {
+        c.last_error = e.what();
+        return BEM_ERR_CUDA;
+    }
+}
+

@@ -5,6 +5,7 @@
 // memory to their own pool up front (a framework's caching allocator, a
 // real-time loop with a fixed memory budget) and would otherwise see a
 // cudaMalloc that synchronises the device or fails under their budget.
+#include <chrono>
 #include <cmath>
 #include <mutex>
 
@@ -27,7 +28,10 @@ constexpr int MAX_DEVICES = 64;
 std::mutex g_setup_mutex;
 void* g_scratch_ptr[MAX_DEVICES] = {};
 
-// Once per device, with that device current: resolve the array's device address.
+// Once per device, with that device current: resolve the array's device
+// address.  The address is kept for the life of the process, so the entry
+// point is not valid after cudaDeviceReset (or any other re-creation of the
+// device's primary context) in the same process.
 void* scratch_address(int device) {
     require(device >= 0 && device < MAX_DEVICES, "device index out of range");
     std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -56,6 +60,7 @@ BEM_API bem_status bem_gmres_solve_noalloc(bem_ctx* ctx, int64_t n, const bem_cp
         report->rel_err_vs_lu = -1;
     }
     Context& c = ctx->c;
+    const auto t0 = std::chrono::steady_clock::now();
     try {
         BEM_CUDA(cudaSetDevice(c.device));
         // the restart rule of gmres.rs:41-48
@@ -91,6 +96,7 @@ BEM_API bem_status bem_gmres_solve_noalloc(bem_ctx* ctx, int64_t n, const bem_cp
             report->iterations = st.iterations;
             report->backward_error = st.error;
             report->flag = st.converged ? 1 : 2;
+            report->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         }
         return st.converged ? BEM_OK : BEM_ERR_NOT_CONVERGED;
     } catch (const Error& e) {

@@ -5,8 +5,8 @@
  * The reference is a pure-Rust crate whose hot-path boundary is its module API
  * (influence_matrix / solve / postprocess, driven by analysis.rs).  Every entry
  * point below replaces one of those functions; the comment gives the reference
- * file:line.  A Rust crate would bind these with `extern "C"` declarations
- * (see INTEGRATION.md).
+ * file:line.  A Rust crate binds these with `extern "C"` declarations of the
+ * same signatures.
  *
  * Conventions
  *  - Complex values are interleaved {re, im} doubles (bem_cplx), matching
@@ -208,9 +208,13 @@ BEM_API bem_status bem_gmres_solve(bem_ctx* ctx, int64_t n, const bem_cplx* A, i
  * fixed-budget loop, where a cudaMalloc would synchronise the device or fail.
  * Limit: n up to 4096 at any iteration limit; sizes whose workspace exceeds the
  * array are rejected with BEM_ERR_BAD_INPUT before any work is issued.  The
- * first call on each device looks up the array's device address; make that
- * first call before any stream capture.  Every call uses the same array, so
- * calls that overlap on the GPU (other threads, other streams) race. */
+ * first call on each device looks up the array's device address and keeps it
+ * for the life of the process; make that first call before any stream capture,
+ * and do not use this entry point after a cudaDeviceReset in the same process.
+ * The call synchronises the context's stream after every iteration (it reads
+ * the convergence state on the host) and fills report->seconds like
+ * bem_gmres_solve.  Every call uses the same array, so calls that overlap on
+ * the GPU (other threads, other streams) race. */
 BEM_API bem_status bem_gmres_solve_noalloc(bem_ctx* ctx, int64_t n, const bem_cplx* A, int64_t lda,
                                            int64_t max_it, double tol, bem_cplx* x, bem_solve_report* report);
 /* solve.rs:173-185 get_field: out = [phi_inc if Total] - M phi + L vn. */
@@ -224,6 +228,27 @@ BEM_API bem_status bem_evaluate_field(bem_ctx* ctx, const bem_problem* p, const 
                                       const bem_cplx* vn, const bem_cplx* phi_inc_fp, bem_cplx* out);
 /* postprocess.rs:83-87 convert_phi_to_pressure_vec: v *= i omega rho. */
 BEM_API bem_status bem_convert_to_pressure(const bem_problem* p, double frequency, bem_cplx* v, int64_t n);
+
+/* ---- output (postprocess.rs:15-67) --------------------------------------- */
+/* postprocess.rs:15-44 write_results_at_frequency: one CSV record per field
+ * point (index, x, y, z, pre_re/vpo_re, pre_im/vpo_im, inc_re, inc_im) of one
+ * frequency's results (nfp entries each, host memory, as bem_run leaves them:
+ * pressure or potential).  path NULL: the input's output.file.  Numbers as
+ * Rust's f64 Display writes them (see bem_format_f64); records end in "\n".
+ * ctx (may be NULL) receives the error message. */
+BEM_API bem_status bem_write_results_at_frequency(bem_ctx* ctx, const bem_problem* p, const char* path,
+                                                  const bem_cplx* scattered, const bem_cplx* incident);
+/* postprocess.rs:46-67 write_results_at_point: one CSV record per frequency
+ * (freq, pre_re/vpo_re, pre_im/vpo_im, inc_re, inc_im) for field point
+ * `index`; scattered and incident are num_frequencies x nfp (field point
+ * fastest, one wave), as bem_run fills them. */
+BEM_API bem_status bem_write_results_at_point(bem_ctx* ctx, const bem_problem* p, const char* path, int64_t index,
+                                              const bem_cplx* scattered, const bem_cplx* incident);
+/* The number format of the CSV writers: Rust's `f64::to_string()` (shortest
+ * round-trip digits, positional notation, no ".0" on integral values, "NaN",
+ * "inf").  Writes at most len - 1 characters and a terminating NUL into buf;
+ * returns the full length (or -1). */
+BEM_API int64_t bem_format_f64(double v, char* buf, int64_t len);
 
 /* ---- driver (analysis.rs:57-118) --------------------------------------- */
 /* Runs every frequency of the problem.  scattered and incident are
@@ -277,6 +302,28 @@ BEM_API bem_status bem_learned_mlp_eval(bem_ctx* ctx, int64_t P, const float* fe
 /* Network outputs (P x 2) by the tensor-core (tcgen05) inference kernel that
  * bem_run uses to emit the learned preconditioner entries. */
 BEM_API bem_status bem_learned_mlp_infer(bem_ctx* ctx, int64_t P, const float* features, float* out);
+
+/* ---- LU preconditioner kernels (instrumentation; no reference counterpart) */
+/* The LU preconditioner's factorization (TF32 tensor-core trailing updates,
+ * no pivoting, blocks of 128) and one application z = U^-1 L^-1 q, on
+ * caller-given operators, with everything read back, so the device kernels
+ * can be compared entry by entry with an FP64 LU.  System s has n[s] unknowns
+ * and its complex FP32 matrix (interleaved {re, im}, column-major, leading
+ * dimension ld[s]) at complex offset a_off[s] of the host array A (a_entries
+ * complex entries); ld[s] and a_off[s] are multiples of 64; systems with the
+ * same a_off share one operator (several right-hand sides).  F (may be NULL)
+ * receives A's layout holding, per block row/column of 128, L21 below the
+ * diagonal blocks, U12 above them and the updated diagonal blocks
+ * (L_bb U_bb).  D (may be NULL; d_entries complex entries) receives per
+ * factored operator, in order of first appearance, one 128 x 128 column-major
+ * tile per diagonal block: L_bb^-1 strictly below the diagonal (unit diagonal
+ * implied) and U_bb^-1 on and above it.  q and z (may be NULL) are the
+ * systems' vectors back to back (sum of n[s] complex doubles); z receives
+ * M q.  small_pivots (may be NULL) receives the number of pivots replaced. */
+BEM_API bem_status bem_lu32_factor_apply(bem_ctx* ctx, int nsys, const int64_t* n, const int64_t* ld,
+                                         const int64_t* a_off, int64_t a_entries, const float* A, float* F,
+                                         float* D, int64_t d_entries, const bem_cplx* q, bem_cplx* z,
+                                         int* small_pivots);
 
 /* ---- H-matrix (h_matrix.rs, aca.rs, cluster.rs, block.rs) -------------- */
 /* h_matrix.rs:127-148 HMatrix::new_from over the problem's collocation points

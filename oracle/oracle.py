@@ -472,3 +472,52 @@ def block_tree_path_admissible(points, leaf, eta, path):
     pts = np.ascontiguousarray(points, dtype=float)
     p = np.ascontiguousarray(path, dtype=np.int32)
     return lib().oc_block_tree_path_admissible(len(pts), _ptr(pts), pts.shape[1], leaf, eta, _ptr(p), len(p))
+
+
+# ---- postprocess.rs:15-67: the CSV writers ----------------------------------
+def rust_f64_display(v):
+    """Rust's `f64::to_string()` (core::fmt Display for f64): the shortest
+    round-trip digits (Python's repr finds the same digits) laid out without an
+    exponent, integral values without a decimal point, NaN / inf / -inf."""
+    import decimal
+    v = float(v)
+    if v != v:
+        return "NaN"
+    if v in (float("inf"), float("-inf")):
+        return "inf" if v > 0 else "-inf"
+    d = decimal.Decimal(repr(v))
+    sign, digits, exp = d.as_tuple()
+    ds = "".join(map(str, digits)).lstrip("0") or "0"
+    # value = ds * 10**exp with ds stripped of leading zeros; drop trailing zeros
+    # of the digit string into the exponent
+    stripped = ds.rstrip("0") or "0"
+    exp += len(ds) - len(stripped)
+    ds = stripped
+    if ds == "0":
+        body = "0"
+    elif exp >= 0:
+        body = ds + "0" * exp
+    else:
+        point = len(ds) + exp  # digits before the decimal point
+        body = ("0." + "0" * (-point) + ds) if point <= 0 else ds[:point] + "." + ds[point:]
+    return ("-" if sign else "") + body
+
+
+def csv_results_at_frequency(field_points, scattered, incident, pressure=True):
+    """The bytes of postprocess.rs:15-44 (csv 1.3.1 Writer: comma, "\\n")."""
+    on = "pre" if pressure else "vpo"
+    f = rust_f64_display
+    lines = ["index,x,y,z,%s_re,%s_im,inc_re,inc_im" % (on, on)]
+    for i, (p, s, c) in enumerate(zip(field_points, scattered, incident)):
+        lines.append(",".join([str(i), f(p[0]), f(p[1]), f(p[2]), f(s.real), f(s.imag), f(c.real), f(c.imag)]))
+    return ("\n".join(lines) + "\n").encode()
+
+
+def csv_results_at_point(freqs, scattered, incident, index, pressure=True):
+    """The bytes of postprocess.rs:47-67; scattered / incident: nfreq x nfp."""
+    on = "pre" if pressure else "vpo"
+    f = rust_f64_display
+    lines = ["freq,%s_re,%s_im,inc_re,inc_im" % (on, on)]
+    for fr, s, c in zip(freqs, scattered, incident):
+        lines.append(",".join([f(fr), f(s[index].real), f(s[index].imag), f(c[index].real), f(c[index].imag)]))
+    return ("\n".join(lines) + "\n").encode()

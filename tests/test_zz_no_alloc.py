@@ -3,11 +3,13 @@ allocate device memory at solve time (their device memory is handed to their
 own pool up front, or they run under a fixed memory budget).  Its working
 memory is a fixed array inside the library, so each call only launches kernels.
 
-The checks: called through the C ABI with device buffers, two calls in a row
-(different sizes, so the second runs over the first call's leftovers) give the
-same answer and mat-vec count as bem_gmres_solve; the second call leaves the
-device's free memory unchanged; a size beyond the array is refused up front.
-This file is collected last so a failure here comes after every other test.
+The checks: called through the C ABI with device buffers, calls in a row of
+growing size (each runs over the previous call's leftovers, and a hidden
+allocation that grows with n would show on the later, larger calls) give the
+same answer and mat-vec count as bem_gmres_solve; the calls after the first
+leave the device's free memory unchanged; a size beyond the array is refused up
+front.  This file is collected last so a failure here comes after every other
+test.
 """
 import ctypes as C
 
@@ -34,11 +36,13 @@ def _noalloc(ctx, Ad, bd, n, max_it, tol):
     return st, rep
 
 
-def test_noalloc_matches_gmres_two_calls():
+def test_noalloc_matches_gmres_calls_in_a_row():
     ctx = bem.Context.default()
-    cases = [(300, 3, 300, 1e-10), (100, 10, 100, 1e-8)]  # larger system first, then the golden one
-    free_between = []
-    for n, seed, max_it, tol in cases:
+    # the reference's golden system first, then larger ones (n = 4096 is the
+    # stated limit at any iteration count)
+    cases = [(100, 10, 100, 1e-8), (300, 3, 300, 1e-10), (4096, 7, 4096, 1e-10)]
+    free = []
+    for i, (n, seed, max_it, tol) in enumerate(cases):
         A, b = O.generate_random_ab(n, n, seed)
         Ad = _device_matrix(A)
         xd = torch.from_numpy(np.ascontiguousarray(b)).cuda()
@@ -46,17 +50,21 @@ def test_noalloc_matches_gmres_two_calls():
         free_before = torch.cuda.mem_get_info()[0]
         st, rep = _noalloc(ctx, Ad, xd, n, max_it, tol)
         torch.cuda.synchronize()
-        free_between.append((free_before, torch.cuda.mem_get_info()[0]))
+        free.append((free_before, torch.cuda.mem_get_info()[0]))
         assert st == 0, ctx.lib.bem_last_error(ctx.h)
         x_ref, rep_ref = bem.gmres(A, b, max_it, tol, ctx=ctx)
         x = xd.cpu().numpy()
         assert rep.num_mv == rep_ref["num_mv"] and rep.flag == 1
+        assert rep.seconds > 0.0
         assert np.max(np.abs(x - x_ref)) <= 1e-12 * np.max(np.abs(x_ref))
+        if i == 0:
+            # the golden value of src/solve.rs:220-228 (1e-6)
+            assert abs(x[0] - (0.0035386336544537098 + 0.0017794290945383035j)) < 1e-6
+        del Ad, xd
     # the first call on a device resolves the array's address (and may load the
-    # library's device image); the second call must not change free memory
-    assert free_between[1][0] == free_between[1][1]
-    # the golden value of src/solve.rs:220-228 (1e-6) for the second system
-    assert abs(x[0] - (0.0035386336544537098 + 0.0017794290945383035j)) < 1e-6
+    # library's device image); the later, larger calls must not change free memory
+    for before, after in free[1:]:
+        assert before == after, free
 
 
 def test_noalloc_rejects_oversized_problem():
