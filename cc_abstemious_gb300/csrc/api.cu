@@ -117,31 +117,36 @@ void unpack_solution(Context& c, const Problem& p, const double2* x, double2* ph
 // Dense plain-FP64 surface solve on device vectors (solve.rs:24-71 and
 // :153-171): the fused kernel assembles the system matrix alpha H + beta G and
 // the uniform-BC right-hand side in one pass.
+// reuse_lu (Direct solver only): the previous call factored this frequency's
+// operator into the context's buffers (w_mat, w_piv, and the boundary
+// condition's row sums in w_vec); only the right-hand side is new (several
+// incident waves share one factorization).
 void solve_surface_dense_fp64(Context& c, const Problem& p, const double2* d_rhs_inc, double2* d_phi,
-                              double2* d_vn, bem_solve_report* rep, double2* d_A_keep) {
+                              double2* d_vn, bem_solve_report* rep, double2* d_A_keep, bool reuse_lu) {
     int64_t n = p.n;
     cd a, b, g, d;
     lhs_factors(p, a, b);
     rhs_factors(p, g, d);
     bool need_rowsum = !(p.in.bc_value[0] == 0.0 && p.in.bc_value[1] == 0.0) && p.in.bc_type != 2;
+    reuse_lu = reuse_lu && p.in.solver == 0 && !d_A_keep;
     double2* A = d_A_keep;
     if (!A) {
-        c.w_mat.ensure(sizeof(double2) * (size_t)n * n);
+        if (!reuse_lu) c.w_mat.ensure(sizeof(double2) * (size_t)n * n);
         A = c.w_mat.as<double2>();
     }
-    c.w_vec.ensure(sizeof(double2) * (size_t)n * 4);
+    if (!reuse_lu) c.w_vec.ensure(sizeof(double2) * (size_t)n * 4);
     double2* rowsum = c.w_vec.as<double2>();
     double2* x = rowsum + n;
-    assemble_system_fp64(c, p, A, n, a, b, g, d, need_rowsum ? rowsum : nullptr);
+    if (!reuse_lu) assemble_system_fp64(c, p, A, n, a, b, g, d, need_rowsum ? rowsum : nullptr);
     double s = p.in.bc_type == 0 ? 1.0 : -1.0;
     launch_rhs_combine(c, n, s, d_rhs_inc, {p.in.bc_value[0], p.in.bc_value[1]}, need_rowsum ? rowsum : nullptr, x);
     if (p.in.solver == 0) {
-        c.w_small.ensure(sizeof(int32_t) * (size_t)n + 64);
-        DevBuf piv;
-        piv.ensure(sizeof(int32_t) * (size_t)n);
         c.w_flags.ensure(256);
-        lu_factor_fp64(c, n, A, n, piv.as<int32_t>(), c.w_flags.as<int>() + 1);
-        lu_solve_fp64(c, n, A, n, piv.as<int32_t>(), x);
+        if (!reuse_lu) {
+            c.w_piv.ensure(sizeof(int32_t) * (size_t)n);
+            lu_factor_fp64(c, n, A, n, c.w_piv.as<int32_t>(), c.w_flags.as<int>() + 1);
+        }
+        lu_solve_fp64(c, n, A, n, c.w_piv.as<int32_t>(), x);
         int info = 0;
         to_host(c, &info, c.w_flags.as<int>() + 1, sizeof(int));
         if (rep) rep->flag = 3;
@@ -163,7 +168,7 @@ void solve_surface_dense_fp64(Context& c, const Problem& p, const double2* d_rhs
 void solve_surface_fp64(Context& c, const Problem& p, const double2* d_rhs_inc, double2* d_phi, double2* d_vn,
                         bem_solve_report* rep) {
     if (p.in.solver == 2) solve_surface_hmatrix(c, p, d_rhs_inc, d_phi, d_vn, rep);
-    else solve_surface_dense_fp64(c, p, d_rhs_inc, d_phi, d_vn, rep, nullptr);
+    else solve_surface_dense_fp64(c, p, d_rhs_inc, d_phi, d_vn, rep, nullptr, false);
 }
 
 static void load_problem(Context& c, Problem& p, const std::string& json, const std::string& base_dir) {
@@ -680,16 +685,19 @@ BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* pp, bem_form form, bem_pre
         c.last_n = n;
         c.last_nf = nf;
         int64_t saved = p.ifreq;
-        // one right-hand side after the other, each as the reference would run it
-        for (int64_t r = 0; r < nrhs; ++r)
-        for (int64_t f0 = 0; f0 < nf; ++f0) {
+        // every right-hand side as the reference would run it; with the
+        // Direct solver the waves of a frequency share its LU factorization
+        // (the same factors and the same answer as factoring per wave)
+        for (int64_t f0 = 0; f0 < nf; ++f0)
+        for (int64_t r = 0; r < nrhs; ++r) {
             p.select_rhs(r);
             p.ifreq = f0;
             const int64_t f = r * nf + f0;  // output slot
             auto t0 = std::chrono::steady_clock::now();
             incident_surface(c, p, rhs);
             bem_solve_report* rep = reports ? &reports[f] : nullptr;
-            solve_surface_fp64(c, p, rhs, phi, vn, rep);
+            if (p.in.solver == 2) solve_surface_hmatrix(c, p, rhs, phi, vn, rep);
+            else solve_surface_dense_fp64(c, p, rhs, phi, vn, rep, nullptr, r > 0 && !check_vs_lu);
             incident_field(c, p, inc);
             evaluate_field(c, p, phi, vn, p.in.output_total ? inc : nullptr, fps);
             std::vector<double2> hs((size_t)nfp), hi((size_t)nfp);

@@ -190,6 +190,7 @@ struct Context {
     // every mixed solve)
     DevBuf w_gm, w_gmz, w_lu_F, w_lu_D, w_lu_W, w_lu_P;
     DevBuf w_upload;  // mesh staging of problem construction
+    DevBuf w_piv;     // row pivots of the plain form's FP64 LU
     // results of the last bem_run
     std::vector<double> last_phi, last_vn;
     int64_t last_n = 0, last_nf = 0;

@@ -21,6 +21,6 @@ void unpack_solution(Context& c, const Problem& p, const double2* x, double2* ph
 void launch_rhs_combine(Context& c, int64_t n, double s, const double2* inc, cd bc, const double2* rowsum,
                         double2* out);
 void solve_surface_dense_fp64(Context& c, const Problem& p, const double2* d_rhs_inc, double2* d_phi,
-                              double2* d_vn, bem_solve_report* rep, double2* d_A_keep);
+                              double2* d_vn, bem_solve_report* rep, double2* d_A_keep, bool reuse_lu = false);
 
 }  // namespace bem
