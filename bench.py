@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--nfreq", type=int, default=16)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="one mixed run (for ncu launch lists)")
+    ap.add_argument("--hierarchical", action="store_true",
+                    help="with --profile-only: the H-matrix operators (leaf 64, eta 1, ACA 1e-5) instead of dense")
     ap.add_argument("--workload", default=WORKLOAD,
                     choices=[WORKLOAD, "perturbed_spheres", "held_out_learned", "ellipsoid_bm"],
                     help="rigid_sphere_bm (the metric's configuration, default); perturbed_spheres (bodies of "
@@ -306,6 +308,10 @@ def main():
     from cc_abstemious_gb300 import workloads
     workdir = tempfile.mkdtemp(prefix="bem_bench_")
     inp = workloads.rigid_sphere_bm(workdir, m=args.mesh_m, nfreq=args.nfreq)
+    if args.profile_only and args.hierarchical:
+        # the mixed form over ACA-compressed operators (leaf 64, eta 1, ACA 1e-5)
+        inp["solver"] = {"Hierarchical": {"tolerance": 1e-8, "max_iterations": 2500, "leaf_size": 64, "eta": 1.0,
+                                          "aca_tolerance": 1e-5}}
     if args.impl == "reference":
         run_reference_arm(args, inp)
         return
@@ -622,23 +628,30 @@ def target_held_out(sh):
     held = workloads.perturbed_sphere_input(sh.wd, 777777, a.held_out_tri, kas, tol=1e-8)
     held["solver"]["Iterative"]["max_iterations"] = 20000
     pd = bem.PreData.from_dict(held, ctx=ctx)
+    # the near-field preconditioners stop at backward error 1e-10: at 1e-8
+    # their forward error reached 2e-5 at ka 16 (the LU form overshoots 1e-8
+    # by orders in its last iteration and stays near 1e-7)
+    tight = json.loads(json.dumps(held))
+    tight["solver"]["Iterative"]["tolerance"] = 1e-10
+    pd_t = bem.PreData.from_dict(tight, ctx=ctx)
     nf, n = len(pd.frequencies), pd.n
     sc = np.zeros((nf, pd.nfp), dtype=np.complex128)
     inc = np.zeros_like(sc)
     forms = {}
     phis = {}
-    for name, form, code in (("mixed+lu", bem.FORM_MIXED, 3), ("mixed+learned", bem.FORM_MIXED, 2),
-                             ("mixed+block_jacobi", bem.FORM_MIXED, 1)):
+    for name, form, code, p in (("mixed+lu", bem.FORM_MIXED, 3, pd), ("mixed+learned", bem.FORM_MIXED, 2, pd_t),
+                                ("mixed+block_jacobi", bem.FORM_MIXED, 1, pd_t)):
         reps = (bem.SolveReport * nf)()
 
         def step():
-            ctx.check(ctx.lib.bem_run(ctx.h, pd.h, form, code, bem._ptr(sc), bem._ptr(inc), reps, 0))
+            ctx.check(ctx.lib.bem_run(ctx.h, p.h, form, code, bem._ptr(sc), bem._ptr(inc), reps, 0))
 
         l0 = ctx.kernel_launches
         ms, clk = _timed_region(a, sh.local, step, sh.stream, a.target_steps, a.target_warmup)
         launches = (ctx.kernel_launches - l0) // (a.target_steps + a.target_warmup)
-        phis[name] = _surface(ctx, pd, 1, nf)
+        phis[name] = _surface(ctx, p, 1, nf)
         forms[name] = {"value": nf * 1000.0 / ms, "unit": UNIT, "ms_per_step": ms, "clocks": clk,
+                       "gmres_tol": 1e-8 if p is pd else 1e-10,
                        "gpu_launches": launches, "iterations": [reps[i].iterations for i in range(nf)],
                        "converged": all(reps[i].flag == 1 for i in range(nf)),
                        "precond_used": [reps[i].precond for i in range(nf)]}
@@ -673,7 +686,8 @@ def target_held_out(sh):
         "workload": "held_out_learned", "value": forms[best]["value"] if best else None, "unit": UNIT,
         "best_form": best, "steps": a.target_steps, "warmup": a.target_warmup,
         "config": {"n_unknowns": n, "frequencies": nf, "ka": [4.0, 16.0], "bc": "impedance rho c (1 + 0.2i)",
-                   "solver": "GMRES tol 1e-8 (backward error), restart 142", "training": training},
+                   "solver": "GMRES backward error 1e-8 (LU form) or 1e-10 (near-field preconditioners), "
+                             "restart 142", "training": training},
         "forms": forms, "plain_fp64": plain,
         "speedup_vs_plain_fp64": forms[best]["value"] / plain["value"] if best else None,
         "learned_vs_plain_fp64": learned["value"] / plain["value"],

@@ -99,6 +99,10 @@ SIGNATURES = {
     "bem_hmatrix_norm": (_d, [_vp]),
     "bem_hmatrix_stats": (_i, [_vp, _vp]),
     "bem_hmatrix_to_full": (_i, [_vp, _vp, _vp, _i64]),
+    "bem_ctx_load_tuning": (_i, [_vp, C.c_char_p]),
+    "bem_ctx_set_tuning": (_i, [_vp, C.c_char_p, C.c_char_p, _i]),
+    "bem_ctx_get_tuning": (_i, [_vp, C.c_char_p, C.c_char_p, _i64, _i64]),
+    "bem_ctx_tuning_source": (C.c_char_p, [_vp]),
     "bem_ctx_set_profiling": (_i, [_vp, _i]),
     "bem_ctx_stream": (_vp, [_vp]),
     "bem_ctx_profile_count": (_i64, [_vp]),

@@ -1,6 +1,7 @@
 // C ABI of libbem_gb300.so (include/bem.h): context, problem (UserInput +
 // PreData), the influence_matrix / incident_wave / solve / postprocess entry
 // points and the analysis driver.
+#include <dlfcn.h>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -171,6 +172,39 @@ void solve_surface_fp64(Context& c, const Problem& p, const double2* d_rhs_inc, 
     else solve_surface_dense_fp64(c, p, d_rhs_inc, d_phi, d_vn, rep, nullptr, false);
 }
 
+// The built-in launch parameters (used where no tuning entry applies).
+int tuning_default(const std::string& kernel, const std::string& param) {
+    if (kernel == "lu_gemm_trail") return param == "sb_r" ? 8 : param == "sb_c" ? 32 : -1;
+    if (kernel == "gm_apply_fp32" && param == "unroll") return 8;
+    if (kernel == "assemble32" && param == "min_ctas") return 3;
+    return -1;
+}
+
+// tuning.json in the directory of this library.
+static std::string default_tuning_path() {
+    Dl_info info;
+    if (!dladdr(reinterpret_cast<void*>(&tuning_default), &info) || !info.dli_fname) return "";
+    std::string so = info.dli_fname;
+    const size_t slash = so.rfind('/');
+    const std::string dir = slash == std::string::npos ? "." : so.substr(0, slash);
+    const std::string path = dir + "/tuning.json";
+    std::ifstream f(path);
+    return f.good() ? path : "";
+}
+
+// Reads a tuning table; a missing file is an error only when it was asked for.
+static void load_tuning_file(Context& c, const std::string& path, bool required) {
+    std::ifstream f(path);
+    if (!f.good()) {
+        require(!required, "cannot open tuning table " + path);
+        return;
+    }
+    std::stringstream ss;
+    ss << f.rdbuf();
+    c.tuning.entries = parse_tuning(ss.str());
+    c.tuning.source = path;
+}
+
 static void load_problem(Context& c, Problem& p, const std::string& json, const std::string& base_dir) {
     p.in = parse_user_input(json);
     std::string path = p.in.mesh_file;
@@ -203,10 +237,47 @@ BEM_API bem_status bem_ctx_create(int device, bem_ctx** out) {
         ctx->c.device = device;
         set_device(ctx->c);
         BEM_CUDA(cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking));
+        // the tuned launch table: BEM_TUNING_FILE ("none": built-in
+        // defaults), else tuning.json beside the library when present
+        const char* env = std::getenv("BEM_TUNING_FILE");
+        std::string path = env ? env : default_tuning_path();
+        if (!path.empty() && path != "none") load_tuning_file(ctx->c, path, env != nullptr);
     });
     if (st == BEM_OK) *out = ctx.release();
     return st;
 }
+
+BEM_API bem_status bem_ctx_load_tuning(bem_ctx* ctx, const char* path) {
+    if (!ctx) return BEM_ERR_BAD_INPUT;
+    return guard(ctx, [&] {
+        if (!path) {
+            ctx->c.tuning.entries.clear();
+            ctx->c.tuning.source.clear();
+            return;
+        }
+        load_tuning_file(ctx->c, path, true);
+    });
+}
+
+BEM_API bem_status bem_ctx_set_tuning(bem_ctx* ctx, const char* kernel, const char* param, int value) {
+    if (!ctx || !kernel || !param) return BEM_ERR_BAD_INPUT;
+    auto& ov = ctx->c.tuning.overrides;
+    const std::string key = std::string(kernel) + "." + param;
+    for (size_t i = 0; i < ov.size(); ++i)
+        if (ov[i].first == key) {
+            ov.erase(ov.begin() + (long)i);
+            break;
+        }
+    if (value >= 0) ov.emplace_back(key, value);
+    return BEM_OK;
+}
+
+BEM_API int bem_ctx_get_tuning(const bem_ctx* ctx, const char* kernel, const char* param, int64_t n, int64_t nsys) {
+    if (!ctx || !kernel || !param) return -1;
+    return ctx->c.tuning.pick(kernel, param, n, nsys, tuning_default(kernel, param));
+}
+
+BEM_API const char* bem_ctx_tuning_source(const bem_ctx* ctx) { return ctx ? ctx->c.tuning.source.c_str() : ""; }
 
 BEM_API void bem_ctx_destroy(bem_ctx* ctx) {
     if (!ctx) return;

@@ -332,8 +332,10 @@ __device__ __forceinline__ void assemble32_tile(int64_t n, int64_t npad, const f
     }
 }
 
-template <int WITH_RHS>
-__global__ void __launch_bounds__(ASM_THREADS, 3) assemble32_kernel(
+// MINB: CTAs per SM the register allocation must allow (tuned per size:
+// more CTAs hide latency, fewer registers per thread cost spills and ILP).
+template <int WITH_RHS, int MINB = 3>
+__global__ void __launch_bounds__(ASM_THREADS, MINB) assemble32_kernel(
     int64_t n, int64_t npad, const float* __restrict__ g32, const double* __restrict__ geo, Asm32Params prm,
     float2* __restrict__ A, int64_t ld, size_t mat_stride, double2* __restrict__ part, size_t part_stride,
     double* __restrict__ norm_part, int* __restrict__ err) {
@@ -448,8 +450,16 @@ void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks,
                 launch_reduce_parts(ctx, p.n, p.geo.npad, ntiles, part + s * pstride,
                                     rowsum + (size_t)(s0 + s) * vec_stride);
         } else {
-            assemble32_kernel<0><<<grid, ASM_THREADS, 0, ctx.stream>>>(
-                p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0), prm, As, ld, mat_stride, nullptr, 0, np_, err);
+            const int minb = ctx.tuning.pick("assemble32", "min_ctas", p.n, nsys, 3);
+            if (minb == 2)
+                assemble32_kernel<0, 2><<<grid, ASM_THREADS, 0, ctx.stream>>>(
+                    p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0), prm, As, ld, mat_stride, nullptr, 0, np_, err);
+            else if (minb == 4)
+                assemble32_kernel<0, 4><<<grid, ASM_THREADS, 0, ctx.stream>>>(
+                    p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0), prm, As, ld, mat_stride, nullptr, 0, np_, err);
+            else
+                assemble32_kernel<0, 3><<<grid, ASM_THREADS, 0, ctx.stream>>>(
+                    p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0), prm, As, ld, mat_stride, nullptr, 0, np_, err);
             BEM_CHECK_LAUNCH(&ctx);
         }
         if (norms) {

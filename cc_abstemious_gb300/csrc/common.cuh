@@ -165,7 +165,32 @@ struct Stage {
 
 struct LearnedNet;
 
+// Launch parameters chosen by the offline sweep (cc_abstemious_gb300/tune.py
+// writes tuning.json beside the library): per kernel, entries keyed by the
+// problem size n and the number of systems; a lookup takes the nearest entry
+// (log distance), else the built-in default.  Overrides (set through the C
+// ABI, used by the sweep itself) take precedence.
+struct TuneEntry {
+    std::string kernel;
+    int64_t n = 0, nsys = 0;
+    std::vector<std::pair<std::string, int>> params;
+};
+struct TuningTable {
+    std::vector<TuneEntry> entries;
+    std::string source;  // file the table was read from ("" : built-in defaults)
+    std::vector<std::pair<std::string, int>> overrides;  // "kernel.param" -> value
+    int get(const char* kernel, const char* param, int64_t n, int64_t nsys, int dflt) const;
+    int pick(const char* kernel, const char* param, int64_t n, int64_t nsys, int dflt) const {
+        const std::string key = std::string(kernel) + "." + param;
+        for (auto& kv : overrides)
+            if (kv.first == key) return kv.second;
+        return get(kernel, param, n, nsys, dflt);
+    }
+};
+std::vector<TuneEntry> parse_tuning(const std::string& text);
+
 struct Context {
+    TuningTable tuning;
     int device = 0;
     bool profiling = false;
     std::shared_ptr<LearnedNet> net;  // preconditioner network (trained or loaded)

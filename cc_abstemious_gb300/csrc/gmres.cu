@@ -84,8 +84,9 @@ __device__ __forceinline__ float4 ff_split(double2 x) {
 //        the exact residual at each check and restart keeps the answer exact.
 constexpr int MV_UNROLL = 8;
 
-template <typename T, int EXACT>
+template <typename T, int EXACT, int U = MV_UNROLL>
 __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mode) {
+    static_assert(MV_COLS % U == 0, "the column chunk is a whole number of unrolled groups");
     int s, bx, by;
     if (bt.sys) {
         // ragged batch: one flattened grid over every system's (row block,
@@ -141,10 +142,10 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
             const float2* A = reinterpret_cast<const float2*>(bt.A) + g.a + i0;
             // float-float accumulators for (re0, im0, re1, im1)
             float h0 = 0, l0 = 0, h1 = 0, l1 = 0, h2 = 0, l2 = 0, h3 = 0, l3 = 0;
-            for (int q0 = 0; q0 < jn; q0 += MV_UNROLL) {
-                float4 a[MV_UNROLL];
+            for (int q0 = 0; q0 < jn; q0 += U) {
+                float4 a[U];
 #pragma unroll
-                for (int u = 0; u < MV_UNROLL; ++u) {
+                for (int u = 0; u < U; ++u) {
                     const int q = q0 + u;
                     if (q < jn) {
                         const float2* col = A + (j0 + q) * lda;
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
                 }
                 if (EXACT) {
 #pragma unroll
-                    for (int u = 0; u < MV_UNROLL; ++u) {
+                    for (int u = 0; u < U; ++u) {
                         const float2 H = xh[q0 + u], L = xl[q0 + u];
                         const float4 w = a[u];
                         ff_acc(h0, l0, w.x, H.x); ff_acc(h0, l0, -w.y, H.y);
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
                 } else {
                     float b0 = 0, b1 = 0, b2 = 0, b3 = 0;
 #pragma unroll
-                    for (int u = 0; u < MV_UNROLL; ++u) {
+                    for (int u = 0; u < U; ++u) {
                         const float2 H = xh[q0 + u];
                         const float4 w = a[u];
                         b0 = fmaf(w.x, H.x, fmaf(-w.y, H.y, b0));
@@ -190,17 +191,17 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
             r1 = make_double2((double)h2 + (double)l2, (double)h3 + (double)l3);
         } else {
             const double2* A = reinterpret_cast<const double2*>(bt.A) + g.a + i0;
-            for (int q0 = 0; q0 < jn; q0 += MV_UNROLL) {
-                double2 a0[MV_UNROLL], a1[MV_UNROLL];
+            for (int q0 = 0; q0 < jn; q0 += U) {
+                double2 a0[U], a1[U];
 #pragma unroll
-                for (int u = 0; u < MV_UNROLL; ++u) {
+                for (int u = 0; u < U; ++u) {
                     const int q = q0 + u;
                     const double2* col = A + (j0 + (q < jn ? q : 0)) * lda;
                     a0[u] = q < jn ? col[0] : make_double2(0, 0);
                     a1[u] = (q < jn && pair) ? col[1] : make_double2(0, 0);
                 }
 #pragma unroll
-                for (int u = 0; u < MV_UNROLL; ++u) {
+                for (int u = 0; u < U; ++u) {
                     const double2 xv = xd[q0 + u];
                     cfma(r0, a0[u], xv);
                     cfma(r1, a1[u], xv);
@@ -861,8 +862,15 @@ static void launch_apply(Context& ctx, GmWorkspace& ws, int mode) {
     }
     dim3 grid = ws.bt.sys ? dim3((unsigned)ws.bt.ntiles) : dim3((unsigned)ws.rb, (unsigned)ws.cb, (unsigned)ws.bt.nsys);
     if (ws.fp32) {
-        if (mode == MV_Q) gm_apply_kernel<float2, 0><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
-        else gm_apply_kernel<float2, 1><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+        if (mode == MV_Q) {
+            // columns per load batch (loads in flight per thread), tuned per size
+            const int u = ctx.tuning.pick("gm_apply_fp32", "unroll", ws.bt.n, ws.bt.nsys, MV_UNROLL);
+            if (u == 4) gm_apply_kernel<float2, 0, 4><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+            else if (u == 16) gm_apply_kernel<float2, 0, 16><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+            else gm_apply_kernel<float2, 0, 8><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+        } else {
+            gm_apply_kernel<float2, 1><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+        }
     } else {
         gm_apply_kernel<double2, 1><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
     }
@@ -896,9 +904,80 @@ void gm_read_states(Context& ctx, GmWorkspace& ws, std::vector<GmState>& out) {
     ctx.sync();
 }
 
+// The solve graph's loop test, run on the device after every round of
+// `chunk` iterations: another round while some system is not done and the
+// round cap is not reached (no host round trip between rounds).
+__global__ void gm_continue_kernel(const GmState* __restrict__ st, int nsys, int* __restrict__ rounds, int max_rounds,
+                                   cudaGraphConditionalHandle handle) {
+    __shared__ int open;
+    if (threadIdx.x == 0) open = 0;
+    __syncthreads();
+    for (int s = threadIdx.x; s < nsys; s += blockDim.x)
+        if (!st[s].done) open = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int r = *rounds + 1;
+        *rounds = r;
+        cudaGraphSetConditional(handle, (open && r < max_rounds) ? 1u : 0u);
+    }
+}
+
+// The whole solve as one graph: a conditional WHILE node whose body is
+// `chunk` captured iterations plus the loop test.  Returns false (and leaves
+// no error pending) where the runtime cannot build it.
+static bool gm_build_solve_graph(Context& ctx, GmWorkspace& ws, int chunk, int max_rounds) {
+    cudaGraph_t g = nullptr;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaGraphConditionalHandle h;
+    cudaGraphNodeParams np = {};
+    cudaGraphNode_t node;
+    bool ok = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+    if (ok) {
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+    }
+    if (ok) {
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        ok = cudaStreamBeginCaptureToGraph(ctx.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+             cudaSuccess;
+        if (ok) {
+            const int64_t before = ctx.launches;
+            try {
+                for (int c = 0; c < chunk; ++c) gm_launch_iteration(ctx, ws, nullptr, nullptr);
+                gm_continue_kernel<<<1, 256, 0, ctx.stream>>>(ws.bt.st, ws.bt.nsys, ws.rounds.as<int>(), max_rounds,
+                                                              h);
+                BEM_CHECK_LAUNCH(&ctx);
+            } catch (...) {
+                cudaStreamEndCapture(ctx.stream, &body);  // leave the stream out of capture mode
+                cudaGraphDestroy(g);
+                ctx.launches = before;
+                throw;
+            }
+            ws.launches_per_graph = ctx.launches - before;
+            ctx.launches = before;
+            ok = cudaStreamEndCapture(ctx.stream, &body) == cudaSuccess;
+        }
+    }
+    if (ok) ok = cudaGraphInstantiate(&ws.graph_exec, g, 0) == cudaSuccess;
+    cudaGraphDestroy(g);
+    if (!ok) {
+        cudaGetLastError();
+        ws.graph_exec = nullptr;
+    }
+    return ok;
+}
+
 // Run to completion.  chunk == 0: one iteration at a time with a state read
-// after each; chunk > 0: a CUDA graph of `chunk` iterations, state read after
-// each graph launch.
+// after each; chunk > 0: the solve graph (device-side loop over rounds of
+// `chunk` iterations, one launch and one state read per solve), or where the
+// runtime lacks conditional graph nodes a graph of `chunk` iterations with a
+// state read after each launch.
 void gm_run(Context& ctx, GmWorkspace& ws, int chunk, int64_t max_total_iterations) {
     std::vector<GmState> st, prev;
     int64_t issued = 0;
@@ -922,14 +1001,15 @@ void gm_run(Context& ctx, GmWorkspace& ws, int chunk, int64_t max_total_iteratio
             if (ctx.profiling) {
                 float ms = 0;
                 BEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                double entries = 0;
+                double entries = 0, mvs = 0;
                 for (size_t s = 0; s < st.size(); ++s) {
                     const double ns = ws.sys_host.empty() ? (double)ws.bt.n : (double)ws.sys_host[s].n;
                     entries += (double)(st[s].iterations - prev[s].iterations) * ns * ns;
+                    mvs += (double)(st[s].iterations - prev[s].iterations);
                 }
                 if (entries > 0)
-                    ctx.stage_add(ws.fp32 ? "gmres_matvec_fp32" : "gmres_matvec_fp64", ms, 1,
-                                  entries * (ws.fp32 ? 8.0 : 16.0));
+                    ctx.stage_add(ws.mv_stage ? ws.mv_stage : (ws.fp32 ? "gmres_matvec_fp32" : "gmres_matvec_fp64"), ms,
+                                  1, ws.mv_bytes > 0 ? ws.mv_bytes * mvs : entries * (ws.fp32 ? 8.0 : 16.0));
                 if (ws.ev_p0 && entries > 0) {
                     float pms = 0;
                     BEM_CUDA(cudaEventElapsedTime(&pms, ws.ev_p0, ws.ev_p1));
@@ -948,9 +1028,25 @@ void gm_run(Context& ctx, GmWorkspace& ws, int chunk, int64_t max_total_iteratio
         ws.ev_p0 = ws.ev_p1 = nullptr;
         return;
     }
-    if (!ws.graph_exec || ws.graph_chunk != chunk) {
+    const int max_rounds = (int)std::min<int64_t>((max_total_iterations + chunk - 1) / chunk, 1 << 30);
+    if (!ws.graph_exec || ws.graph_chunk != chunk || ws.graph_rounds != max_rounds) {
         if (ws.graph_exec) cudaGraphExecDestroy(ws.graph_exec);
         ws.graph_exec = nullptr;
+        ws.rounds.ensure(sizeof(int));
+        ws.graph_loop = gm_build_solve_graph(ctx, ws, chunk, max_rounds);
+        ws.graph_chunk = chunk;
+        ws.graph_rounds = max_rounds;
+    }
+    if (ws.graph_loop) {
+        int rounds = 0;
+        BEM_CUDA(cudaMemsetAsync(ws.rounds.p, 0, sizeof(int), ctx.stream));
+        BEM_CUDA(cudaGraphLaunch(ws.graph_exec, ctx.stream));
+        BEM_CUDA(cudaMemcpyAsync(&rounds, ws.rounds.p, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+        ctx.sync();
+        ctx.launches += ws.launches_per_graph * rounds;
+        return;
+    }
+    if (!ws.graph_exec) {
         cudaGraph_t g;
         int64_t before = ctx.launches;
         BEM_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));

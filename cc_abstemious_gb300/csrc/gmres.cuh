@@ -127,8 +127,15 @@ struct GmWorkspace {
     int rb = 0, cb = 0;
     double* norm_part = nullptr;
     double* anorm = nullptr;
+    // operator applied through `hook`: bytes streamed per system and mat-vec
+    // and the profiling stage name of the Krylov mat-vec (0 / nullptr: the
+    // dense operator's n^2 entries)
+    double mv_bytes = 0;
+    const char* mv_stage = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
-    int graph_chunk = 0;
+    int graph_chunk = 0, graph_rounds = 0;
+    bool graph_loop = false;  // graph_exec is the whole solve (device-side loop)
+    DevBuf rounds;            // rounds the solve graph ran
     int64_t launches_per_graph = 0;
     ~GmWorkspace();
 };

@@ -957,6 +957,39 @@ std::unique_ptr<HMatrixDev> hmatrix_build(Context& c, const Problem& p, int side
     return H;
 }
 
+void hmatrix_gemv(Context& c, const HMatrixDev& H, cd alpha, const double2* x, cd beta, double2* b);
+
+// The built leaves for the mixed form's repacking (hmixed.cu): index lists,
+// ranks, norms and the device data of the FP64 build, kept alive by `keep`.
+HBuilt hmatrix_build_view(Context& c, const Problem& p, int side) {
+    std::shared_ptr<HMatrixDev> H(hmatrix_build(c, p, side).release());
+    HBuilt v;
+    v.n = H->n;
+    v.norm = H->norm;
+    v.leaves.reserve(H->leaves.size());
+    for (const HLeaf& L : H->leaves)
+        v.leaves.push_back(HLeafView{L.row_off, L.m, L.col_off, L.n, L.store_off, L.adm, L.kmax, L.rank, L.norm});
+    v.rows = H->rows;
+    v.cols = H->cols;
+    v.d_rows = H->d_rows.as<int64_t>();
+    v.d_cols = H->d_cols.as<int64_t>();
+    v.d_store = H->d_store.as<double2>();
+    v.keep = H;
+    return v;
+}
+
+// out = (alpha H + beta G) 1 with the FP64 H-matrix of `side`
+// (h_matrix.rs:218-234 applied to the constant vector), device memory.
+void hmatrix_row_sums(Context& c, const Problem& p, int side, double2* out) {
+    auto H = hmatrix_build(c, p, side);
+    DevBuf ones;
+    ones.ensure(sizeof(double2) * (size_t)p.n);
+    std::vector<double2> h((size_t)p.n, make_double2(1.0, 0.0));
+    BEM_CUDA(cudaMemcpyAsync(ones.p, h.data(), sizeof(double2) * (size_t)p.n, cudaMemcpyHostToDevice, c.stream));
+    hmatrix_gemv(c, *H, {1.0, 0.0}, ones.as<double2>(), {0.0, 0.0}, out);
+    c.sync();
+}
+
 // b = alpha H x + beta b on device vectors (h_matrix.rs:218-234).
 void hmatrix_gemv(Context& c, const HMatrixDev& H, cd alpha, const double2* x, cd beta, double2* b) {
     GmBatch none{};

@@ -577,6 +577,56 @@ static std::vector<double> linspace(double start, double end, int64_t n) {
     return x;
 }
 
+// Tuning table (tuning.json, written by cc_abstemious_gb300/tune.py):
+// {"entries": [{"kernel": K, "n": N, "nsys": S, "params": {name: int, ...}}, ...]}
+std::vector<TuneEntry> parse_tuning(const std::string& text) {
+    JValue root = JParser(text).parse();
+    require(root.kind == JValue::Object, "tuning table: expected an object");
+    const JValue* ents = root.get("entries");
+    require(ents && ents->kind == JValue::Array, "tuning table: missing `entries`");
+    std::vector<TuneEntry> out;
+    for (const JValue& e : ents->arr) {
+        require(e.kind == JValue::Object, "tuning table: entries must be objects");
+        TuneEntry t;
+        const JValue* k = e.get("kernel");
+        const JValue* n = e.get("n");
+        const JValue* ns = e.get("nsys");
+        const JValue* ps = e.get("params");
+        require(k && k->kind == JValue::String && n && n->kind == JValue::Number && ns &&
+                    ns->kind == JValue::Number && ps && ps->kind == JValue::Object,
+                "tuning table: an entry needs kernel, n, nsys and params");
+        t.kernel = k->str;
+        t.n = (int64_t)n->num;
+        t.nsys = (int64_t)ns->num;
+        for (auto& kv : ps->obj) {
+            require(kv.second.kind == JValue::Number, "tuning table: parameters are integers");
+            t.params.emplace_back(kv.first, (int)kv.second.num);
+        }
+        out.push_back(std::move(t));
+    }
+    return out;
+}
+
+int TuningTable::get(const char* kernel, const char* param, int64_t n, int64_t nsys, int dflt) const {
+    // the entry of this kernel nearest in log(n), then log(nsys)
+    const TuneEntry* best = nullptr;
+    double bd = 0;
+    for (const TuneEntry& e : entries) {
+        if (e.kernel != kernel) continue;
+        const double d = std::fabs(std::log((double)std::max<int64_t>(n, 1) / (double)std::max<int64_t>(e.n, 1))) +
+                         0.25 * std::fabs(std::log((double)std::max<int64_t>(nsys, 1) /
+                                                   (double)std::max<int64_t>(e.nsys, 1)));
+        if (!best || d < bd) {
+            best = &e;
+            bd = d;
+        }
+    }
+    if (!best) return dflt;
+    for (auto& kv : best->params)
+        if (kv.first == param) return kv.second;
+    return dflt;
+}
+
 std::vector<double> frequency_list(const UserInput& in) {
     if (in.freq_kind == 0) return in.freq_values;
     require(in.freq_number >= 1, "frequency: number must be at least 1");

@@ -328,6 +328,24 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* tma
         : "memory");
 }
 
+// The same copy with an L2 eviction policy (createpolicy): the GEMM operands
+// are panels that every tile of a launch re-reads, so they are kept in L2
+// (evict_last) while the trailing block streams past them.
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ void tma_load_2d_hint(uint32_t dst, const CUtensorMap* tmap, int x, int y, uint64_t* bar,
+                                                 uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+        " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+
 // Shared-memory descriptor of a K-major operand in the 128-byte swizzle
 // layout written by the tensor copies: rows of 128 bytes, 8-row atoms of
 // 1024 bytes (stride between atoms), descriptor version bit 46, layout type 2.
@@ -381,9 +399,28 @@ struct GemmTile {
     int64_t n, ld, ld2, k0, ktw, row0, rows_end, col0, col_end;
 };
 
+// Raster of a TRAIL region's tiles (tiles_i row tiles x tiles_j column
+// tiles): bands of sb_c column tiles, each swept by super-blocks of sb_r row
+// tiles x the band's columns, row tiles fastest.  A band's slice of the row
+// panel Y (sb_c x 1 MB at K = 1024) stays in L2 while the band's rows stream
+// the column panel W past it, so W is read once per band and Y once per
+// launch (column-after-column order re-reads W for every column tile, which
+// for n >= 12000 is larger than L2).  (sb_r, sb_c) comes from the tuning
+// table.
+__device__ __forceinline__ void raster_tile(int64_t local, int64_t tiles_i, int64_t tiles_j, int sb_r, int sb_c,
+                                            int64_t& ti, int64_t& tj) {
+    const int64_t per_band = tiles_i * sb_c;
+    const int64_t band = local / per_band, rem = local - band * per_band;
+    const int64_t bc = min((int64_t)sb_c, tiles_j - band * sb_c);  // columns of this band
+    const int64_t sr = rem / (sb_r * bc), rem2 = rem - sr * (sb_r * bc);
+    const int64_t br = min((int64_t)sb_r, tiles_i - sr * sb_r);     // rows of this super-block
+    ti = sr * sb_r + rem2 % br;
+    tj = band * sb_c + rem2 / br;
+}
+
 template <int MODE>
 __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl, int nw,
-                                              int64_t t, int ks, int kw, int woff) {
+                                              int64_t t, int ks, int kw, int woff, int raster) {
     int64_t local;
     const LuWork& w = wl[lu_entry(wl, nw, t, local)];
     const LuSys S = sys[w.sys];
@@ -397,9 +434,11 @@ __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, con
     g.k0 = (int64_t)ks * LB;
     g.ktw = (int64_t)(kw + 1) * LB;
     if (MODE == G_TRAIL) {
-        g.row0 = w.r0 + (local % w.tiles_i) * GM;
+        int64_t ti, tj;
+        raster_tile(local, w.tiles_i, (w.c1 - w.c0 + GN - 1) / GN, raster >> 16, raster & 0xFFFF, ti, tj);
+        g.row0 = w.r0 + ti * GM;
         g.rows_end = w.r1;
-        g.col0 = w.c0 + (local / w.tiles_i) * GN;
+        g.col0 = w.c0 + tj * GN;
         g.col_end = w.c1;
         g.tmA = S.tmW;
         g.ax = 0;
@@ -437,6 +476,7 @@ template <int MODE>
 __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __restrict__ sys,
                                                               const LuWork* __restrict__ wl, int nw, int ks, int kw,
                                                               int nchunks, int woff, int yoff, int64_t ntiles,
+                                                              int raster,
                                                               int* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + GS * GSTAGE);
@@ -474,9 +514,10 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
     if (warp == 0) {
         // ---- producer: one thread, two tensor copies per stage
         if (lane == 0) {
+            const uint64_t keep = l2_policy_evict_last();
             int64_t it = 0;
             for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
-                const GemmTile g = gemm_tile<MODE>(sys, wl, nw, t, ks, kw, woff);
+                const GemmTile g = gemm_tile<MODE>(sys, wl, nw, t, ks, kw, woff, raster);
                 for (int c = 0; c < nchunks; ++c, ++it) {
                     const int st = (int)(it % GS);
                     const int64_t round = it / GS;
@@ -486,8 +527,8 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                     }
                     const uint32_t As = base + st * GSTAGE, Bs = As + GA_BYTES;
                     mbar_arrive_expect_tx(&full[st], GSTAGE);
-                    tma_load_2d(As, g.tmA, g.ax + c * GK, g.ay, &full[st]);
-                    tma_load_2d(Bs, g.tmB, g.bx + c * GK, g.by, &full[st]);
+                    tma_load_2d_hint(As, g.tmA, g.ax + c * GK, g.ay, &full[st], keep);
+                    tma_load_2d_hint(Bs, g.tmB, g.bx + c * GK, g.by, &full[st], keep);
                 }
             }
             if (*abort_flag) {
@@ -543,7 +584,7 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                 break;
             }
             tc_fence_after();
-            const GemmTile g = gemm_tile<MODE>(sys, wl, nw, t, ks, kw, woff);
+            const GemmTile g = gemm_tile<MODE>(sys, wl, nw, t, ks, kw, woff, raster);
             const int64_t r = g.row0 + 32 * quarter + lane;
             const bool rok = r < g.rows_end;
             for (int cc = half * (GN / 64); cc < (half + 1) * (GN / 64); ++cc) {
@@ -553,15 +594,17 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                 tmem_ld32(tmem + lane_base + (uint32_t)(acc * GN + cc * 32), v);
                 if (MODE == G_TRAIL) {
                     if (!rok) continue;
-                    // all 32 loads in flight before the first store
+                    // all 32 loads in flight before the first store; the
+                    // trailing block is touched once per launch: streaming
+                    // (evict-first) loads and stores keep the panels in L2
                     const int nq = (int)min((int64_t)32, g.col_end - jb);
                     float* p0 = g.F + jb * g.ld2 + 2 * g.ktw + r;
                     float cv[32];
 #pragma unroll
-                    for (int q = 0; q < 32; ++q) cv[q] = q < nq ? __ldcg(p0 + q * g.ld2) : 0.f;
+                    for (int q = 0; q < 32; ++q) cv[q] = q < nq ? __ldcs(p0 + q * g.ld2) : 0.f;
 #pragma unroll
                     for (int q = 0; q < 32; ++q)
-                        if (q < nq) p0[q * g.ld2] = cv[q] - v[q];
+                        if (q < nq) __stcs(p0 + q * g.ld2, cv[q] - v[q]);
                 } else if (MODE == G_U12) {
                     const int nq = (int)min((int64_t)32, g.col_end - jb);
                     float* p0 = g.Y + jb * WK + yoff + r;
@@ -1131,6 +1174,16 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         BEM_CUDA(cudaEventCreate(&ev1));
     }
     auto persistent = [&](int64_t ctas) { return (unsigned)std::min<int64_t>(ctas, nsm); };
+    // tile raster of the trailing updates (super-blocks of sb_r x sb_c tiles)
+    // (keyed by the largest operator and the number of factored operators)
+    int64_t nfact = 0, nmax = 0;
+    for (int s = 0; s < nsys; ++s) {
+        nfact += owner[(size_t)s] == s;
+        nmax = std::max(nmax, d->sys[(size_t)s].n);
+    }
+    const int sb_r = std::max(1, std::min(65535, c.tuning.pick("lu_gemm_trail", "sb_r", nmax, nfact, 8)));
+    const int sb_c = std::max(1, std::min(65535, c.tuning.pick("lu_gemm_trail", "sb_c", nmax, nfact, 32)));
+    const int raster = (sb_r << 16) | sb_c;
     for (const LuData::Launch& l : d->plan) {
         const LuData::Seg& sg = l.seg;
         if (c.profiling) BEM_CUDA(cudaEventRecord(ev0, c.stream));
@@ -1145,11 +1198,11 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
                 break;
             case LuData::L21:
                 lu_gemm_kernel<G_L21><<<persistent(sg.ctas), GTHREADS, G_SMEM, c.stream>>>(
-                    sys, wk + sg.off, sg.count, l.ks, l.kw, l.nchunks, l.woff, l.yoff, sg.ctas, err);
+                    sys, wk + sg.off, sg.count, l.ks, l.kw, l.nchunks, l.woff, l.yoff, sg.ctas, raster, err);
                 break;
             case LuData::U12:
                 lu_gemm_kernel<G_U12><<<persistent(sg.ctas), GTHREADS, G_SMEM, c.stream>>>(
-                    sys, wk + sg.off, sg.count, l.ks, l.kw, l.nchunks, l.woff, l.yoff, sg.ctas, err);
+                    sys, wk + sg.off, sg.count, l.ks, l.kw, l.nchunks, l.woff, l.yoff, sg.ctas, raster, err);
                 break;
             case LuData::COPY:
                 lu_copy_u12_kernel<<<(unsigned)sg.ctas, 256, 0, c.stream>>>(sys, wk + sg.off, sg.count, l.ks,
@@ -1157,7 +1210,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
                 break;
             case LuData::TRAIL:
                 lu_gemm_kernel<G_TRAIL><<<persistent(sg.ctas), GTHREADS, G_SMEM, c.stream>>>(
-                    sys, wk + sg.off, sg.count, l.ks, l.kw, l.nchunks, l.woff, l.yoff, sg.ctas, err);
+                    sys, wk + sg.off, sg.count, l.ks, l.kw, l.nchunks, l.woff, l.yoff, sg.ctas, raster, err);
                 break;
         }
         BEM_CHECK_LAUNCH(&c);

@@ -12,6 +12,8 @@
 #include "common.cuh"
 #include "complex.cuh"
 #include "gmres.cuh"
+#include "hmixed.cuh"
+#include "hmatrix.cuh"
 #include "mixed.cuh"
 #include "precond.cuh"
 
@@ -115,7 +117,10 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
     // storage at 1e-6; those systems keep an FP64 operator in the same batch,
     // as every operator of the refined form does.
     const bool first_kind = fp64_operator || (p.in.method_type == 0 && p.in.bc_type == 0);
-    c.w_mat.ensure((first_kind ? sizeof(double2) : sizeof(float2)) * mstride * nf);
+    // the Hierarchical solver: ACA-compressed operators with FP32 factors
+    // instead of dense ones (hmixed.cu)
+    const bool hier = p.in.solver == 2 && !first_kind;
+    if (!hier) c.w_mat.ensure((first_kind ? sizeof(double2) : sizeof(float2)) * mstride * nf);
     float2* A32 = c.w_mat.as<float2>();
     double2* A64 = c.w_mat.as<double2>();
     c.w_vec.ensure(sizeof(double2) * ((size_t)ns * (3 * n + 2 * nfp) + (size_t)nf * n + 2) + sizeof(double) * nf);
@@ -140,7 +145,10 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
     ws.mem_pool = &c.w_gm;
     ws.z_pool = &c.w_gmz;
     const void* Aop = first_kind ? (const void*)A64 : (const void*)A32;
-    if (R == 1) {
+    std::shared_ptr<HMixed> Hm;
+    if (hier) {
+        gm_prepare(c, ws, (int)ns, n, m, nullptr, n, 0, true, false);
+    } else if (R == 1) {
         gm_prepare(c, ws, (int)nf, n, m, Aop, ld, mstride, !first_kind, false);
     } else {
         std::vector<int64_t> nsz((size_t)ns, n), lds((size_t)ns, ld);
@@ -149,7 +157,20 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
         gm_prepare_ragged(c, ws, nsz, lds, aoff, m, Aop, !first_kind);
     }
 
-    if (first_kind && !need_rowsum) {
+    if (hier) {
+        EventTimer t(c);
+        Hm = hmixed_build(c, p, F0, nf, (int)R);
+        hmixed_attach(c, ws, Hm);
+        const HMixedStats hs = hmixed_stats(*Hm);
+        ws.mv_bytes = 8.0 * (double)hs.store_entries / (double)nf;  // per system and mat-vec
+        ws.mv_stage = "gmres_matvec_hmatrix";
+        if (need_rowsum)
+            for (int64_t f = 0; f < nf; ++f) {
+                p.ifreq = F0 + f;
+                hmatrix_row_sums(c, p, 0, rowsum + f * n);
+            }
+        t.stop("hmatrix_build", nf, 8.0 * (double)hs.store_entries);
+    } else if (first_kind && !need_rowsum) {
         // every frequency in one pass, norms accumulated by the kernel
         EventTimer t(c);
         assemble_system_fp64_multi(c, p, ks.data(), al.data(), be.data(), (int)nf, A64, ld, mstride,
@@ -197,13 +218,17 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
     {
         EventTimer t(c);
         gm_init(c, ws, tol, restarts);
-        if (precond != BEM_PRECOND_NONE)
+        if (precond != BEM_PRECOND_NONE && hier)
+            // the compressed operators have no dense copy to factor: every
+            // preconditioner request becomes block-Jacobi on the diagonal leaves
+            precond = hmixed_block_jacobi(c, ws, Hm) ? BEM_PRECOND_BLOCK_JACOBI : BEM_PRECOND_NONE;
+        else if (precond != BEM_PRECOND_NONE)
             precond = precond_setup(c, p, ws, precond, ks_sys.data());
         gm_run(c, ws, c.profiling ? 0 : 4, restarts * (int64_t)m + 1);
         gm_read_states(c, ws, st);
         int64_t mv = 0;
         for (auto& x : st) mv += x.num_mv;
-        t.stop("gmres", mv, (first_kind ? 16.0 : 8.0) * (double)n * n * mv);
+        t.stop("gmres", mv, hier ? ws.mv_bytes * mv : (first_kind ? 16.0 : 8.0) * (double)n * n * mv);
     }
     {
         EventTimer t(c);
@@ -285,7 +310,9 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     size_t fr = 0, tot = 0;
     BEM_CUDA(cudaMemGetInfo(&fr, &tot));
     const double budget = 0.6 * (double)(fr + c.w_mat.bytes + c.w_lu_F.bytes);
-    const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nf, (int64_t)(budget / per)));
+    // (compressed operators: every frequency at once)
+    const bool hier = p.in.solver == 2 && !op64;
+    const int64_t chunk = hier ? nf : std::max<int64_t>(1, std::min<int64_t>(nf, (int64_t)(budget / per)));
     for (int64_t f0 = 0; f0 < nf; f0 += chunk)
         run_mixed_range(c, p, f0, std::min(chunk, nf - f0), precond, scattered, incident, reports, check_vs_lu,
                         fp64_operator);

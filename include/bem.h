@@ -143,6 +143,22 @@ BEM_API int64_t bem_ctx_profile_count(const bem_ctx* ctx);
 BEM_API bem_status bem_ctx_profile_get(const bem_ctx* ctx, int64_t i, char* name, int64_t name_len,
                                        double* ms, int64_t* launches, double* bytes);
 
+/* ---- launch tuning (no reference counterpart) ------------------------- */
+/* Launch parameters of the hot kernels (the trailing update's tile raster,
+ * the Krylov mat-vec's load batch, the FP32 assembly's occupancy) come from a
+ * tuning table keyed by problem size and number of systems, written by the
+ * offline sweep cc_abstemious_gb300/tune.py.  A context reads tuning.json
+ * beside the library at creation when it exists (the environment variable
+ * BEM_TUNING_FILE names another file, or "none" for the built-in defaults).
+ * bem_ctx_load_tuning reads a table (NULL: back to the defaults);
+ * bem_ctx_set_tuning forces one parameter (value < 0 removes the override);
+ * bem_ctx_get_tuning returns the value a launch of that size would use. */
+BEM_API bem_status bem_ctx_load_tuning(bem_ctx* ctx, const char* path);
+BEM_API bem_status bem_ctx_set_tuning(bem_ctx* ctx, const char* kernel, const char* param, int value);
+BEM_API int bem_ctx_get_tuning(const bem_ctx* ctx, const char* kernel, const char* param, int64_t n, int64_t nsys);
+/* The file the context's table was read from ("" for the built-in defaults). */
+BEM_API const char* bem_ctx_tuning_source(const bem_ctx* ctx);
+
 /* ---- input and preprocessing ------------------------------------------ */
 /* analysis.rs:50-53 input_from_string + preprocess.rs:104-124 preprocess.
  * base_dir (may be NULL) resolves a relative mesh_file; the reference resolves
