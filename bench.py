@@ -60,7 +60,7 @@ def parse():
                          "two right-hand sides, 8 frequencies up to ka 20)")
     ap.add_argument("--bodies", type=int, default=256, help="perturbed_spheres: number of bodies")
     ap.add_argument("--train-bodies", type=int, default=16, help="held_out_learned: training bodies")
-    ap.add_argument("--train-steps", type=int, default=400, help="held_out_learned: training steps")
+    ap.add_argument("--train-steps", type=int, default=1000, help="learned preconditioner: training steps")
     ap.add_argument("--held-out-tri", type=int, default=20000, help="held_out_learned: triangles")
     ap.add_argument("--targets", default="all",
                     help="target workloads added to the default line at N = 1 under 'targets': all, none, or a "
@@ -601,7 +601,7 @@ class _Shared:
         train = workloads.perturbed_spheres(self.wd, count=a.train_bodies, seed=1, nfreq=8, tri_lo=500, tri_hi=3000)
         tpds = [bem.PreData.from_dict(d, ctx=self.ctx) for d in train]
         t0 = time.perf_counter()
-        losses = bem.learned_train(tpds, steps=a.train_steps, nprobe=8, lr=2e-3, seed=5, ctx=self.ctx)
+        losses = bem.learned_train(tpds, steps=a.train_steps, nprobe=8, lr=1e-2, seed=5, ctx=self.ctx)
         self.training = {"bodies": len(train), "steps": a.train_steps, "seconds": time.perf_counter() - t0,
                          "loss_first": float(np.mean(losses[:10])), "loss_last": float(np.mean(losses[-10:]))}
         del tpds

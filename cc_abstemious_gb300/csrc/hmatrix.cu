@@ -820,15 +820,32 @@ static GenParams gen_params(const Problem& p, int side) {
 
 constexpr int ACA_RMAX = 256;
 
-std::unique_ptr<HMatrixDev> hmatrix_build(Context& c, const Problem& p, int side) {
+// The cluster tree and block leaves of a problem's collocation points (they
+// depend on the geometry, the leaf size and eta only, not on the frequency).
+struct HTrees {
+    std::unique_ptr<ClNode> root;
+    std::vector<std::tuple<const ClNode*, const ClNode*, int>> bl;
+};
+
+static std::shared_ptr<HTrees> build_trees(const Problem& p) {
+    auto T = std::make_shared<HTrees>();
+    const int64_t n = p.n;
+    std::vector<int64_t> idx((size_t)n);
+    for (int64_t i = 0; i < n; ++i) idx[(size_t)i] = i;
+    T->root = build_cluster(p.cpts, 8, idx, p.in.hm_leaf, 0);
+    block_leaves(*T->root, *T->root, p.in.hm_eta, T->bl);
+    return T;
+}
+
+// trees: the problem's trees from an earlier build (several frequencies of
+// one body), or null to build them here.
+std::unique_ptr<HMatrixDev> hmatrix_build(Context& c, const Problem& p, int side,
+                                          std::shared_ptr<HTrees> trees = nullptr) {
     auto H = std::make_unique<HMatrixDev>();
     const int64_t n = p.n;
     H->n = n;
-    std::vector<int64_t> idx((size_t)n);
-    for (int64_t i = 0; i < n; ++i) idx[(size_t)i] = i;
-    auto root = build_cluster(p.cpts, 8, idx, p.in.hm_leaf, 0);
-    std::vector<std::tuple<const ClNode*, const ClNode*, int>> bl;
-    block_leaves(*root, *root, p.in.hm_eta, bl);
+    if (!trees) trees = build_trees(p);
+    const auto& bl = trees->bl;
     int64_t store = 0, scratch = 0, yoff = 0;
     for (auto& t : bl) {
         const ClNode* r = std::get<0>(t);
@@ -961,8 +978,14 @@ void hmatrix_gemv(Context& c, const HMatrixDev& H, cd alpha, const double2* x, c
 
 // The built leaves for the mixed form's repacking (hmixed.cu): index lists,
 // ranks, norms and the device data of the FP64 build, kept alive by `keep`.
-HBuilt hmatrix_build_view(Context& c, const Problem& p, int side) {
-    std::shared_ptr<HMatrixDev> H(hmatrix_build(c, p, side).release());
+HBuilt hmatrix_build_view(Context& c, const Problem& p, int side, std::shared_ptr<void>* tree_cache) {
+    std::shared_ptr<HTrees> trees;
+    if (tree_cache && *tree_cache) trees = std::static_pointer_cast<HTrees>(*tree_cache);
+    if (!trees) {
+        trees = build_trees(p);
+        if (tree_cache) *tree_cache = trees;
+    }
+    std::shared_ptr<HMatrixDev> H(hmatrix_build(c, p, side, trees).release());
     HBuilt v;
     v.n = H->n;
     v.norm = H->norm;

@@ -40,7 +40,9 @@ struct HBuilt {
 // h_matrix.rs:127-148 HMatrix::new_from at the problem's current frequency
 // (side 1: lhs factors, 0: rhs factors), leaf size, eta and ACA tolerance
 // from the problem.
-HBuilt hmatrix_build_view(Context& c, const Problem& p, int side);
+// tree_cache (may be null): holds the problem's cluster / block trees between
+// calls for several frequencies of one body (built on the first call).
+HBuilt hmatrix_build_view(Context& c, const Problem& p, int side, std::shared_ptr<void>* tree_cache = nullptr);
 // out = H 1 (n entries, device) for the H-matrix of `side`.
 void hmatrix_row_sums(Context& c, const Problem& p, int side, double2* out);
 

@@ -454,9 +454,10 @@ std::shared_ptr<HMixed> hmixed_build(Context& c, Problem& p, int64_t F0, int64_t
     upload(c, H->d_perm, H->perm);
     const int64_t saved = p.ifreq;
     size_t store_total = 0;
+    std::shared_ptr<void> trees;  // built once, shared by every frequency
     for (int64_t f = 0; f < nops; ++f) {
         p.ifreq = F0 + f;
-        HBuilt B = hmatrix_build_view(c, p, 1);
+        HBuilt B = hmatrix_build_view(c, p, 1, &trees);
         const int nb = (int)B.leaves.size();
         if (f == 0) {
             H->nb = nb;

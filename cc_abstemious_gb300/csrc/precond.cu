@@ -14,7 +14,8 @@
 //    and the phase k r.  C_ij = s_ij (o_1 + i o_2) with s_ij = wa_j / (4 pi r).
 //    Weights and activations are rounded to BF16, products accumulate in
 //    FP32.  The network is trained on the GPU on operators the BEM assembles,
-//    minimising E_z ||A M z - z||^2 / ||z||^2 over random probes z, with
+//    minimising E_z ||A M z - z||^2 / ||z||^2 over random probes z (relative to
+//    the system's block-Jacobi value, so every wavenumber weighs alike), with
 //    hand-written forward / backward kernels and Adam.  The block-Jacobi part
 //    is always present, so an untrained (zero) correction is block-Jacobi.
 #include <cuda_bf16.h>
@@ -456,11 +457,12 @@ __global__ void probe_residual_kernel(int64_t total, const double2* __restrict__
     }
 }
 
-// dL/d(o1, o2) of every pair: 2 s (Re, Im) sum_q G_iq conj(Z_jq) / sum |Z|^2.
+// dL/d(o1, o2) of every pair: 2 s (Re, Im) sum_q G_iq conj(Z_jq) / sum |Z|^2,
+// times w (the system's loss normalisation).
 __global__ void pair_grad_kernel(int64_t P, int nprobe, int64_t n, const int32_t* __restrict__ pi,
                                  const int32_t* __restrict__ pj, const float* __restrict__ scale,
                                  const double2* __restrict__ G, const double2* __restrict__ Z,
-                                 const double* __restrict__ acc, float* __restrict__ dO) {
+                                 const double* __restrict__ acc, double w, float* __restrict__ dO) {
     int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (p >= P) return;
     const int64_t i = pi[p], j = pj[p];
@@ -470,7 +472,7 @@ __global__ void pair_grad_kernel(int64_t P, int nprobe, int64_t n, const int32_t
         re += g.x * z.x + g.y * z.y;
         im += g.y * z.x - g.x * z.y;
     }
-    const double f = 2.0 * scale[p] / acc[1];
+    const double f = 2.0 * w * scale[p] / acc[1];
     dO[2 * p] = (float)(f * re);
     dO[2 * p + 1] = (float)(f * im);
 }
@@ -856,10 +858,39 @@ double learned_train(Context& c, std::vector<Problem*>& probs, int steps, int np
     dO.ensure(sizeof(float) * pmax * NO);
     for (DevBuf* v : {&Z, &Y, &W, &R, &G}) v->ensure(sizeof(double2) * (size_t)nmax * nprobe);
     losses.clear();
+    // every system's block-Jacobi probe loss (the correction still zero): the
+    // training loss of a system is its loss relative to this, so systems of
+    // every wavenumber weigh alike (1 = no better than block-Jacobi)
+    std::vector<std::vector<double>> lbj(bodies.size());
+    for (size_t bi = 0; bi < bodies.size(); ++bi) {
+        Body& b = *bodies[bi];
+        const int64_t n = b.p->n, tot = n * nprobe;
+        for (int f = 0; f < b.nf; ++f) {
+            probes_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(tot, seed * 104729 + (uint64_t)f,
+                                                                                Z.as<double2>());
+            BEM_CHECK_LAUNCH(&c);
+            pc_apply_probes_kernel<<<dim3((unsigned)b.pc.pat.nc, (unsigned)nprobe), PC_LEAF, 0, c.stream>>>(
+                b.pc.dev(1), f, Z.as<double2>(), Y.as<double2>(), n);
+            BEM_CHECK_LAUNCH(&c);
+            probe_matvec_kernel<<<dim3((unsigned)((n + 127) / 128), (unsigned)nprobe), 128, 0, c.stream>>>(
+                n, b.A.as<float2>() + (size_t)f * b.mstride, b.lda, Y.as<double2>(), W.as<double2>(), 0);
+            BEM_CHECK_LAUNCH(&c);
+            BEM_CUDA(cudaMemsetAsync(lossacc.p, 0, sizeof(double) * 2, c.stream));
+            probe_residual_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(
+                tot, W.as<double2>(), Z.as<double2>(), R.as<double2>(), lossacc.as<double>());
+            BEM_CHECK_LAUNCH(&c);
+            double la[2];
+            BEM_CUDA(cudaMemcpyAsync(la, lossacc.p, sizeof(la), cudaMemcpyDeviceToHost, c.stream));
+            c.sync();
+            lbj[bi].push_back(std::max(la[0] / la[1], 1e-30));
+        }
+    }
     int64_t sidx = 0;
     for (int it = 0; it < steps; ++it) {
-        Body& b = *bodies[(size_t)((sidx / 1) % bodies.size())];
+        const size_t bi = (size_t)((sidx / 1) % bodies.size());
+        Body& b = *bodies[bi];
         const int f = (int)((sidx / (int64_t)bodies.size()) % b.nf);
+        const double wsys = 1.0 / lbj[bi][(size_t)f];
         ++sidx;
         const int64_t n = b.p->n, P = b.pc.pat.npairs;
         float2* Ms = b.pc.M.as<float2>() + (size_t)f * b.pc.pat.entries;
@@ -900,7 +931,7 @@ double learned_train(Context& c, std::vector<Problem*>& probs, int steps, int np
         if (P > 0) {
             pair_grad_kernel<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(
                 P, nprobe, n, b.pb.pi.as<int32_t>(), b.pb.pj.as<int32_t>(), b.pb.scale.as<float>(), G.as<double2>(),
-                Z.as<double2>(), lossacc.as<double>(), dO.as<float>());
+                Z.as<double2>(), lossacc.as<double>(), wsys, dO.as<float>());
             BEM_CHECK_LAUNCH(&c);
             mlp_backward(c, net, P, b.pb.F.as<float>(), b.pb.H1.as<float>(), b.pb.H2.as<float>(), dO.as<float>(),
                          D2.as<float>(), D1.as<float>(), grad.as<float>());
@@ -914,7 +945,7 @@ double learned_train(Context& c, std::vector<Problem*>& probs, int steps, int np
         BEM_CHECK_LAUNCH(&c);
         net.refresh(c);
         c.sync();
-        losses.push_back(la[0] / la[1]);
+        losses.push_back(wsys * la[0] / la[1]);
     }
     net.w_host.resize(NPARAM);
     BEM_CUDA(cudaMemcpyAsync(net.w_host.data(), net.w.p, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, c.stream));

@@ -303,9 +303,11 @@ BEM_API bem_status bem_last_surface(bem_ctx* ctx, const bem_problem* p, bem_cplx
  * of C on the near off-diagonal leaf blocks come from a 3-layer MLP (width 128,
  * BF16 weights/activations, FP32 accumulation) over pair geometry and ka.
  * bem_learned_train trains the context's network on the GPU on the operators of
- * the given problems (all their frequencies) by minimising E ||A M z - z||^2 /
- * ||z||^2 over random probes; losses (steps entries, may be NULL) receive the
- * per-step loss.  Used by bem_run with BEM_PRECOND_LEARNED. */
+ * the given problems (all their frequencies) by minimising, per system,
+ * E ||A M z - z||^2 / ||z||^2 over random probes relative to the same loss
+ * with block-Jacobi alone (so systems of every wavenumber weigh alike); losses
+ * (steps entries, may be NULL) receive that relative loss per step (1: no
+ * better than block-Jacobi).  Used by bem_run with BEM_PRECOND_LEARNED. */
 BEM_API bem_status bem_learned_train(bem_ctx* ctx, bem_problem* const* problems, int nproblems, int steps,
                                      int nprobe, double lr, uint64_t seed, double* losses);
 BEM_API int64_t bem_learned_num_params(void);
