@@ -292,6 +292,20 @@ __device__ __forceinline__ z2 bsum2(z2 v, double* sh) {
     return make_double2(a, b);
 }
 
+// Sum of a complex value over the 32 lanes of a warp (every lane gets it).
+__device__ __forceinline__ z2 wsum2(z2 v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+
+__device__ __forceinline__ double wsum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 // argmax of |v[t]| over t not excluded; first index wins ties (aca.rs:256-268).
 __device__ int64_t bargmax_excl(const double2* v, const int8_t* excl, int64_t len, double* sh, int64_t* shi) {
     double best = -1.0;
@@ -364,12 +378,6 @@ __device__ void aca_res_col(const GenParams& g, const HLeaf& L, const int64_t* r
     __syncthreads();
 }
 
-__device__ __forceinline__ z2 bdotu(const double2* a, const double2* b, int64_t len, double* sh) {
-    z2 acc = make_double2(0, 0);
-    for (int64_t t = threadIdx.x; t < len; t += blockDim.x) cfma(acc, a[t], b[t]);
-    return bsum2(acc, sh);
-}
-
 __device__ __forceinline__ double bnsq(const double2* a, int64_t len, double* sh) {
     double acc = 0;
     for (int64_t t = threadIdx.x; t < len; t += blockDim.x) acc += a[t].x * a[t].x + a[t].y * a[t].y;
@@ -389,6 +397,7 @@ __global__ void __launch_bounds__(LEAF_THREADS) hm_aca_kernel(HLeaf* __restrict_
     __shared__ int64_t s_iref, s_jref, s_istar, s_jstar;
     __shared__ double s_total;
     __shared__ int s_stop;
+    __shared__ double s_prod[256];  // one per earlier rank (kmax <= ACA_RMAX = 256)
     HLeaf& L = leaves[list[blockIdx.x]];
     const int64_t m = L.m, n = L.n;
     const int64_t nr = m < n ? m : n;
@@ -444,15 +453,26 @@ __global__ void __launch_bounds__(LEAF_THREADS) hm_aca_kernel(HLeaf* __restrict_
         for (int64_t t = threadIdx.x; t < m; t += blockDim.x) uk[t] = rjstar[t];
         __syncthreads();
         rank = (int)k + 1;
-        // update_norm_estimate (aca.rs:224-241)
+        // update_norm_estimate (aca.rs:224-241): the products with every
+        // earlier rank one warp each, summed in rank order by one thread
         double nk = bnsq(uk, m, sh) * bnsq(vk, n, sh);
-        double add = 0;
-        for (int t = 0; t < k; ++t) {
-            z2 du = bdotu(U + (size_t)t * m, uk, m, sh);
-            z2 dv = bdotu(V + (size_t)t * n, vk, n, sh);
-            add += 2.0 * hypot(du.x, du.y) * hypot(dv.x, dv.y);
+        {
+            const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+            for (int t = warp; t < k; t += nw) {
+                const double2* ut = U + (size_t)t * m;
+                const double2* vt = V + (size_t)t * n;
+                z2 du = make_double2(0, 0), dv = make_double2(0, 0);
+                for (int64_t i = lane; i < m; i += 32) cfma(du, ut[i], uk[i]);
+                for (int64_t j = lane; j < n; j += 32) cfma(dv, vt[j], vk[j]);
+                du = wsum2(du);
+                dv = wsum2(dv);
+                if (lane == 0) s_prod[t] = 2.0 * hypot(du.x, du.y) * hypot(dv.x, dv.y);
+            }
         }
+        __syncthreads();
         if (threadIdx.x == 0) {
+            double add = 0;
+            for (int t = 0; t < k; ++t) add += s_prod[t];
             s_total += nk;
             s_total += add;
             double step = sqrt(nk) / sqrt(s_total);
@@ -518,12 +538,16 @@ __global__ void __launch_bounds__(LEAF_THREADS) hm_aca_kernel(HLeaf* __restrict_
 __device__ void house_qr_dev(double2* A, int64_t m, int r, double2* R, double2* tau, double* sh) {
     // A: m x r column-major; on exit the reflectors v_k (v_k[k] = 1 implied
     // by storing the full vector) are kept in A below and on the diagonal.
+    // Column k's reflector comes from two block reductions; its application
+    // to the later columns runs one warp per column (warp reductions, one
+    // barrier per k).
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __shared__ double2 s_alpha, s_tau;
     for (int k = 0; k < r; ++k) {
         double2* a = A + (size_t)k * m;
         double nx2 = 0;
         for (int64_t i = k + threadIdx.x; i < m; i += blockDim.x) nx2 += cnorm2(a[i]);
         double nx = sqrt(bsum(nx2, sh));
-        __shared__ double2 s_alpha, s_tau;
         if (threadIdx.x == 0) {
             z2 x0 = a[k];
             double ax0 = hypot(x0.x, x0.y);
@@ -540,20 +564,17 @@ __device__ void house_qr_dev(double2* A, int64_t m, int r, double2* R, double2* 
         if (threadIdx.x == 0) s_tau = make_double2(vn2 == 0 ? 0.0 : 2.0 / vn2, 0.0);
         __syncthreads();
         const double tk = s_tau.x;
-        // R column k: alpha on the diagonal; apply H_k to columns j > k
-        for (int j = k + 1; j < r; ++j) {
+        // apply H_k to columns j > k, one warp per column
+        for (int j = k + 1 + warp; j < r; j += nw) {
             double2* c = A + (size_t)j * m;
             z2 d = make_double2(0, 0);
-            for (int64_t i = k + threadIdx.x; i < m; i += blockDim.x) cfma(d, cconj(a[i]), c[i]);
-            d = cscale(bsum2(d, sh), tk);
-            for (int64_t i = k + threadIdx.x; i < m; i += blockDim.x) cfma(c[i], cneg(a[i]), d);
-            __syncthreads();
+            for (int64_t i = k + lane; i < m; i += 32) cfma(d, cconj(a[i]), c[i]);
+            d = cscale(wsum2(d), tk);
+            for (int64_t i = k + lane; i < m; i += 32) cfma(c[i], cneg(a[i]), d);
         }
-        if (threadIdx.x == 0) {
-            tau[k] = make_double2(tk, 0.0);
-            for (int i = 0; i < r; ++i) R[(size_t)k * r + i] = i < k ? A[(size_t)k * m + i] : make_double2(0, 0);
-            R[(size_t)k * r + k] = s_alpha;
-        }
+        if (threadIdx.x == 0) tau[k] = make_double2(tk, 0.0);
+        for (int i = threadIdx.x; i < r; i += blockDim.x)
+            R[(size_t)k * r + i] = i == k ? s_alpha : make_double2(0, 0);
         __syncthreads();
     }
     // R above the diagonal lives in rows < k of columns k (read after the loop)
@@ -562,9 +583,12 @@ __device__ void house_qr_dev(double2* A, int64_t m, int r, double2* R, double2* 
     __syncthreads();
 }
 
-// out (m x c) = Q [B; 0] where Q = H_0 ... H_{r-1} (reflectors in A), B r x c.
+// out (m x c) = Q [B; 0] where Q = H_0 ... H_{r-1} (reflectors in A), B r x c;
+// one warp per output column for each reflector.
 __device__ void house_apply_dev(const double2* A, int64_t m, int r, const double2* tau, const double2* B, int c,
                                 double2* out, double* sh) {
+    (void)sh;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int j = 0; j < c; ++j)
         for (int64_t i = threadIdx.x; i < m; i += blockDim.x)
             out[(size_t)j * m + i] = i < r ? B[(size_t)j * r + i] : make_double2(0, 0);
@@ -573,52 +597,62 @@ __device__ void house_apply_dev(const double2* A, int64_t m, int r, const double
         const double2* v = A + (size_t)k * m;
         const double tk = tau[k].x;
         if (tk == 0.0) continue;
-        for (int j = 0; j < c; ++j) {
+        for (int j = warp; j < c; j += nw) {
             double2* o = out + (size_t)j * m;
             z2 d = make_double2(0, 0);
-            for (int64_t i = k + threadIdx.x; i < m; i += blockDim.x) cfma(d, cconj(v[i]), o[i]);
-            d = cscale(bsum2(d, sh), tk);
-            for (int64_t i = k + threadIdx.x; i < m; i += blockDim.x) cfma(o[i], cneg(v[i]), d);
-            __syncthreads();
+            for (int64_t i = k + lane; i < m; i += 32) cfma(d, cconj(v[i]), o[i]);
+            d = cscale(wsum2(d), tk);
+            for (int64_t i = k + lane; i < m; i += 32) cfma(o[i], cneg(v[i]), d);
         }
+        __syncthreads();
     }
 }
 
 // One-sided Jacobi SVD of the r x r matrix M (overwritten): M = W S Vh with S
-// descending.  Rotations of column pairs run one at a time across the CTA.
+// descending.  Each sweep visits every column pair once in the round-robin
+// order: r' - 1 steps (r' = r rounded up to even) of r' / 2 disjoint pairs,
+// one warp per pair, one barrier per step.
 __device__ void jacobi_svd_dev(double2* M, double2* Vm, int r, double* S, int* perm, double* sh) {
+    (void)sh;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int j = 0; j < r; ++j)
         for (int i = threadIdx.x; i < r; i += blockDim.x) Vm[(size_t)j * r + i] = make_double2(i == j, 0.0);
     __syncthreads();
-    __shared__ double s_off;
+    __shared__ unsigned long long s_off;  // largest |cos angle| of a sweep, as the bits of a positive double
+    const int rr = r + (r & 1);           // players of the round robin (index r: a bye when r is odd)
     for (int sweep = 0; sweep < 60; ++sweep) {
-        if (threadIdx.x == 0) s_off = 0;
+        if (threadIdx.x == 0) s_off = 0ull;
         __syncthreads();
-        for (int p = 0; p < r; ++p)
-            for (int q = p + 1; q < r; ++q) {
+        for (int step = 0; step < rr - 1; ++step) {
+            for (int pi = warp; pi < rr / 2; pi += nw) {
+                // circle method: player 0 fixed, the others rotate by `step`
+                const int a0 = pi == 0 ? 0 : 1 + (pi - 1 + step) % (rr - 1);
+                const int b0 = 1 + (rr - 2 - pi + step) % (rr - 1);
+                const int p = min(a0, b0), q = max(a0, b0);
+                if (q >= r) continue;  // the bye
                 double2* up = M + (size_t)p * r;
                 double2* uq = M + (size_t)q * r;
                 double a = 0, b = 0;
                 z2 cc = make_double2(0, 0);
-                for (int i = threadIdx.x; i < r; i += blockDim.x) {
+                for (int i = lane; i < r; i += 32) {
                     a += cnorm2(up[i]);
                     b += cnorm2(uq[i]);
                     cfma(cc, cconj(up[i]), uq[i]);
                 }
-                a = bsum(a, sh);
-                b = bsum(b, sh);
-                cc = bsum2(cc, sh);
-                double ac = hypot(cc.x, cc.y);
+                a = wsum(a);
+                b = wsum(b);
+                cc = wsum2(cc);
+                const double ac = hypot(cc.x, cc.y);
                 if (ac == 0 || ac <= 1e-15 * sqrt(a * b)) continue;
-                if (threadIdx.x == 0) s_off = fmax(s_off, ac / sqrt(a * b));
-                double zeta = (b - a) / (2.0 * ac);
-                double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                double cs = 1.0 / sqrt(1.0 + t * t), sn = cs * t;
-                z2 e = make_double2(cc.x / ac, cc.y / ac);
-                z2 se = cscale(e, sn), sce = cscale(cconj(e), sn);
+                if (lane == 0) atomicMax(&s_off, (unsigned long long)__double_as_longlong(ac / sqrt(a * b)));
+                const double zeta = (b - a) / (2.0 * ac);
+                const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                const double cs = 1.0 / sqrt(1.0 + t * t), sn = cs * t;
+                const z2 e = make_double2(cc.x / ac, cc.y / ac);
+                const z2 se = cscale(e, sn), sce = cscale(cconj(e), sn);
                 double2* vp = Vm + (size_t)p * r;
                 double2* vq = Vm + (size_t)q * r;
-                for (int i = threadIdx.x; i < r; i += blockDim.x) {
+                for (int i = lane; i < r; i += 32) {
                     z2 x = up[i], y = uq[i];
                     up[i] = csub(cscale(x, cs), cmul(sce, y));
                     uq[i] = cadd(cmul(se, x), cscale(y, cs));
@@ -626,16 +660,19 @@ __device__ void jacobi_svd_dev(double2* M, double2* Vm, int r, double* S, int* p
                     vp[i] = csub(cscale(vx, cs), cmul(sce, vy));
                     vq[i] = cadd(cmul(se, vx), cscale(vy, cs));
                 }
-                __syncthreads();
             }
+            __syncthreads();
+        }
+        const double off = __longlong_as_double((long long)s_off);
         __syncthreads();
-        if (s_off < 1e-15) break;
-        __syncthreads();
+        if (off < 1e-15) break;
     }
     // singular values, descending order (stable)
-    for (int j = 0; j < r; ++j) {
-        double v = bnsq(M + (size_t)j * r, r, sh);
-        if (threadIdx.x == 0) S[j] = sqrt(v);
+    for (int j = warp; j < r; j += nw) {
+        double v = 0;
+        for (int i = lane; i < r; i += 32) v += cnorm2(M[(size_t)j * r + i]);
+        v = wsum(v);
+        if (lane == 0) S[j] = sqrt(v);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -714,16 +751,27 @@ __global__ void __launch_bounds__(LEAF_THREADS) hm_recompress_kernel(HLeaf* __re
         for (int64_t i = threadIdx.x; i < n; i += blockDim.x) V[(size_t)t * n + i] = outV[(size_t)t * n + i];
     }
     __syncthreads();
-    // calculate_norm_estimate (aca.rs:212-222)
+    // calculate_norm_estimate (aca.rs:212-222): for each rank a, its products
+    // with the earlier ranks one warp each, summed in rank order by one thread
+    __shared__ double s_prod[256];  // keep <= kmax <= 256
     double tot = 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int a = 0; a < keep; ++a) {
         double nu = bnsq(U + (size_t)a * m, m, sh), nv = bnsq(V + (size_t)a * n, n, sh);
-        tot += nu * nv;
-        for (int b = 0; b < a; ++b) {
-            z2 du = bdotu(U + (size_t)a * m, U + (size_t)b * m, m, sh);
-            z2 dv = bdotu(V + (size_t)a * n, V + (size_t)b * n, n, sh);
-            tot += 2.0 * hypot(du.x, du.y) * hypot(dv.x, dv.y);
+        for (int b = warp; b < a; b += nw) {
+            z2 du = make_double2(0, 0), dv = make_double2(0, 0);
+            for (int64_t i = lane; i < m; i += 32) cfma(du, U[(size_t)a * m + i], U[(size_t)b * m + i]);
+            for (int64_t j = lane; j < n; j += 32) cfma(dv, V[(size_t)a * n + j], V[(size_t)b * n + j]);
+            du = wsum2(du);
+            dv = wsum2(dv);
+            if (lane == 0) s_prod[b] = 2.0 * hypot(du.x, du.y) * hypot(dv.x, dv.y);
         }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            tot += nu * nv;
+            for (int b = 0; b < a; ++b) tot += s_prod[b];
+        }
+        __syncthreads();
     }
     if (threadIdx.x == 0) {
         L.rank = keep;
@@ -818,7 +866,7 @@ static GenParams gen_params(const Problem& p, int side) {
     return g;
 }
 
-constexpr int ACA_RMAX = 256;
+constexpr int ACA_RMAX = 256;  // also the size of the ACA kernel's s_prod
 
 // The cluster tree and block leaves of a problem's collocation points (they
 // depend on the geometry, the leaf size and eta only, not on the frequency).
