@@ -338,8 +338,13 @@ def main():
         ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_MIXED, precond, bem._ptr(sc), bem._ptr(inc), reps, check))
 
     if args.profile_only:
+        # the library's per-stage timing runs GMRES iteration by iteration:
+        # every kernel is its own launch (a profiler sees them, as it does not
+        # inside the solve graph's device-side loop)
+        ctx.set_profiling(True)
         run_mixed()
         torch.cuda.synchronize()
+        print(json.dumps({k: v["ms"] for k, v in ctx.profile().items()}))
         return
 
     def barrier():

@@ -3,7 +3,7 @@
 // different sizes (ragged layout, per-system offsets in GmSys).
 //
 // One iteration is the fixed launch sequence
-//   apply(START) -> start -> apply(Q) -> arnoldi -> apply(CHECK) -> check
+//   apply(START) -> start -> apply(Q) -> [Gram-Schmidt x 2] -> arnoldi -> apply(CHECK) -> check
 // where every kernel reads the per-system state and returns immediately when
 // it has nothing to do.  The sequence can therefore be issued step by step
 // (plain form, host reads the state after each step) or captured into a CUDA
@@ -11,8 +11,10 @@
 //
 // Operator: FP64 matrix (plain form, bit-for-bit the reference arithmetic up
 // to summation order) or FP32 matrix with FP64 vectors and compensated
-// products/sums (mixed form).  Arnoldi (modified Gram-Schmidt), Givens
-// rotations, the small triangular solve and the stopping test are FP64.
+// products/sums (mixed form).  Arnoldi, Givens rotations, the small
+// triangular solve and the stopping test are FP64: the reference form keeps
+// its single-CTA modified Gram-Schmidt, the mixed and refined forms
+// orthogonalise across the whole GPU (classical Gram-Schmidt twice).
 #include <mutex>
 
 #include "common.cuh"
@@ -50,24 +52,6 @@ __device__ __forceinline__ void ff_acc(float& hi, float& lo, float a, float b) {
     two_sum(hi, p, s, err);
     hi = s;
     lo += err + e;
-}
-
-// (h, l) += a b for float-float a and b: the hi product exactly (FMA), the
-// cross terms to first order, renormalised.
-__device__ __forceinline__ void ff_madd(float& h, float& l, float ah, float al, float bh, float bl) {
-    const float p = ah * bh;
-    const float pe = fmaf(ah, bh, -p) + fmaf(ah, bl, al * bh);
-    float s, e;
-    two_sum(h, p, s, e);
-    e += l + pe;
-    h = s + e;
-    l = e - (h - s);
-}
-
-// A complex FP64 value as float-float parts (re hi, re lo, im hi, im lo).
-__device__ __forceinline__ float4 ff_split(double2 x) {
-    const float rh = (float)x.x, ih = (float)x.y;
-    return make_float4(rh, (float)(x.x - (double)rh), ih, (float)(x.y - (double)ih));
 }
 
 // Batched operator application W_s = A_s v_s, v_s = x_s (START/CHECK) or
@@ -298,11 +282,9 @@ __global__ void __launch_bounds__(AR_THREADS) gm_start_kernel(GmBatch bt) {
         acc += r.x * r.x + r.y * r.y;
     }
     double rn = sqrt(block_sum(acc, sh));
-    float4* Qf = (bt.Qf && !bt.ref_dotc) ? bt.Qf + g.q : nullptr;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
         double2 r = Q[i];
         Q[i] = make_double2(r.x / rn, r.y / rn);
-        if (Qf) Qf[i] = ff_split(Q[i]);
     }
     double xn = vec_norm(bt.X + g.v, n, sh);
     if (threadIdx.x == 0) {
@@ -316,6 +298,93 @@ __global__ void __launch_bounds__(AR_THREADS) gm_start_kernel(GmBatch bt) {
         st.need_start = 0;
         st.check = 0;
         st.num_mv += zero_x ? 0 : 1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gram-Schmidt of the mixed and refined forms across the whole GPU: classical
+// Gram-Schmidt applied twice (the second pass re-orthogonalises; as accurate
+// as the modified form), in FP64.  Every CTA owns a chunk of GS_ROWS rows of
+// one system: the dots kernel forms its chunk's contribution to q_i^H w for
+// every i <= k (a warp per basis vector), the update kernel adds the chunks'
+// contributions in chunk order and subtracts Q h from its rows (and, after
+// the second pass, leaves the squared norm of its rows).  Systems pending a
+// Krylov step only (the Arnoldi kernel's predicate).
+constexpr int GS_ROWS = 512, GS_THREADS = 256;
+
+__device__ __forceinline__ bool gm_arnoldi_active(const GmState& st) {
+    return !(st.done || st.need_start || st.check);
+}
+
+__global__ void __launch_bounds__(GS_THREADS) gm_gs_dots_kernel(GmBatch bt) {
+    const int s = blockIdx.y, c = blockIdx.x;
+    const GmState& st = bt.st[s];
+    if (!gm_arnoldi_active(st)) return;
+    const GmView g = gm_view(bt, s);
+    const int64_t r0 = (int64_t)c * GS_ROWS;
+    if (r0 >= g.n) return;
+    const int rows = (int)min((int64_t)GS_ROWS, g.n - r0);
+    __shared__ double2 ws[GS_ROWS];
+    const double2* W = bt.W + g.v + r0;
+    for (int l = threadIdx.x; l < rows; l += GS_THREADS) ws[l] = W[l];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const double2* Q = bt.Q + g.q + r0;
+    double2* part = bt.gs_part + ((size_t)s * bt.gs_chunks + c) * (bt.m + 1);
+    for (int i = warp; i <= st.k; i += GS_THREADS / 32) {
+        const double2* qi = Q + (size_t)i * g.n;
+        double2 acc = make_double2(0, 0);
+        for (int l = lane; l < rows; l += 32) cfma(acc, cconj(qi[l]), ws[l]);
+        for (int o = 16; o > 0; o >>= 1) {
+            acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+            acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+        }
+        if (lane == 0) part[i] = acc;
+    }
+}
+
+// pass 0: hk1[i] = h_i; pass 1: hk1[i] += h_i and the chunk's squared norm.
+__global__ void __launch_bounds__(GS_THREADS) gm_gs_update_kernel(GmBatch bt, int pass) {
+    const int s = blockIdx.y, c = blockIdx.x;
+    const GmState& st = bt.st[s];
+    if (!gm_arnoldi_active(st)) return;
+    const GmView g = gm_view(bt, s);
+    const int64_t r0 = (int64_t)c * GS_ROWS;
+    if (r0 >= g.n) return;
+    const int rows = (int)min((int64_t)GS_ROWS, g.n - r0);
+    const int k = st.k;
+    const int nch = (int)((g.n + GS_ROWS - 1) / GS_ROWS);
+    extern __shared__ double2 hsum[];  // k + 1 coefficients
+    __shared__ double red[GS_THREADS / 32];
+    const double2* part = bt.gs_part + (size_t)s * bt.gs_chunks * (bt.m + 1);
+    for (int i = threadIdx.x; i <= k; i += GS_THREADS) {
+        double2 h = make_double2(0, 0);
+        for (int cc = 0; cc < nch; ++cc) h = cadd(h, part[(size_t)cc * (bt.m + 1) + i]);
+        hsum[i] = h;
+    }
+    __syncthreads();
+    if (c == 0 && threadIdx.x == 0) {
+        GmSmall sm = gm_small(bt, s);
+        for (int i = 0; i <= k; ++i) sm.hk1[i] = pass == 0 ? hsum[i] : cadd(sm.hk1[i], hsum[i]);
+    }
+    double2* W = bt.W + g.v + r0;
+    const double2* Q = bt.Q + g.q + r0;
+    double nn = 0;
+    for (int l = threadIdx.x; l < rows; l += GS_THREADS) {
+        double2 a = W[l];
+        for (int i = 0; i <= k; ++i) cfma(a, cneg(hsum[i]), Q[(size_t)i * g.n + l]);
+        W[l] = a;
+        nn += a.x * a.x + a.y * a.y;
+    }
+    if (pass == 1) {
+        for (int o = 16; o > 0; o >>= 1) nn += __shfl_down_sync(0xffffffffu, nn, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nn;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (int w = 0; w < GS_THREADS / 32; ++w) t += red[w];
+            bt.gs_norm[(size_t)s * bt.gs_chunks + c] = t;
+        }
     }
 }
 
@@ -341,55 +410,18 @@ __global__ void __launch_bounds__(AR_THREADS) gm_arnoldi_kernel(GmBatch bt, int 
     GmSmall sm = gm_small(bt, s);
     double2* qk1 = Q + (size_t)(k + 1) * n;
     double hn;
-    if (bt.Qf && !bt.ref_dotc && w_in_smem) {
-        // modified Gram-Schmidt in float-float on the FP32 pipes (GB300's FP64
-        // rate is ~1/60 of its FP32 rate; this loop was bound by it), against
-        // the float-float copy of the basis; ~1e-14 relative
-        float4* wf = reinterpret_cast<float4*>(wsh);
-        const float4* Qf = bt.Qf + g.q;
-        for (int64_t l = threadIdx.x; l < n; l += blockDim.x) wf[l] = ff_split(Wg[l]);
-        __syncthreads();
-        for (int i = 0; i <= k; ++i) {
-            const float4* qi = Qf + (size_t)i * n;
-            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;  // q_i^H w
-            for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
-                const float4 q = qi[l], a = wf[l];
-                ff_madd(rh, rl, q.x, q.y, a.x, a.y);
-                ff_madd(rh, rl, q.z, q.w, a.z, a.w);
-                ff_madd(ih, il, q.x, q.y, a.z, a.w);
-                ff_madd(ih, il, -q.z, -q.w, a.x, a.y);
-            }
-            const double2 h = block_sum2(make_double2((double)rh + (double)rl, (double)ih + (double)il), sh);
-            const float4 hf = ff_split(h);
-            for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
-                float4 a = wf[l];
-                const float4 q = qi[l];
-                ff_madd(a.x, a.y, -hf.x, -hf.y, q.x, q.y);  // re -= hr qr - hi qi
-                ff_madd(a.x, a.y, hf.z, hf.w, q.z, q.w);
-                ff_madd(a.z, a.w, -hf.x, -hf.y, q.z, q.w);  // im -= hr qi + hi qr
-                ff_madd(a.z, a.w, -hf.z, -hf.w, q.x, q.y);
-                wf[l] = a;
-            }
-            if (threadIdx.x == 0) sm.hk1[i] = h;
-            __syncthreads();
-        }
-        float nh = 0.f, nl = 0.f;
-        for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
-            const float4 a = wf[l];
-            ff_madd(nh, nl, a.x, a.y, a.x, a.y);
-            ff_madd(nh, nl, a.z, a.w, a.z, a.w);
-        }
-        hn = sqrt(block_sum((double)nh + (double)nl, sh));
+    if (bt.gs_part && !bt.ref_dotc) {
+        // orthogonalised across the GPU (gm_gs_dots_kernel /
+        // gm_gs_update_kernel): h_{:,k} is in hk1[0..k], w in W; its norm
+        // from the chunks' partial squares
+        double nn = 0;
+        const int nch = (int)((n + GS_ROWS - 1) / GS_ROWS);  // this system's chunks (ragged batches)
+        for (int c = 0; c < nch; ++c) nn += bt.gs_norm[(size_t)s * bt.gs_chunks + c];
+        hn = sqrt(nn);
         const double sc = 1.0 / hn;
-        const float sch = (float)sc, scl = (float)(sc - (double)sch);
-        float4* qf1 = bt.Qf + g.q + (size_t)(k + 1) * n;
         for (int64_t l = threadIdx.x; l < n; l += blockDim.x) {
-            const float4 a = wf[l];
-            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-            ff_madd(q.x, q.y, a.x, a.y, sch, scl);
-            ff_madd(q.z, q.w, a.z, a.w, sch, scl);
-            qf1[l] = q;
-            qk1[l] = make_double2((double)q.x + (double)q.y, (double)q.z + (double)q.w);
+            const double2 a = Wg[l];
+            qk1[l] = make_double2(a.x * sc, a.y * sc);
         }
     } else {
         if (w_in_smem)
@@ -630,15 +662,18 @@ void gm_prepare(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, int m, const
     size_t oS = carve(sizeof(double2) * nsys * small), oSt = carve(sizeof(GmState) * nsys);
     size_t oN = carve(sizeof(double) * nsys * 1024 + sizeof(double) * nsys);
     ws.w_in_smem = (n * sizeof(double2) <= AR_SMEM_CAP);
-    // float-float basis copy for the Gram-Schmidt on the FP32 pipes
-    const bool qf = !ref_dotc && ws.w_in_smem;
-    size_t oQf = qf ? carve(sizeof(float4) * nsys * bt.qstride) : 0;
+    // partial sums of the whole-GPU Gram-Schmidt (forms other than the reference's)
+    const int gsc = ref_dotc ? 0 : (int)((n + GS_ROWS - 1) / GS_ROWS);
+    size_t oG = gsc ? carve(sizeof(double2) * nsys * gsc * (m + 1)) : 0;
+    size_t oGn = gsc ? carve(sizeof(double) * nsys * gsc) : 0;
     ws.memb().ensure(bytes);
     char* base = ws.memb().as<char>();
     bt.X = reinterpret_cast<double2*>(base + oX);
     bt.B = reinterpret_cast<double2*>(base + oB);
     bt.Q = reinterpret_cast<double2*>(base + oQ);
-    bt.Qf = qf ? reinterpret_cast<float4*>(base + oQf) : nullptr;
+    bt.gs_chunks = gsc;
+    bt.gs_part = gsc ? reinterpret_cast<double2*>(base + oG) : nullptr;
+    bt.gs_norm = gsc ? reinterpret_cast<double*>(base + oGn) : nullptr;
     bt.W = reinterpret_cast<double2*>(base + oW);
     bt.part = reinterpret_cast<double2*>(base + oP);
     bt.tickets = reinterpret_cast<int*>(base + oT);
@@ -694,7 +729,9 @@ size_t gm_prepare_external(Context& ctx, GmWorkspace& ws, int nsys, int64_t n, i
     bt.X = reinterpret_cast<double2*>(base + oX);
     bt.B = reinterpret_cast<double2*>(base + oB);
     bt.Q = reinterpret_cast<double2*>(base + oQ);
-    bt.Qf = nullptr;  // caller memory: the FP64 Gram-Schmidt
+    bt.gs_part = nullptr;  // caller memory: the single-CTA Gram-Schmidt
+    bt.gs_norm = nullptr;
+    bt.gs_chunks = 0;
     bt.W = reinterpret_cast<double2*>(base + oW);
     bt.part = reinterpret_cast<double2*>(base + oP);
     bt.tickets = reinterpret_cast<int*>(base + oT);
@@ -766,14 +803,18 @@ void gm_prepare_ragged(Context& ctx, GmWorkspace& ws, const std::vector<int64_t>
     size_t oN = carve(sizeof(double) * nsys * 1024 + sizeof(double) * nsys);
     size_t oD = carve(sizeof(GmSys) * nsys);
     ws.w_in_smem = (nmax * sizeof(double2) <= AR_SMEM_CAP);
-    // float-float basis copy for the Gram-Schmidt on the FP32 pipes
-    size_t oQf = ws.w_in_smem ? carve(sizeof(float4) * q) : 0;
+    // partial sums of the whole-GPU Gram-Schmidt
+    const int gsc = (int)((nmax + GS_ROWS - 1) / GS_ROWS);
+    size_t oG = carve(sizeof(double2) * nsys * gsc * (m + 1));
+    size_t oGn = carve(sizeof(double) * nsys * gsc);
     ws.memb().ensure(bytes);
     char* base = ws.memb().as<char>();
     bt.X = reinterpret_cast<double2*>(base + oX);
     bt.B = reinterpret_cast<double2*>(base + oB);
     bt.Q = reinterpret_cast<double2*>(base + oQ);
-    bt.Qf = ws.w_in_smem ? reinterpret_cast<float4*>(base + oQf) : nullptr;
+    bt.gs_chunks = gsc;
+    bt.gs_part = reinterpret_cast<double2*>(base + oG);
+    bt.gs_norm = reinterpret_cast<double*>(base + oGn);
     bt.W = reinterpret_cast<double2*>(base + oW);
     bt.part = reinterpret_cast<double2*>(base + oP);
     bt.tickets = reinterpret_cast<int*>(base + oT);
@@ -890,8 +931,19 @@ void gm_launch_iteration(Context& ctx, GmWorkspace& ws, cudaEvent_t ev_q0, cudaE
     if (ev_q0) BEM_CUDA(cudaEventRecord(ev_q0, ctx.stream));
     launch_apply(ctx, ws, MV_Q);
     if (ev_q1) BEM_CUDA(cudaEventRecord(ev_q1, ctx.stream));
-    size_t dyn = ws.w_in_smem ? (size_t)ws.bt.n * sizeof(double2) : 0;
-    gm_arnoldi_kernel<<<nsys, AR_THREADS, dyn, ctx.stream>>>(ws.bt, ws.w_in_smem ? 1 : 0);
+    const bool gs = ws.bt.gs_part && !ws.bt.ref_dotc;
+    if (gs) {
+        const dim3 grid((unsigned)ws.bt.gs_chunks, (unsigned)nsys);
+        const size_t hsm = sizeof(double2) * (size_t)(ws.bt.m + 1);
+        for (int pass = 0; pass < 2; ++pass) {
+            gm_gs_dots_kernel<<<grid, GS_THREADS, 0, ctx.stream>>>(ws.bt);
+            BEM_CHECK_LAUNCH(&ctx);
+            gm_gs_update_kernel<<<grid, GS_THREADS, hsm, ctx.stream>>>(ws.bt, pass);
+            BEM_CHECK_LAUNCH(&ctx);
+        }
+    }
+    size_t dyn = (!gs && ws.w_in_smem) ? (size_t)ws.bt.n * sizeof(double2) : 0;
+    gm_arnoldi_kernel<<<nsys, AR_THREADS, dyn, ctx.stream>>>(ws.bt, (!gs && ws.w_in_smem) ? 1 : 0);
     BEM_CHECK_LAUNCH(&ctx);
     launch_apply(ctx, ws, MV_CHECK);
     gm_check_kernel<<<nsys, AR_THREADS, 0, ctx.stream>>>(ws.bt);

@@ -41,8 +41,13 @@ struct GmBatch {
     double2* small;     // per-system Hessenberg / rotations
     GmState* st;
     double2* Z;         // flexible right preconditioning: Z[:, k] = M Q[:, k] (nullptr: none)
-    float4* Qf = nullptr;  // float-float copy of Q (re hi, re lo, im hi, im lo) for the
-                           // Gram-Schmidt of the mixed / refined forms (nullptr: FP64)
+    // Gram-Schmidt of the mixed / refined forms across the whole GPU (null:
+    // the single-CTA modified Gram-Schmidt of the reference form): per system,
+    // partial dot products of every row chunk with the basis (gs_chunks x
+    // (m + 1)) and partial squared norms (gs_chunks)
+    double2* gs_part = nullptr;
+    double* gs_norm = nullptr;
+    int gs_chunks = 0;
 };
 
 // Whether the operator application of `mode` has work for a system.

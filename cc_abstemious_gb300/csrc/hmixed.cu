@@ -12,14 +12,15 @@
 //     181-195 applies it as U (V^T x)).
 //
 // The batched mat-vec W_s = A_s v_s (h_matrix.rs:218-234) of every active
-// system runs in three launches:
+// system runs in four launches:
 //   gather   v_s in cluster order, split into FP32 hi + lo parts;
-//   project  t_b = V_b^T v[cols_b] for every admissible block (one CTA per
-//            block and system, a warp per rank column);
-//   rows     for every leaf row cluster (64 rows), the sum over the blocks that
-//            cover it of their dense rows times v[cols] or their U rows times
-//            t_b, written back in the original order (one CTA per cluster and
-//            system; no atomics, a fixed order).
+//   project  t_b = V_b^T v[cols_b], one warp per group of four rank columns
+//            of every admissible block (a flat list per operator);
+//   rows     for every leaf row cluster (<= 64 rows), the blocks that cover it
+//            in chunks of eight, one warp per block: its dense rows times
+//            v[cols] or its U rows times t_b, the chunk's sum stored apart;
+//   reduce   every cluster's chunk sums added in chunk order and written back
+//            in the original order (no atomics, a fixed order).
 // Each stored FP32 entry is read once per mat-vec: the kernel is bound by HBM
 // bandwidth (8 B per stored entry).  Products are FP32; Krylov mat-vecs fold
 // partial sums of 16 terms into FP64, residual mat-vecs (START / CHECK) split
@@ -63,7 +64,36 @@ struct HmDev {
     const int32_t* item_row;  // the cluster's first row, local to the block
     const int64_t* perm;      // permuted position -> original index
     float2 *xh, *xl;          // nsys x n gathered operand, hi + lo
-    double2* t;               // nsys x ttot projections
+    float4* t;                // nsys x ttot projections, float-float (re hi, im hi, re lo, im lo)
+    const struct HmItem* items;  // [op * nitems + it]: the rows pass, packed
+    int64_t nitems;
+    const struct HmProj* proj;   // [op * pstride + q]: one per rank column
+    int64_t pstride;
+    const int32_t* nproj;        // [op]: rank columns of the operator
+    const int32_t* ch_rc;        // [chunk]: cluster of a chunk of items
+    const int32_t* ch_it;        // [chunk + 1]: the chunk's items
+    const int32_t* rc_ch;        // [cluster + 1]: the cluster's chunks
+    int64_t nchunks;
+    float4* part;                // nsys x nchunks x 64 partial row sums (float-float)
+};
+
+// One block's contribution to one row cluster, packed for a single load: the
+// block's data at `off` (dense: m x n; low-rank: U, m x r), its leading
+// dimension m, len = n (dense) or r (low-rank), the cluster's first row local
+// to the block, and the operand: columns from c0 (dense) or the projections
+// from toff (low-rank).
+struct HmItem {
+    int64_t off, src;  // store offset; c0 (dense) or toff (low-rank)
+    int32_t ld, len, lr, adm;
+};
+
+// Up to PJ_COLS consecutive rank columns k .. k + cnt of one admissible
+// block: V's column k at voff (columns n entries apart), the block's first
+// column c0, and the projection slot of column k.
+constexpr int PJ_COLS = 4;
+struct HmProj {
+    int64_t voff, c0, t;
+    int32_t n, cnt;
 };
 
 __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
@@ -82,14 +112,26 @@ __device__ __forceinline__ void ff_acc2(float& hi, float& lo, float a, float b) 
     lo += err + e;
 }
 
-// Accumulator of a complex sum of FP32 products with an FP64 operand split
-// into hi + lo: EXACT -- every product exact, float-float sums (residuals);
-// otherwise FP32 sums of FOLD terms moved into FP64 (Krylov vectors).
+// Accumulator of a complex sum of FP32 products with an operand split into
+// hi + lo floats, in FP32 arithmetic only (GB300 runs FP64 at ~1/64 of the
+// FP32 rate, so FP64 in these streaming loops would bound them): EXACT --
+// every product split exactly by an FMA, float-float sums (residuals);
+// otherwise FP32 sums of FOLD terms folded into float-float (Krylov vectors).
 constexpr int FOLD = 16;
+
+// (h, l) += (h2, l2), renormalised.
+__device__ __forceinline__ void ff_add(float& h, float& l, float h2, float l2) {
+    float s, e;
+    two_sum_f(h, h2, s, e);
+    e += l + l2;
+    h = s + e;
+    l = e - (h - s);
+}
+
 template <int EXACT>
 struct CAcc {
-    float rh = 0, rl = 0, ih = 0, il = 0;  // EXACT: float-float; else the open FP32 partial sum in rh, ih
-    double dr = 0, di = 0;
+    float rh = 0, rl = 0, ih = 0, il = 0;  // float-float real and imaginary sums
+    float pr = 0, pi = 0;                  // FAST: the open FP32 partial sums
     int cnt = 0;
     __device__ __forceinline__ void add(float2 a, float2 xh, float2 xl) {
         if (EXACT) {
@@ -100,21 +142,43 @@ struct CAcc {
             rl = fmaf(a.x, xl.x, fmaf(-a.y, xl.y, rl));
             il = fmaf(a.x, xl.y, fmaf(a.y, xl.x, il));
         } else {
-            rh = fmaf(a.x, xh.x, fmaf(-a.y, xh.y, rh));
-            ih = fmaf(a.x, xh.y, fmaf(a.y, xh.x, ih));
-            if (++cnt == FOLD) {
-                dr += rh;
-                di += ih;
-                rh = ih = 0.f;
-                cnt = 0;
-            }
+            pr = fmaf(a.x, xh.x, fmaf(-a.y, xh.y, pr));
+            pi = fmaf(a.x, xh.y, fmaf(a.y, xh.x, pi));
+            if (++cnt == FOLD) fold();
         }
     }
-    __device__ __forceinline__ double2 value() const {
-        if (EXACT) return make_double2((double)rh + (double)rl, (double)ih + (double)il);
-        return make_double2(dr + rh, di + ih);
+    __device__ __forceinline__ void fold() {
+        float s, e;
+        two_sum_f(rh, pr, s, e);
+        rh = s;
+        rl += e;
+        two_sum_f(ih, pi, s, e);
+        ih = s;
+        il += e;
+        pr = pi = 0.f;
+        cnt = 0;
+    }
+    // the sum as float-float: (re hi, im hi, re lo, im lo)
+    __device__ __forceinline__ float4 ff() {
+        if (!EXACT) fold();
+        return make_float4(rh, ih, rl, il);
     }
 };
+
+// Sum of a float-float complex value over the 32 lanes of a warp.
+__device__ __forceinline__ float4 warp_ff_sum(float4 v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const float hx = __shfl_xor_sync(0xffffffffu, v.x, o), hy = __shfl_xor_sync(0xffffffffu, v.y, o);
+        const float lx = __shfl_xor_sync(0xffffffffu, v.z, o), ly = __shfl_xor_sync(0xffffffffu, v.w, o);
+        ff_add(v.x, v.z, hx, lx);
+        ff_add(v.y, v.w, hy, ly);
+    }
+    return v;
+}
+
+__device__ __forceinline__ double2 ff_to_double(float4 v) {
+    return make_double2((double)v.x + (double)v.z, (double)v.y + (double)v.w);
+}
 
 __device__ __forceinline__ const double2* hm_operand(const GmBatch& bt, const GmState& st, int s, int mode) {
     const GmView g = gm_view(bt, s);
@@ -136,86 +200,142 @@ __global__ void hmx_gather_kernel(HmDev h, GmBatch bt, int mode) {
 
 constexpr int PJ_WARPS = 8;
 
+// t_b[k] = V_b[:, k]^T v[cols_b]: one warp per group of up to PJ_COLS rank
+// columns of an admissible block (a flat list per operator), lanes along
+// the columns, the group's loads in flight together.
 template <int EXACT>
 __global__ void __launch_bounds__(PJ_WARPS * 32) hmx_project_kernel(HmDev h, GmBatch bt, int mode) {
     const int s = blockIdx.y;
     if (!gm_apply_active(bt, bt.st[s], mode)) return;
-    const int b = h.adm_list[blockIdx.x];
     const int op = s / h.R;
-    const size_t ob = (size_t)op * h.nb + b;
-    const int r = h.rank[ob];
-    const HmBlock B = h.blk[b];
-    const float2* V = h.store + h.off[ob] + (size_t)B.m * r;
-    const float2* xh = h.xh + (size_t)s * h.n + B.c0;
-    const float2* xl = h.xl + (size_t)s * h.n + B.c0;
-    double2* t = h.t + (size_t)s * h.ttot + h.toff[ob];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = warp; k < r; k += PJ_WARPS) {
-        const float2* vk = V + (size_t)k * B.n;
-        CAcc<EXACT> acc;
-        for (int64_t j = lane; j < B.n; j += 32) acc.add(__ldcs(vk + j), xh[j], xl[j]);
-        double2 v = acc.value();
-        for (int o = 16; o > 0; o >>= 1) {
-            v.x += __shfl_down_sync(0xffffffffu, v.x, o);
-            v.y += __shfl_down_sync(0xffffffffu, v.y, o);
-        }
-        if (lane == 0) t[k] = v;
+    const int64_t q = (int64_t)blockIdx.x * PJ_WARPS + (threadIdx.x >> 5);
+    if (q >= h.nproj[op]) return;
+    const int lane = threadIdx.x & 31;
+    const HmProj P = h.proj[(size_t)op * h.pstride + q];
+    const float2* v0 = h.store + P.voff;
+    const float2* xh = h.xh + (size_t)s * h.n + P.c0;
+    const float2* xl = h.xl + (size_t)s * h.n + P.c0;
+    CAcc<EXACT> acc[PJ_COLS];
+    for (int64_t j = lane; j < P.n; j += 32) {
+        float2 a[PJ_COLS];
+#pragma unroll
+        for (int c = 0; c < PJ_COLS; ++c)
+            a[c] = c < P.cnt ? __ldcs(v0 + (size_t)c * P.n + j) : make_float2(0.f, 0.f);
+        const float2 x1 = xh[j], x2 = xl[j];
+#pragma unroll
+        for (int c = 0; c < PJ_COLS; ++c)
+            if (c < P.cnt) acc[c].add(a[c], x1, x2);
+    }
+#pragma unroll
+    for (int c = 0; c < PJ_COLS; ++c) {
+        if (c >= P.cnt) break;  // uniform over the warp
+        const float4 v = warp_ff_sum(acc[c].ff());
+        if (lane == 0) h.t[(size_t)s * h.ttot + P.t + c] = v;
     }
 }
 
-constexpr int RW_ROWS = 64, RW_SLICES = 4, RW_THREADS = RW_ROWS * RW_SLICES;
+constexpr int RW_ROWS = 64, RW_WARPS = 8, RW_THREADS = RW_WARPS * 32;
 
+// Partial row sums of one chunk of a cluster's items (up to RW_WARPS): one
+// warp per item, each lane two rows (lane, lane + 32); the warps' sums are
+// added in shared memory and stored as the chunk's partial.  Clusters hold
+// at most RW_ROWS rows (leaf size <= 64, checked on the host).
 template <int EXACT>
 __global__ void __launch_bounds__(RW_THREADS) hmx_rows_kernel(HmDev h, GmBatch bt, int mode) {
     const int s = blockIdx.y;
     if (!gm_apply_active(bt, bt.st[s], mode)) return;
-    __shared__ double2 red[RW_SLICES][RW_ROWS];
-    const int rc = blockIdx.x, op = s / h.R;
-    const int q = threadIdx.x / RW_ROWS;
-    const int64_t rs = h.rc_start[rc];
-    const int rows = (int)(h.rc_start[rc + 1] - rs);
-    const float2* xh = h.xh + (size_t)s * h.n;
-    const float2* xl = h.xl + (size_t)s * h.n;
-    const double2* tsys = h.t + (size_t)s * h.ttot;
-    const GmView g = gm_view(bt, s);
-    // clusters of up to RW_ROWS rows take one pass (leaf size <= 64)
-    for (int i0 = 0; i0 < rows; i0 += RW_ROWS) {
-        const int i = i0 + threadIdx.x % RW_ROWS;
-        CAcc<EXACT> acc;
-        if (i < rows) {
-            for (int it = h.rc_ptr[rc]; it < h.rc_ptr[rc + 1]; ++it) {
-                const int b = h.item_blk[it];
-                const int64_t lr = h.item_row[it] + i;
-                const size_t ob = (size_t)op * h.nb + b;
-                const HmBlock B = h.blk[b];
-                const float2* D = h.store + h.off[ob];
-                if (!B.adm) {
-                    for (int64_t j = q; j < B.n; j += RW_SLICES)
-                        acc.add(__ldcs(D + (size_t)j * B.m + lr), xh[B.c0 + j], xl[B.c0 + j]);
-                } else {
-                    const int r = h.rank[ob];
-                    const double2* t = tsys + h.toff[ob];
-                    for (int k = q; k < r; k += RW_SLICES) {
-                        const double2 tk = t[k];
-                        const float thx = (float)tk.x, thy = (float)tk.y;
-                        acc.add(__ldcs(D + (size_t)k * B.m + lr), make_float2(thx, thy),
-                                make_float2((float)(tk.x - (double)thx), (float)(tk.y - (double)thy)));
-                    }
+    __shared__ float4 red[RW_WARPS][RW_ROWS];
+    const int64_t ch = blockIdx.x;
+    const int rc = h.ch_rc[ch], op = s / h.R;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rows = (int)(h.rc_start[rc + 1] - h.rc_start[rc]);
+    const bool oka = lane < rows, okb = lane + 32 < rows;
+    CAcc<EXACT> acc_a, acc_b;
+    const int it = h.ch_it[ch] + warp;
+    if (it < h.ch_it[ch + 1]) {
+        const HmItem I = h.items[(size_t)op * h.nitems + it];
+        const float2* D = h.store + I.off + I.lr;
+        if (!I.adm) {
+            const float2* xa = h.xh + (size_t)s * h.n + I.src;
+            const float2* xb = h.xl + (size_t)s * h.n + I.src;
+            int j = 0;
+            for (; j + 4 <= I.len; j += 4) {
+                float2 a[4], b[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    a[u] = oka ? __ldcs(D + (size_t)(j + u) * I.ld + lane) : make_float2(0.f, 0.f);
+                    b[u] = okb ? __ldcs(D + (size_t)(j + u) * I.ld + lane + 32) : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float2 x1 = xa[j + u], x2 = xb[j + u];
+                    acc_a.add(a[u], x1, x2);
+                    acc_b.add(b[u], x1, x2);
                 }
             }
-        }
-        red[q][threadIdx.x % RW_ROWS] = acc.value();
-        __syncthreads();
-        if (q == 0 && i < rows) {
-            double2 v = red[0][i - i0];
-            for (int u = 1; u < RW_SLICES; ++u) {
-                v.x += red[u][i - i0].x;
-                v.y += red[u][i - i0].y;
+            for (; j < I.len; ++j) {
+                const float2 a = oka ? __ldcs(D + (size_t)j * I.ld + lane) : make_float2(0.f, 0.f);
+                const float2 b = okb ? __ldcs(D + (size_t)j * I.ld + lane + 32) : make_float2(0.f, 0.f);
+                acc_a.add(a, xa[j], xb[j]);
+                acc_b.add(b, xa[j], xb[j]);
             }
-            bt.W[g.v + h.perm[rs + i]] = v;
+        } else {
+            const float4* t = h.t + (size_t)s * h.ttot + I.src;
+            int k = 0;
+            for (; k + 4 <= I.len; k += 4) {
+                float2 a[4], b[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    a[u] = oka ? __ldcs(D + (size_t)(k + u) * I.ld + lane) : make_float2(0.f, 0.f);
+                    b[u] = okb ? __ldcs(D + (size_t)(k + u) * I.ld + lane + 32) : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float4 tk = t[k + u];
+                    const float2 th = make_float2(tk.x, tk.y), tl = make_float2(tk.z, tk.w);
+                    acc_a.add(a[u], th, tl);
+                    acc_b.add(b[u], th, tl);
+                }
+            }
+            for (; k < I.len; ++k) {
+                const float4 tk = t[k];
+                const float2 th = make_float2(tk.x, tk.y), tl = make_float2(tk.z, tk.w);
+                const float2 a = oka ? __ldcs(D + (size_t)k * I.ld + lane) : make_float2(0.f, 0.f);
+                const float2 b = okb ? __ldcs(D + (size_t)k * I.ld + lane + 32) : make_float2(0.f, 0.f);
+                acc_a.add(a, th, tl);
+                acc_b.add(b, th, tl);
+            }
         }
-        __syncthreads();
     }
+    red[warp][lane] = acc_a.ff();
+    red[warp][lane + 32] = acc_b.ff();
+    __syncthreads();
+    if (threadIdx.x < RW_ROWS) {
+        float4 v = red[0][threadIdx.x];
+        for (int w = 1; w < RW_WARPS; ++w) {
+            const float4 u = red[w][threadIdx.x];
+            ff_add(v.x, v.z, u.x, u.z);
+            ff_add(v.y, v.w, u.y, u.w);
+        }
+        h.part[((size_t)s * h.nchunks + ch) * RW_ROWS + threadIdx.x] = v;
+    }
+}
+
+// W[rows of cluster rc] = the cluster's chunk partials, added in chunk order.
+__global__ void __launch_bounds__(RW_ROWS) hmx_reduce_kernel(HmDev h, GmBatch bt, int mode) {
+    const int s = blockIdx.y;
+    if (!gm_apply_active(bt, bt.st[s], mode)) return;
+    const int rc = blockIdx.x, i = threadIdx.x;
+    const int64_t rs = h.rc_start[rc];
+    if (i >= (int)(h.rc_start[rc + 1] - rs)) return;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int ch = h.rc_ch[rc]; ch < h.rc_ch[rc + 1]; ++ch) {
+        const float4 p = h.part[((size_t)s * h.nchunks + ch) * RW_ROWS + i];
+        ff_add(v.x, v.z, p.x, p.z);
+        ff_add(v.y, v.w, p.y, p.w);
+    }
+    const GmView g = gm_view(bt, s);
+    bt.W[g.v + h.perm[rs + i]] = ff_to_double(v);
 }
 
 // Repacking of one FP64 leaf into FP32 cluster order (one CTA per leaf).
@@ -368,6 +488,8 @@ struct HMixed {
     std::vector<int64_t> off, toff, rc_start, perm, pos;
     std::vector<double> norms;  // per operator
     int64_t ttot = 0, store_entries = 0, dense_entries = 0, lowrank_entries = 0;
+    int64_t nitems = 0, pstride = 0, nchunks = 0;
+    DevBuf d_items, d_proj, d_nproj, d_chrc, d_chit, d_rcch, d_part;
     int nsys = 0;
     DevBuf d_blk, d_adm, d_off, d_rank, d_toff, d_store, d_rcs, d_rcp, d_iblk, d_irow, d_perm, d_x, d_t;
     DevBuf d_diag, d_minv, d_small;
@@ -393,7 +515,17 @@ struct HMixed {
         h.perm = d_perm.as<int64_t>();
         h.xh = d_x.as<float2>();
         h.xl = h.xh + (size_t)nsys * n;
-        h.t = d_t.as<double2>();
+        h.t = d_t.as<float4>();
+        h.items = d_items.as<HmItem>();
+        h.nitems = nitems;
+        h.proj = d_proj.as<HmProj>();
+        h.pstride = pstride;
+        h.nproj = d_nproj.as<int32_t>();
+        h.ch_rc = d_chrc.as<int32_t>();
+        h.ch_it = d_chit.as<int32_t>();
+        h.rc_ch = d_rcch.as<int32_t>();
+        h.nchunks = nchunks;
+        h.part = d_part.as<float4>();
         return h;
     }
 };
@@ -411,13 +543,17 @@ void hmx_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
     const unsigned ns = (unsigned)ws.bt.nsys;
     hmx_gather_kernel<<<dim3((unsigned)((H.n + 255) / 256), ns), 256, 0, c.stream>>>(h, ws.bt, mode);
     BEM_CHECK_LAUNCH(&c);
-    if (h.nadm) {
-        if (mode == MV_Q) hmx_project_kernel<0><<<dim3((unsigned)h.nadm, ns), PJ_WARPS * 32, 0, c.stream>>>(h, ws.bt, mode);
-        else hmx_project_kernel<1><<<dim3((unsigned)h.nadm, ns), PJ_WARPS * 32, 0, c.stream>>>(h, ws.bt, mode);
+    if (h.pstride) {
+        const dim3 grid((unsigned)((h.pstride + PJ_WARPS - 1) / PJ_WARPS), ns);
+        if (mode == MV_Q) hmx_project_kernel<0><<<grid, PJ_WARPS * 32, 0, c.stream>>>(h, ws.bt, mode);
+        else hmx_project_kernel<1><<<grid, PJ_WARPS * 32, 0, c.stream>>>(h, ws.bt, mode);
         BEM_CHECK_LAUNCH(&c);
     }
-    if (mode == MV_Q) hmx_rows_kernel<0><<<dim3((unsigned)H.nrc, ns), RW_THREADS, 0, c.stream>>>(h, ws.bt, mode);
-    else hmx_rows_kernel<1><<<dim3((unsigned)H.nrc, ns), RW_THREADS, 0, c.stream>>>(h, ws.bt, mode);
+    const dim3 gr((unsigned)h.nchunks, ns);
+    if (mode == MV_Q) hmx_rows_kernel<0><<<gr, RW_THREADS, 0, c.stream>>>(h, ws.bt, mode);
+    else hmx_rows_kernel<1><<<gr, RW_THREADS, 0, c.stream>>>(h, ws.bt, mode);
+    BEM_CHECK_LAUNCH(&c);
+    hmx_reduce_kernel<<<dim3((unsigned)H.nrc, ns), RW_ROWS, 0, c.stream>>>(h, ws.bt, mode);
     BEM_CHECK_LAUNCH(&c);
 }
 
@@ -554,6 +690,63 @@ std::shared_ptr<HMixed> hmixed_build(Context& c, Problem& p, int64_t F0, int64_t
         tmax = std::max(tmax, t);
     }
     H->ttot = std::max<int64_t>(tmax, 1);
+    // the rows pass: items packed per operator, in chunks of RW_WARPS per cluster
+    for (int rc = 0; rc < H->nrc; ++rc)
+        require(H->rc_start[(size_t)rc + 1] - H->rc_start[(size_t)rc] <= RW_ROWS,
+                "H-matrix mixed form: leaf clusters of more than 64 unknowns");
+    H->nitems = (int64_t)H->item_blk.size();
+    std::vector<HmItem> items((size_t)(nops * H->nitems));
+    for (int64_t f = 0; f < nops; ++f)
+        for (int64_t it = 0; it < H->nitems; ++it) {
+            const int b = H->item_blk[(size_t)it];
+            const HmBlock& K = H->blocks[(size_t)b];
+            const size_t ob = (size_t)f * H->nb + b;
+            items[(size_t)(f * H->nitems + it)] =
+                HmItem{H->off[ob], K.adm ? H->toff[ob] : K.c0, (int32_t)K.m, K.adm ? H->rank[ob] : (int32_t)K.n,
+                       H->item_row[(size_t)it], K.adm};
+        }
+    // chunk c holds items ch_it[c] .. ch_it[c + 1] of one cluster (the
+    // clusters' item lists are contiguous, so a cluster's last chunk ends
+    // where the next cluster's first begins); a cluster without items still
+    // gets one empty chunk, so its rows are written
+    std::vector<int32_t> ch_rc, ch_it, rc_ch(1, 0);
+    for (int rc = 0; rc < H->nrc; ++rc) {
+        const int32_t i0 = H->rc_ptr[(size_t)rc], i1 = H->rc_ptr[(size_t)rc + 1];
+        int32_t c0 = i0;
+        do {
+            ch_rc.push_back(rc);
+            ch_it.push_back(c0);
+            c0 += RW_WARPS;
+        } while (c0 < i1);
+        rc_ch.push_back((int32_t)ch_rc.size());
+    }
+    ch_it.push_back((int32_t)H->nitems);
+    H->nchunks = (int64_t)ch_rc.size();
+    // the rank columns of every operator's admissible blocks, flat
+    std::vector<std::vector<HmProj>> proj((size_t)nops);
+    std::vector<int32_t> nproj((size_t)nops);
+    for (int64_t f = 0; f < nops; ++f) {
+        for (int b : H->adm_list) {
+            const HmBlock& K = H->blocks[(size_t)b];
+            const size_t ob = (size_t)f * H->nb + b;
+            const int r = H->rank[ob];
+            for (int k = 0; k < r; k += PJ_COLS)
+                proj[(size_t)f].push_back(HmProj{H->off[ob] + K.m * r + (int64_t)k * K.n, K.c0, H->toff[ob] + k,
+                                                 (int32_t)K.n, std::min(PJ_COLS, r - k)});
+        }
+        nproj[(size_t)f] = (int32_t)proj[(size_t)f].size();
+        H->pstride = std::max<int64_t>(H->pstride, (int64_t)proj[(size_t)f].size());
+    }
+    std::vector<HmProj> pflat((size_t)(nops * std::max<int64_t>(H->pstride, 1)));
+    for (int64_t f = 0; f < nops; ++f)
+        std::copy(proj[(size_t)f].begin(), proj[(size_t)f].end(), pflat.begin() + f * H->pstride);
+    upload(c, H->d_items, items);
+    upload(c, H->d_proj, pflat);
+    upload(c, H->d_nproj, nproj);
+    upload(c, H->d_chrc, ch_rc);
+    upload(c, H->d_chit, ch_it);
+    upload(c, H->d_rcch, rc_ch);
+    H->d_part.ensure(sizeof(float4) * (size_t)H->nsys * H->nchunks * RW_ROWS);
     upload(c, H->d_blk, H->blocks);
     upload(c, H->d_adm, H->adm_list);
     upload(c, H->d_off, H->off);
@@ -564,7 +757,7 @@ std::shared_ptr<HMixed> hmixed_build(Context& c, Problem& p, int64_t F0, int64_t
     upload(c, H->d_iblk, H->item_blk);
     upload(c, H->d_irow, H->item_row);
     H->d_x.ensure(sizeof(float2) * 2 * (size_t)H->nsys * n);
-    H->d_t.ensure(sizeof(double2) * (size_t)H->nsys * H->ttot);
+    H->d_t.ensure(sizeof(float4) * (size_t)H->nsys * H->ttot);
     c.sync();
     return H;
 }
