@@ -607,7 +607,7 @@ class _Shared:
         train = workloads.perturbed_spheres(self.wd, count=a.train_bodies, seed=1, nfreq=8, tri_lo=500, tri_hi=3000)
         tpds = [bem.PreData.from_dict(d, ctx=self.ctx) for d in train]
         t0 = time.perf_counter()
-        losses = bem.learned_train(tpds, steps=a.train_steps, nprobe=8, lr=1e-2, seed=5, ctx=self.ctx)
+        losses = bem.learned_train(tpds, steps=a.train_steps, nprobe=8, lr=3e-3, seed=5, ctx=self.ctx)
         self.training = {"bodies": len(train), "steps": a.train_steps, "seconds": time.perf_counter() - t0,
                          "loss_first": float(np.mean(losses[:10])), "loss_last": float(np.mean(losses[-10:]))}
         del tpds

@@ -20,6 +20,7 @@
 //    is always present, so an untrained (zero) correction is block-Jacobi.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -96,6 +97,9 @@ struct PcDev {
     // body, offset of each system's blocks in M (all nullptr: one body)
     const int32_t *sys_body, *body_leaf0;
     const size_t* sys_moff;
+    // learned form: per system, whether its correction is used (nullptr: all);
+    // block-Jacobi alone where the correction did not lower the probe residual
+    const int8_t* sys_off;
 };
 
 // Leaf index of the c-th leaf of system s's body, or -1 past its last leaf.
@@ -215,14 +219,17 @@ __global__ void __launch_bounds__(PC_LEAF) pc_apply_gmres_kernel(PcDev pc, GmBat
     const GmView g = gm_view(bt, s);
     const double2* q = bt.Q + g.q + (size_t)st.k * g.n;
     double2* z = bt.Z + g.q + (size_t)st.k * g.n;
-    pc_block_apply(c, pc.cl_off, pc.cl_idx, pc.nb_off, pc.nb_d, pc.nb_blk, pc.M + pc_moff(pc, s), q, z, pc.offdiag);
+    const int off = pc.offdiag && (!pc.sys_off || pc.sys_off[s]);
+    pc_block_apply(c, pc.cl_off, pc.cl_idx, pc.nb_off, pc.nb_d, pc.nb_blk, pc.M + pc_moff(pc, s), q, z, off);
 }
 
 // Probe form: Y[:, q] = M_s Z[:, q] for nprobe vectors (training).
 __global__ void __launch_bounds__(PC_LEAF) pc_apply_probes_kernel(PcDev pc, int s, const double2* __restrict__ Zp,
                                                                   double2* __restrict__ Yp, int64_t n) {
     const int q = blockIdx.y;
-    pc_block_apply(blockIdx.x, pc.cl_off, pc.cl_idx, pc.nb_off, pc.nb_d, pc.nb_blk, pc.M + pc_moff(pc, s),
+    const int c = pc_leaf(pc, s, blockIdx.x);
+    if (c < 0) return;
+    pc_block_apply(c, pc.cl_off, pc.cl_idx, pc.nb_off, pc.nb_d, pc.nb_blk, pc.M + pc_moff(pc, s),
                    Zp + (size_t)q * n, Yp + (size_t)q * n, pc.offdiag);
 }
 
@@ -593,8 +600,11 @@ struct PcData {
         d.sys_body = multi ? sys_body.as<int32_t>() : nullptr;
         d.body_leaf0 = multi ? body_leaf0.as<int32_t>() : nullptr;
         d.sys_moff = multi ? sys_moff.as<size_t>() : nullptr;
+        d.sys_off = gated ? sys_off.as<int8_t>() : nullptr;
         return d;
     }
+    DevBuf sys_off;
+    bool gated = false;
 };
 
 static void upload_pattern(Context& c, PcData& d) {
@@ -684,6 +694,62 @@ static void pc_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
     BEM_CHECK_LAUNCH(&c);
 }
 
+// Block-Jacobi is the learned form's fallback: for every system the learned
+// correction is kept only where it lowers the probe residual
+// E ||A M z - z||^2 / ||z||^2 (GATE_PROBES random probes, the same for both)
+// below GATE_KEEP times block-Jacobi's.  FP32 operators only (the refined
+// form's FP64 operators keep the correction).  Returns the systems kept.
+constexpr int GATE_PROBES = 2;
+constexpr double GATE_KEEP = 0.95;
+
+static int learned_gate(Context& c, PcData& d, GmWorkspace& ws, uint64_t seed) {
+    const int nsys = ws.bt.nsys;
+    if (!ws.fp32) return nsys;
+    int64_t nmax = 0;
+    for (int s = 0; s < nsys; ++s) nmax = std::max(nmax, ws.sys_host.empty() ? ws.bt.n : ws.sys_host[(size_t)s].n);
+    DevBuf Z, Y, W, R, acc;
+    for (DevBuf* v : {&Z, &Y, &W, &R}) v->ensure(sizeof(double2) * (size_t)nmax * GATE_PROBES);
+    acc.ensure(sizeof(double) * 4 * (size_t)nsys);
+    BEM_CUDA(cudaMemsetAsync(acc.p, 0, sizeof(double) * 4 * (size_t)nsys, c.stream));
+    const int nleaf = d.multi ? d.nc_max : d.pat.nc;
+    for (int s = 0; s < nsys; ++s) {
+        const int64_t n = ws.sys_host.empty() ? ws.bt.n : ws.sys_host[(size_t)s].n;
+        const int64_t lda = ws.sys_host.empty() ? ws.bt.lda : ws.sys_host[(size_t)s].lda;
+        const size_t aoff = ws.sys_host.empty() ? (size_t)s * ws.bt.mat_stride : ws.sys_host[(size_t)s].a_off;
+        const float2* As = static_cast<const float2*>(ws.bt.A) + aoff;
+        const int64_t tot = n * GATE_PROBES;
+        probes_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(tot, seed * 2654435761ull + (uint64_t)s,
+                                                                            Z.as<double2>());
+        BEM_CHECK_LAUNCH(&c);
+        for (int use = 0; use < 2; ++use) {
+            pc_apply_probes_kernel<<<dim3((unsigned)nleaf, (unsigned)GATE_PROBES), PC_LEAF, 0, c.stream>>>(
+                d.dev(use), s, Z.as<double2>(), Y.as<double2>(), n);
+            BEM_CHECK_LAUNCH(&c);
+            probe_matvec_kernel<<<dim3((unsigned)((n + 127) / 128), (unsigned)GATE_PROBES), 128, 0, c.stream>>>(
+                n, As, lda, Y.as<double2>(), W.as<double2>(), 0);
+            BEM_CHECK_LAUNCH(&c);
+            probe_residual_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(
+                tot, W.as<double2>(), Z.as<double2>(), R.as<double2>(), acc.as<double>() + 4 * (size_t)s + 2 * use);
+            BEM_CHECK_LAUNCH(&c);
+        }
+    }
+    std::vector<double> h(4 * (size_t)nsys);
+    BEM_CUDA(cudaMemcpyAsync(h.data(), acc.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    std::vector<int8_t> keep((size_t)nsys);
+    int kept = 0;
+    for (int s = 0; s < nsys; ++s) {
+        const double bj = h[4 * (size_t)s] / h[4 * (size_t)s + 1], ln = h[4 * (size_t)s + 2] / h[4 * (size_t)s + 3];
+        keep[(size_t)s] = (int8_t)(std::isfinite(ln) && ln < GATE_KEEP * bj);
+        kept += keep[(size_t)s];
+    }
+    d.sys_off.ensure(std::max<size_t>((size_t)nsys, 1));
+    BEM_CUDA(cudaMemcpyAsync(d.sys_off.p, keep.data(), (size_t)nsys, cudaMemcpyHostToDevice, c.stream));
+    c.sync();
+    d.gated = true;
+    return kept;
+}
+
 bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks) {
     if (kind == BEM_PRECOND_LU) {
         lu_precond_setup(c, ws);  // FP64 operators are factored from their FP32 rounding
@@ -707,6 +773,7 @@ bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond k
                             h->data.M.as<float2>() + (size_t)s * h->data.pat.entries);
         h->use_off = true;
         c.sync();
+        learned_gate(c, h->data, ws, 17);
     }
     ws.zb().ensure(sizeof(double2) * gm_q_total(ws));
     ws.bt.Z = ws.zb().as<double2>();
@@ -784,6 +851,7 @@ bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies,
             c.sync();  // the pair buffers are reused by the next body
         }
         h->use_off = true;
+        learned_gate(c, d, ws, 17);
     }
     c.sync();
     ws.zb().ensure(sizeof(double2) * gm_q_total(ws));
