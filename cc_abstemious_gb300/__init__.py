@@ -439,6 +439,48 @@ def run_batch(predatas, precond=None, check_vs_lu=False, max_operator_bytes=0, c
     return results
 
 
+def cluster_tree(point_sets, leaf, eta=None, ctx=None):
+    """Cluster trees (cluster.rs:35-105) of one or several point sets and,
+    with eta, their block trees (block.rs:38-93), built on the device in one
+    pass.  point_sets: an (n, >= 3) array or a list of them.  Per set returns
+    dict(perm, leaves [(begin, end)], blocks [(row begin, row end, column
+    begin, column end, admissible)], root_diameter); a cluster's points are
+    perm[begin:end], and leaves and blocks are in the reference's depth-first
+    order."""
+    ctx = ctx or Context.default()
+    single = isinstance(point_sets, np.ndarray)
+    sets = [np.ascontiguousarray(point_sets if single else p, dtype=np.float64) for p in
+            ([point_sets] if single else point_sets)]
+    stride = sets[0].shape[1]
+    if any(p.ndim != 2 or p.shape[1] != stride or stride < 3 for p in sets):
+        raise ValueError("point sets must be (n, k) arrays with one k >= 3")
+    npts = np.array([len(p) for p in sets], dtype=np.int64)
+    pts = np.concatenate(sets) if npts.sum() else np.zeros((1, stride))
+    perm = np.zeros(max(int(npts.sum()), 1), dtype=np.int64)
+    diam = np.zeros(len(sets))
+    nl, nb = C.c_int64(), C.c_int64()
+    e = -1.0 if eta is None else float(eta)
+    lcap, bcap = max(int(npts.sum()), 1), 4 * max(int(npts.sum()), 1)
+    while True:
+        leaves = np.zeros((lcap, 3), dtype=np.int64)
+        blocks = np.zeros((bcap, 6), dtype=np.int64)
+        st = ctx.lib.bem_cluster_tree(ctx.h, len(sets), _ptr(npts), _ptr(pts), stride, int(leaf), e, _ptr(perm),
+                                      _ptr(leaves), lcap, C.byref(nl), _ptr(blocks), bcap, C.byref(nb), _ptr(diam))
+        if st != 0 and (nl.value > lcap or nb.value > bcap):
+            lcap, bcap = max(lcap, nl.value), max(bcap, nb.value)
+            continue
+        ctx.check(st)
+        break
+    leaves, blocks = leaves[:nl.value], blocks[:nb.value]
+    out, p0 = [], 0
+    for s, n in enumerate(npts):
+        lv = leaves[leaves[:, 0] == s][:, 1:]
+        bk = blocks[blocks[:, 0] == s][:, 1:]
+        out.append(dict(perm=perm[p0:p0 + n].copy(), leaves=lv, blocks=bk, root_diameter=float(diam[s])))
+        p0 += n
+    return out[0] if single else out
+
+
 class HMatrix:
     """h_matrix.rs:110-247 over a problem's collocation points."""
 

@@ -17,8 +17,10 @@ LIB = os.path.join(HERE, "libbem_gb300.so")
 CLI = os.path.join(HERE, "bem")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
+# host code without fused multiply-adds, so that it gives the same results on
+# x86-64 and aarch64 (gcc contracts a * b + c by default where FMA is baseline)
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-          "-I", os.path.join(ROOT, "include")]
+          "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(ROOT, "include")]
 
 
 def sources():

@@ -1,8 +1,7 @@
 // Hierarchical matrices (h_matrix.rs, aca.rs, cluster.rs, block.rs).
 //
-// Host C++: the geometric cluster tree and the block tree with its flattened
-// leaf list (tree construction is set-up work, as in the reference).
-// Device: every leaf block is filled in one batched pass -- inadmissible
+// Device: the geometric cluster tree and the block tree with its flattened
+// leaf list (tree.cu), then every leaf block is filled in one batched pass -- inadmissible
 // leaves as dense FP64 blocks, admissible leaves by adaptive cross
 // approximation (one CTA per leaf running the reference's partially pivoted
 // ACA with the rand 0.9 StdRng pivot stream restated below), followed by the
@@ -21,6 +20,7 @@
 #include "hmatrix.cuh"
 #include "kernels.cuh"
 #include "mixed.cuh"
+#include "tree.cuh"
 
 struct bem_hmatrix {
     bem::HMatrixDev* h;
@@ -28,109 +28,6 @@ struct bem_hmatrix {
 };
 
 namespace bem {
-
-// ---------------------------------------------------------------------------
-// Host: cluster tree (cluster.rs:35-105) and block tree (block.rs:38-96).
-namespace {
-struct ClNode {
-    double lo[3], hi[3], diam;
-    std::vector<int64_t> idx;
-    std::unique_ptr<ClNode> son[2];
-    bool leaf() const { return !son[0]; }
-};
-
-std::unique_ptr<ClNode> build_cluster(const std::vector<double>& pts, int64_t stride, std::vector<int64_t> idx,
-                                      int64_t leaf, int depth) {
-    auto c = std::make_unique<ClNode>();
-    for (int d = 0; d < 3; ++d) {
-        c->lo[d] = INFINITY;
-        c->hi[d] = -INFINITY;
-    }
-    for (int64_t i : idx)
-        for (int d = 0; d < 3; ++d) {
-            double v = pts[(size_t)(stride * i + d)];
-            c->lo[d] = std::fmin(v, c->lo[d]);
-            c->hi[d] = std::fmax(v, c->hi[d]);
-        }
-    double s = 0;
-    for (int d = 0; d < 3; ++d) s += (c->hi[d] - c->lo[d]) * (c->hi[d] - c->lo[d]);
-    c->diam = std::sqrt(s);
-    c->idx = std::move(idx);
-    if ((int64_t)c->idx.size() <= leaf) return c;
-    require(depth < 200, "cluster tree: points cannot be separated (coincident collocation points)");
-    int jmax = 0;
-    double diff = 0;
-    for (int d = 0; d < 3; ++d) {
-        double e = c->hi[d] - c->lo[d];
-        if (e > diff) { jmax = d; diff = e; }
-    }
-    double gamma = 0.5 * (c->lo[jmax] + c->hi[jmax]);
-    std::vector<int64_t> a, b;
-    for (int64_t i : c->idx) (pts[(size_t)(stride * i + jmax)] <= gamma ? a : b).push_back(i);
-    require(!a.empty() && !b.empty(), "cluster tree: points cannot be separated (coincident collocation points)");
-    c->son[0] = build_cluster(pts, stride, std::move(a), leaf, depth + 1);
-    c->son[1] = build_cluster(pts, stride, std::move(b), leaf, depth + 1);
-    return c;
-}
-
-double cluster_dist(const ClNode& a, const ClNode& b) {
-    double s = 0;
-    for (int d = 0; d < 3; ++d) {
-        double t1 = std::fmax(0.0, a.lo[d] - b.hi[d]);
-        double t2 = std::fmax(0.0, b.lo[d] - a.hi[d]);
-        s += t1 * t1;
-        s += t2 * t2;
-    }
-    return std::sqrt(s);
-}
-
-void block_leaves(const ClNode& r, const ClNode& c, double eta,
-                  std::vector<std::tuple<const ClNode*, const ClNode*, int>>& out) {
-    int adm = std::fmin(r.diam, c.diam) <= eta * cluster_dist(r, c);
-    if (adm || r.leaf() || c.leaf()) {
-        out.emplace_back(&r, &c, adm);
-        return;
-    }
-    for (int a = 0; a < 2; ++a)
-        for (int b = 0; b < 2; ++b) block_leaves(*r.son[a], *c.son[b], eta, out);
-}
-}  // namespace
-
-static void collect_leaves(const ClNode& c, std::vector<LeafCluster>& out) {
-    if (c.leaf()) {
-        LeafCluster l;
-        l.idx = c.idx;
-        for (int d = 0; d < 3; ++d) {
-            l.lo[d] = c.lo[d];
-            l.hi[d] = c.hi[d];
-        }
-        l.diam = c.diam;
-        out.push_back(std::move(l));
-        return;
-    }
-    collect_leaves(*c.son[0], out);
-    collect_leaves(*c.son[1], out);
-}
-
-std::vector<LeafCluster> cluster_leaves(const std::vector<double>& pts, int64_t stride, int64_t leaf) {
-    const int64_t n = (int64_t)pts.size() / stride;
-    std::vector<int64_t> idx((size_t)n);
-    for (int64_t i = 0; i < n; ++i) idx[(size_t)i] = i;
-    auto root = build_cluster(pts, stride, idx, leaf, 0);
-    std::vector<LeafCluster> out;
-    collect_leaves(*root, out);
-    return out;
-}
-
-double box_distance(const LeafCluster& a, const LeafCluster& b) {
-    double s = 0;
-    for (int d = 0; d < 3; ++d) {
-        double t1 = std::fmax(0.0, a.lo[d] - b.hi[d]);
-        double t2 = std::fmax(0.0, b.lo[d] - a.hi[d]);
-        s += t1 * t1 + t2 * t2;
-    }
-    return std::sqrt(s);
-}
 
 // Leaf descriptor shared with the kernels.
 struct HLeaf {
@@ -869,19 +766,17 @@ static GenParams gen_params(const Problem& p, int side) {
 constexpr int ACA_RMAX = 256;  // also the size of the ACA kernel's s_prod
 
 // The cluster tree and block leaves of a problem's collocation points (they
-// depend on the geometry, the leaf size and eta only, not on the frequency).
+// depend on the geometry, the leaf size and eta only, not on the frequency),
+// built on the device.
 struct HTrees {
-    std::unique_ptr<ClNode> root;
-    std::vector<std::tuple<const ClNode*, const ClNode*, int>> bl;
+    std::shared_ptr<Forest> F;
+    std::vector<BlockLeaf> bl;
 };
 
-static std::shared_ptr<HTrees> build_trees(const Problem& p) {
+static std::shared_ptr<HTrees> build_trees(Context& c, const Problem& p) {
     auto T = std::make_shared<HTrees>();
-    const int64_t n = p.n;
-    std::vector<int64_t> idx((size_t)n);
-    for (int64_t i = 0; i < n; ++i) idx[(size_t)i] = i;
-    T->root = build_cluster(p.cpts, 8, idx, p.in.hm_leaf, 0);
-    block_leaves(*T->root, *T->root, p.in.hm_eta, T->bl);
+    T->F = build_forest(c, std::vector<const Problem*>{&p}, p.in.hm_leaf);
+    T->bl = forest_block_leaves(c, *T->F, p.in.hm_eta);
     return T;
 }
 
@@ -892,20 +787,22 @@ std::unique_ptr<HMatrixDev> hmatrix_build(Context& c, const Problem& p, int side
     auto H = std::make_unique<HMatrixDev>();
     const int64_t n = p.n;
     H->n = n;
-    if (!trees) trees = build_trees(p);
-    const auto& bl = trees->bl;
+    if (!trees) trees = build_trees(c, p);
+    const Forest& F = *trees->F;
+    // every cluster is a range of the cluster-order permutation, so the row
+    // and column lists of all leaves are that one array
+    H->rows = F.perm;
+    H->cols = F.perm;
     int64_t store = 0, scratch = 0, yoff = 0;
-    for (auto& t : bl) {
-        const ClNode* r = std::get<0>(t);
-        const ClNode* cc = std::get<1>(t);
+    for (const BlockLeaf& t : trees->bl) {
+        const TreeNode& r = F.nodes[(size_t)t.r];
+        const TreeNode& cc = F.nodes[(size_t)t.c];
         HLeaf L{};
-        L.row_off = (int64_t)H->rows.size();
-        L.m = (int64_t)r->idx.size();
-        H->rows.insert(H->rows.end(), r->idx.begin(), r->idx.end());
-        L.col_off = (int64_t)H->cols.size();
-        L.n = (int64_t)cc->idx.size();
-        H->cols.insert(H->cols.end(), cc->idx.begin(), cc->idx.end());
-        L.adm = std::get<2>(t);
+        L.row_off = r.begin;
+        L.m = r.end - r.begin;
+        L.col_off = cc.begin;
+        L.n = cc.end - cc.begin;
+        L.adm = t.adm;
         L.store_off = store;
         L.y_off = yoff;
         yoff += L.m;
@@ -923,15 +820,15 @@ std::unique_ptr<HMatrixDev> hmatrix_build(Context& c, const Problem& p, int side
     // device copies
     const size_t nl = H->leaves.size();
     H->d_leaves.ensure(sizeof(HLeaf) * nl);
-    H->d_rows.ensure(sizeof(int64_t) * H->rows.size());
-    H->d_cols.ensure(sizeof(int64_t) * H->cols.size());
+    H->d_rows.ensure(sizeof(int64_t) * std::max<size_t>(H->rows.size(), 1));
+    H->d_cols.ensure(sizeof(int64_t) * std::max<size_t>(H->cols.size(), 1));
     H->d_store.ensure(sizeof(double2) * (size_t)std::max<int64_t>(store, 1));
     H->d_scratch.ensure(sizeof(double2) * (size_t)std::max<int64_t>(scratch, 1));
     H->d_y.ensure(sizeof(double2) * (size_t)std::max<int64_t>(yoff, 1));
     BEM_CUDA(cudaMemcpyAsync(H->d_leaves.p, H->leaves.data(), sizeof(HLeaf) * nl, cudaMemcpyHostToDevice, c.stream));
-    BEM_CUDA(cudaMemcpyAsync(H->d_rows.p, H->rows.data(), sizeof(int64_t) * H->rows.size(), cudaMemcpyHostToDevice,
+    BEM_CUDA(cudaMemcpyAsync(H->d_rows.p, F.d_perm.p, sizeof(int64_t) * H->rows.size(), cudaMemcpyDeviceToDevice,
                              c.stream));
-    BEM_CUDA(cudaMemcpyAsync(H->d_cols.p, H->cols.data(), sizeof(int64_t) * H->cols.size(), cudaMemcpyHostToDevice,
+    BEM_CUDA(cudaMemcpyAsync(H->d_cols.p, F.d_perm.p, sizeof(int64_t) * H->cols.size(), cudaMemcpyDeviceToDevice,
                              c.stream));
     std::vector<int32_t> adm_list, dense_list;
     for (size_t b = 0; b < nl; ++b) (H->leaves[b].adm ? adm_list : dense_list).push_back((int32_t)b);
@@ -1030,7 +927,7 @@ HBuilt hmatrix_build_view(Context& c, const Problem& p, int side, std::shared_pt
     std::shared_ptr<HTrees> trees;
     if (tree_cache && *tree_cache) trees = std::static_pointer_cast<HTrees>(*tree_cache);
     if (!trees) {
-        trees = build_trees(p);
+        trees = build_trees(c, p);
         if (tree_cache) *tree_cache = trees;
     }
     std::shared_ptr<HMatrixDev> H(hmatrix_build(c, p, side, trees).release());
@@ -1047,6 +944,16 @@ HBuilt hmatrix_build_view(Context& c, const Problem& p, int side, std::shared_pt
     v.d_store = H->d_store.as<double2>();
     v.keep = H;
     return v;
+}
+
+std::shared_ptr<const Forest> hmatrix_forest(Context& c, const Problem& p, std::shared_ptr<void>* tree_cache) {
+    std::shared_ptr<HTrees> trees;
+    if (tree_cache && *tree_cache) trees = std::static_pointer_cast<HTrees>(*tree_cache);
+    if (!trees) {
+        trees = build_trees(c, p);
+        if (tree_cache) *tree_cache = trees;
+    }
+    return trees->F;
 }
 
 // out = (alpha H + beta G) 1 with the FP64 H-matrix of `side`

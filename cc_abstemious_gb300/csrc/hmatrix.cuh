@@ -8,13 +8,7 @@ namespace bem {
 
 struct HMatrixDev;
 
-// Leaves of the cluster tree of cluster.rs:35-105 (bounding-box bisection).
-struct LeafCluster {
-    std::vector<int64_t> idx;
-    double lo[3], hi[3], diam;
-};
-std::vector<LeafCluster> cluster_leaves(const std::vector<double>& pts, int64_t stride, int64_t leaf);
-double box_distance(const LeafCluster& a, const LeafCluster& b);
+struct Forest;
 
 void solve_surface_hmatrix(Context& c, const Problem& p, const double2* d_rhs_inc, double2* d_phi, double2* d_vn,
                            bem_solve_report* rep);
@@ -43,6 +37,9 @@ struct HBuilt {
 // tree_cache (may be null): holds the problem's cluster / block trees between
 // calls for several frequencies of one body (built on the first call).
 HBuilt hmatrix_build_view(Context& c, const Problem& p, int side, std::shared_ptr<void>* tree_cache = nullptr);
+// The problem's cluster tree at its H-matrix leaf size (cluster.rs:35-105,
+// built on the device), through the same cache as hmatrix_build_view.
+std::shared_ptr<const Forest> hmatrix_forest(Context& c, const Problem& p, std::shared_ptr<void>* tree_cache);
 // out = H 1 (n entries, device) for the H-matrix of `side`.
 void hmatrix_row_sums(Context& c, const Problem& p, int side, double2* out);
 

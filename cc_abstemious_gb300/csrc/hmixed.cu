@@ -38,6 +38,7 @@
 #include "complex.cuh"
 #include "gmres.cuh"
 #include "hmatrix.cuh"
+#include "tree.cuh"
 #include "hmixed.cuh"
 
 namespace bem {
@@ -573,16 +574,16 @@ std::shared_ptr<HMixed> hmixed_build(Context& c, Problem& p, int64_t F0, int64_t
     H->nops = (int)nops;
     H->R = R;
     H->nsys = (int)(nops * R);
-    // cluster order: the leaves of the tree in depth-first order
-    auto leaves = cluster_leaves(p.cpts, 8, p.in.hm_leaf);
-    H->perm.reserve((size_t)n);
+    // cluster order: the leaves of the tree in depth-first order (built once,
+    // shared by every frequency)
+    std::shared_ptr<void> trees;
+    auto F = hmatrix_forest(c, p, &trees);
+    H->perm = F->perm;
     H->rc_start.push_back(0);
-    for (auto& l : leaves) {
-        H->perm.insert(H->perm.end(), l.idx.begin(), l.idx.end());
-        H->rc_start.push_back((int64_t)H->perm.size());
-    }
-    require((int64_t)H->perm.size() == n, "H-matrix: cluster leaves do not cover the unknowns");
-    H->nrc = (int)leaves.size();
+    for (int32_t v : F->leaves) H->rc_start.push_back(F->nodes[(size_t)v].end);
+    require((int64_t)H->perm.size() == n && H->rc_start.back() == n,
+            "H-matrix: cluster leaves do not cover the unknowns");
+    H->nrc = (int)F->leaves.size();
     H->pos.assign((size_t)n, 0);
     for (int64_t q = 0; q < n; ++q) H->pos[(size_t)H->perm[(size_t)q]] = q;
     DevBuf d_pos;
@@ -590,7 +591,6 @@ std::shared_ptr<HMixed> hmixed_build(Context& c, Problem& p, int64_t F0, int64_t
     upload(c, H->d_perm, H->perm);
     const int64_t saved = p.ifreq;
     size_t store_total = 0;
-    std::shared_ptr<void> trees;  // built once, shared by every frequency
     for (int64_t f = 0; f < nops; ++f) {
         p.ifreq = F0 + f;
         HBuilt B = hmatrix_build_view(c, p, 1, &trees);

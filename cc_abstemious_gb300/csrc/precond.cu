@@ -31,6 +31,7 @@
 #include "gmres.cuh"
 #include "hmatrix.cuh"
 #include "precond.cuh"
+#include "tree.cuh"
 
 namespace bem {
 
@@ -38,17 +39,26 @@ constexpr int PC_LEAF = 64;
 constexpr double PC_ETA = 2.0;
 
 // ---------------------------------------------------------------------------
-// Near-field leaf pattern (host).
-void build_pattern(const Problem& p, NearPattern& P, bool diag_only) {
-    auto leaves = cluster_leaves(p.cpts, 8, PC_LEAF);
-    P.n = p.n;
+// Near-field leaf patterns: the cluster trees of all bodies in one device
+// pass, then per body its leaves and their near neighbours.
+void build_patterns(Context& c, const std::vector<const Problem*>& bodies, std::vector<NearPattern>& pats,
+                    bool diag_only) {
+    auto F = build_forest(c, bodies, PC_LEAF);
+    pats.resize(bodies.size());
+    for (size_t b = 0; b < bodies.size(); ++b)
+        near_pattern(*F, (int)b, pats[b], diag_only);
+}
+
+void near_pattern(const Forest& F, int body, NearPattern& P, bool diag_only) {
+    const int l0 = F.leaf0[(size_t)body], l1 = F.leaf0[(size_t)body + 1];
+    std::vector<const TreeNode*> leaves;
+    for (int l = l0; l < l1; ++l) leaves.push_back(&F.nodes[(size_t)F.leaves[(size_t)l]]);
+    P.n = F.n(body);
     P.nc = (int)leaves.size();
+    // the leaves are consecutive ranges of the body's cluster order
+    P.cl_idx.assign(F.perm.begin() + F.pt0[(size_t)body], F.perm.begin() + F.pt0[(size_t)body + 1]);
     P.cl_off.assign(1, 0);
-    P.cl_idx.clear();
-    for (auto& l : leaves) {
-        P.cl_idx.insert(P.cl_idx.end(), l.idx.begin(), l.idx.end());
-        P.cl_off.push_back((int64_t)P.cl_idx.size());
-    }
+    for (const TreeNode* l : leaves) P.cl_off.push_back(l->end);
     P.nb_off.assign(1, 0);
     P.nb_d.clear();
     P.nb_blk.clear();
@@ -60,7 +70,7 @@ void build_pattern(const Problem& p, NearPattern& P, bool diag_only) {
         std::vector<int> near{c};
         for (int d = 0; d < P.nc && !diag_only; ++d) {
             if (d == c) continue;
-            bool adm = std::fmin(leaves[c].diam, leaves[d].diam) <= PC_ETA * box_distance(leaves[c], leaves[d]);
+            bool adm = std::fmin(leaves[c]->diam, leaves[d]->diam) <= PC_ETA * node_distance(*leaves[c], *leaves[d]);
             if (!adm) near.push_back(d);
         }
         const int64_t bc = P.cl_off[c + 1] - P.cl_off[c];
@@ -630,15 +640,20 @@ static void diag_inverses(Context& c, PcData& d, int nsys, const void* A, bool f
     for (int cc = 0; cc < d.pat.nc; ++cc)
         bmax = std::max(bmax, (int)(d.pat.cl_off[cc + 1] - d.pat.cl_off[cc]));
     size_t smem = sizeof(float2) * (size_t)bmax * 2 * bmax;
+    // the attribute is set to the cap for leaf clusters of PC_LEAF points on
+    // every call (the same value from every thread; a per-call value could
+    // lower it under a concurrent larger launch)
+    const int smem_cap = (int)(sizeof(float2) * PC_LEAF * 2 * PC_LEAF);
+    require(smem <= (size_t)smem_cap, "block-Jacobi: leaf cluster larger than the leaf size", BEM_ERR_CUDA);
     dim3 grid((unsigned)(d.multi ? d.nc_max : d.pat.nc), (unsigned)nsys);
     if (fp32) {
         BEM_CUDA(cudaFuncSetAttribute(pc_diag_inverse_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+                                      smem_cap));
         pc_diag_inverse_kernel<float2><<<grid, 256, smem, c.stream>>>(static_cast<const float2*>(A), lda, mstride,
                                                                       sys, d.dev(0), d.M.as<float2>());
     } else {
         BEM_CUDA(cudaFuncSetAttribute(pc_diag_inverse_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+                                      smem_cap));
         pc_diag_inverse_kernel<double2><<<grid, 256, smem, c.stream>>>(static_cast<const double2*>(A), lda, mstride,
                                                                        sys, d.dev(0), d.M.as<float2>());
     }
@@ -760,7 +775,11 @@ bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond k
     if (kind == BEM_PRECOND_LEARNED && !(c.net && c.net->ready)) kind = BEM_PRECOND_BLOCK_JACOBI;
     auto h = std::make_shared<PcHookData>();
     // block-Jacobi needs the diagonal blocks only
-    build_pattern(p, h->data.pat, kind != BEM_PRECOND_LEARNED);
+    {
+        std::vector<NearPattern> pats;
+        build_patterns(c, std::vector<const Problem*>{&p}, pats, kind != BEM_PRECOND_LEARNED);
+        h->data.pat = std::move(pats[0]);
+    }
     upload_pattern(c, h->data);
     const int nsys = ws.bt.nsys;
     diag_inverses(c, h->data, nsys, ws.bt.A, ws.fp32, ws.bt.lda, ws.bt.mat_stride, ws.bt.sys);
@@ -799,13 +818,13 @@ bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies,
     auto h = std::make_shared<PcHookData>();
     PcData& d = h->data;
     const int nb = (int)bodies.size(), nsys = ws.bt.nsys;
-    std::vector<NearPattern> pats((size_t)nb);
+    std::vector<NearPattern> pats;
+    build_patterns(c, std::vector<const Problem*>(bodies.begin(), bodies.end()), pats, !learned);
     std::vector<int32_t> leaf0(1, 0);
     NearPattern& P = d.pat;
     P.cl_off.assign(1, 0);
     P.nb_off.assign(1, 0);
     for (int b = 0; b < nb; ++b) {
-        build_pattern(*bodies[(size_t)b], pats[(size_t)b], !learned);
         const NearPattern& q = pats[(size_t)b];
         const int64_t idx0 = (int64_t)P.cl_idx.size();
         const int32_t nb0 = (int32_t)P.nb_d.size();
@@ -885,10 +904,12 @@ double learned_train(Context& c, std::vector<Problem*>& probs, int steps, int np
         std::vector<double> ks;
     };
     std::vector<std::unique_ptr<Body>> bodies;
+    std::vector<NearPattern> pats;
+    build_patterns(c, std::vector<const Problem*>(probs.begin(), probs.end()), pats, false);
     for (Problem* p : probs) {
         auto b = std::make_unique<Body>();
         b->p = p;
-        build_pattern(*p, b->pc.pat);
+        b->pc.pat = std::move(pats[bodies.size()]);
         upload_pattern(c, b->pc);
         upload_pairs(c, b->pc.pat, b->pb);
         b->nf = (int)p->freqs.size();

@@ -33,9 +33,14 @@ struct LearnedNet {
 };
 
 int learned_num_params();
-// Leaves of p's cluster tree and their near neighbours (diag_only: each leaf
-// with itself only, the block-Jacobi pattern).
-void build_pattern(const Problem& p, NearPattern& P, bool diag_only = false);
+struct Forest;
+// Leaves of the bodies' cluster trees (leaf size 64, built on the device) and
+// their near neighbours (diag_only: each leaf with itself only, the
+// block-Jacobi pattern); pats[b] belongs to bodies[b].
+void build_patterns(Context& c, const std::vector<const Problem*>& bodies, std::vector<NearPattern>& pats,
+                    bool diag_only);
+// The pattern of one body of a forest built at leaf size 64.
+void near_pattern(const Forest& F, int body, NearPattern& P, bool diag_only);
 // Installs the preconditioner on the batch; returns the kind actually used
 // (the learned form falls back to block-Jacobi when no network is available).
 bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks);

@@ -343,6 +343,28 @@ BEM_API bem_status bem_lu32_factor_apply(bem_ctx* ctx, int nsys, const int64_t* 
                                          float* D, int64_t d_entries, const bem_cplx* q, bem_cplx* z,
                                          int* small_pivots);
 
+/* ---- Cluster and block trees (cluster.rs:35-105, block.rs:38-93) ------- */
+/* Cluster::new_from (cluster.rs:23-31) and BlockList::new_from over
+ * BlockTree::new_from (block.rs:20-28, :76-93) for nsets point sets at once,
+ * built on the device.  Set s has npts[s] points, `stride` doubles per point
+ * (x y z first), the sets back to back in pts (host memory).
+ *   perm (sum of npts entries): each set's point indices (0-based within the
+ *     set) in cluster order, the sets back to back;
+ *   leaves (3 per leaf: set, begin, end): the leaf clusters depth-first, each
+ *     the range begin .. end - 1 of its set's part of perm;
+ *   blocks (6 per block: set, row begin, row end, column begin, column end,
+ *     admissible): the block-tree leaves in the reference's flattening order
+ *     (eta < 0: no block tree, *nblocks = 0);
+ *   root_diam (nsets entries, may be NULL): each root's box diagonal.
+ * *nleaves and *nblocks receive the counts; when one exceeds its capacity the
+ * call returns BEM_ERR_BAD_INPUT without writing leaves and blocks, and the
+ * caller may retry with the counts.  Coincident points that cannot be
+ * separated are BEM_ERR_BAD_INPUT (the reference recurses without end). */
+BEM_API bem_status bem_cluster_tree(bem_ctx* ctx, int nsets, const int64_t* npts, const double* pts, int64_t stride,
+                                    int64_t leaf, double eta, int64_t* perm, int64_t* leaves, int64_t leaf_cap,
+                                    int64_t* nleaves, int64_t* blocks, int64_t block_cap, int64_t* nblocks,
+                                    double* root_diam);
+
 /* ---- H-matrix (h_matrix.rs, aca.rs, cluster.rs, block.rs) -------------- */
 /* h_matrix.rs:127-148 HMatrix::new_from over the problem's collocation points
  * for the given side (leaf, eta and ACA tolerance from the problem). */
