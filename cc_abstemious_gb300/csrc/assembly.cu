@@ -154,10 +154,25 @@ struct Asm64Params {
     Sys64 s[MAX_SYS64];
 };
 
+// Stores entry a of system s at column-major offset o: as a double2 (plane =
+// 0; systems mat_stride entries apart), or split (plane = the FP32 matrix's
+// size): the FP32 rounding hi at float2 offset o and the rounding of the
+// exact remainder a - hi a plane further on (systems mat_stride float2 apart).
+__device__ __forceinline__ void store_a64(double2* A, size_t plane, size_t o, double2 a) {
+    if (!plane) {
+        A[o] = a;
+        return;
+    }
+    float2* F = reinterpret_cast<float2*>(A);
+    const float hx = __double2float_rn(a.x), hy = __double2float_rn(a.y);
+    F[o] = make_float2(hx, hy);
+    F[o + plane] = make_float2(__double2float_rn(a.x - (double)hx), __double2float_rn(a.y - (double)hy));
+}
+
 __global__ void __launch_bounds__(ASM_THREADS) assemble64_multi_kernel(int64_t n, int64_t npad,
                                                                       const double* __restrict__ geo,
                                                                       Asm64Params prm, double2* __restrict__ A,
-                                                                      int64_t ld, size_t mat_stride,
+                                                                      int64_t ld, size_t mat_stride, size_t plane,
                                                                       double* __restrict__ norm_part,
                                                                       int* __restrict__ err) {
     __shared__ __align__(128) TileGeo64 t;
@@ -181,7 +196,7 @@ __global__ void __launch_bounds__(ASM_THREADS) assemble64_multi_kernel(int64_t n
         const int jj = ty + 4 * c;
         const int64_t j = J0 + jj;
         if (i >= n || j >= n) continue;
-        double2* Aij = A + j * ld + i;
+        const size_t oij = (size_t)(j * ld + i);
         if (i == j) {
 #pragma unroll
             for (int s = 0; s < MAX_SYS64; ++s) {
@@ -190,7 +205,7 @@ __global__ void __launch_bounds__(ASM_THREADS) assemble64_multi_kernel(int64_t n
                 self_term64(t.carea[jj], t.cwt[jj], prm.bm, prm.s[s].beta_im, prm.hdiag, prm.s[s].gdiag_im, g, h);
                 z2 a = cmul(prm.s[s].alpha, h);
                 cfma(a, prm.s[s].beta, g);
-                Aij[s * mat_stride] = a;
+                store_a64(A, plane, s * mat_stride + oij, a);
                 nrm[s] += a.x * a.x + a.y * a.y;
             }
             continue;
@@ -234,7 +249,7 @@ __global__ void __launch_bounds__(ASM_THREADS) assemble64_multi_kernel(int64_t n
             }
             z2 a = cmul(prm.s[s].alpha, h);
             cfma(a, prm.s[s].beta, g);
-            Aij[s * mat_stride] = a;
+            store_a64(A, plane, s * mat_stride + oij, a);
             nrm[s] += a.x * a.x + a.y * a.y;
         }
     }
@@ -256,7 +271,12 @@ __global__ void __launch_bounds__(ASM_THREADS) assemble64_multi_kernel(int64_t n
 
 void assemble_system_fp64_multi(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
                                 const cd* betas, int nsys, double2* A, int64_t ld, size_t mat_stride,
-                                double* norms) {
+                                double* norms, bool split) {
+    // split: the systems' planes are ld * n float2 each, systems 2 ld n float2
+    // apart (the bytes of one double2 matrix)
+    const size_t plane = split ? (size_t)ld * p.n : 0;
+    const size_t stride = split ? 2 * plane : mat_stride;
+    require(!split || mat_stride == plane, "split FP64 assembly: systems must be ld * n entries apart");
     int* err = device_err(ctx);
     BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx.stream));
     const int ntiles = (int)(p.geo.npad / TILE);
@@ -286,9 +306,11 @@ void assemble_system_fp64_multi(Context& ctx, const Problem& p, const double* ks
         for (int s = 0; s < prm.nsys && prm.recur; ++s)
             if (std::fabs(ks[s0 + s] - (prm.k0 + s * prm.dk)) > 1e-13 * kmax) prm.recur = 0;
         dim3 grid((unsigned)ntiles, (unsigned)ntiles);
-        assemble64_multi_kernel<<<grid, ASM_THREADS, 0, ctx.stream>>>(p.n, p.geo.npad, p.geo.arr(0), prm,
-                                                                      A + (size_t)s0 * mat_stride, ld, mat_stride,
-                                                                      ctx.w_norm.as<double>(), err);
+        // system s0 starts s0 * stride entries of the store's type in
+        double2* A0 = split ? reinterpret_cast<double2*>(reinterpret_cast<float2*>(A) + (size_t)s0 * stride)
+                            : A + (size_t)s0 * stride;
+        assemble64_multi_kernel<<<grid, ASM_THREADS, 0, ctx.stream>>>(p.n, p.geo.npad, p.geo.arr(0), prm, A0, ld,
+                                                                      stride, plane, ctx.w_norm.as<double>(), err);
         BEM_CHECK_LAUNCH(&ctx);
         finish_norms(ctx, ctx.w_norm.as<double>(), nparts, prm.nsys, norms + s0);
     }

@@ -250,9 +250,12 @@ void assemble_system_fp64(Context& ctx, const Problem& p, double2* A, int64_t ld
 // A_s = alpha_s H_s + beta_s G_s in FP64 for several frequencies (refined
 // form): geometry once per pair, e^{ik r} by recurrence when the wavenumbers
 // are evenly spaced; norms[s] = ||A_s||_F.
+// split: each operator stored as its FP32 rounding (float2, ld * n entries)
+// followed by the FP32 rounding of the remainder (the same size), operators
+// 2 ld n float2 apart (mat_stride must be ld * n).
 void assemble_system_fp64_multi(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
                                 const cd* betas, int nsys, double2* A, int64_t ld, size_t mat_stride,
-                                double* norms);
+                                double* norms, bool split = false);
 void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
                                const cd* betas, const cd* gammas, const cd* deltas, int nsys, float2* A,
                                int64_t ld, size_t mat_stride, double2* rowsum, size_t vec_stride, double* norms);

@@ -66,6 +66,10 @@ __device__ __forceinline__ void ff_acc(float& hi, float& lo, float a, float b) {
 //  FAST  (Krylov vectors, Q): FP32 sums of 8 columns folded into a float-float
 //        accumulator; ~1e-7 relative, which only perturbs the Krylov basis:
 //        the exact residual at each check and restart keeps the answer exact.
+// Split FP64 operators (EXACT == 2, every mode): the EXACT scheme over the
+// FP32 matrix plus the products of its remainder plane with x's hi part, so
+// the mat-vec carries the FP64 operator to ~2^-44 on the FP32 pipe (GB300's
+// FP64 rate is 1/64 of it) while streaming the same 16 B per entry.
 constexpr int MV_UNROLL = 8;
 
 template <typename T, int EXACT, int U = MV_UNROLL>
@@ -127,7 +131,7 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
             // float-float accumulators for (re0, im0, re1, im1)
             float h0 = 0, l0 = 0, h1 = 0, l1 = 0, h2 = 0, l2 = 0, h3 = 0, l3 = 0;
             for (int q0 = 0; q0 < jn; q0 += U) {
-                float4 a[U];
+                float4 a[U], z[EXACT == 2 ? U : 1];
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int q = q0 + u;
@@ -135,8 +139,14 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
                         const float2* col = A + (j0 + q) * lda;
                         if (pair) a[u] = __ldcs(reinterpret_cast<const float4*>(col));
                         else { float2 t = col[0]; a[u] = make_float4(t.x, t.y, 0.f, 0.f); }
+                        if (EXACT == 2) {
+                            const float2* cl = col + bt.split_lo;
+                            if (pair) z[u] = __ldcs(reinterpret_cast<const float4*>(cl));
+                            else { float2 t = cl[0]; z[u] = make_float4(t.x, t.y, 0.f, 0.f); }
+                        }
                     } else {
                         a[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (EXACT == 2) z[u] = make_float4(0.f, 0.f, 0.f, 0.f);
                     }
                 }
                 if (EXACT) {
@@ -152,6 +162,13 @@ __global__ void __launch_bounds__(MV_THREADS) gm_apply_kernel(GmBatch bt, int mo
                         l1 = fmaf(w.x, L.y, fmaf(w.y, L.x, l1));
                         l2 = fmaf(w.z, L.x, fmaf(-w.w, L.y, l2));
                         l3 = fmaf(w.z, L.y, fmaf(w.w, L.x, l3));
+                        if (EXACT == 2) {
+                            const float4 y = z[EXACT == 2 ? u : 0];
+                            l0 = fmaf(y.x, H.x, fmaf(-y.y, H.y, l0));
+                            l1 = fmaf(y.x, H.y, fmaf(y.y, H.x, l1));
+                            l2 = fmaf(y.z, H.x, fmaf(-y.w, H.y, l2));
+                            l3 = fmaf(y.z, H.y, fmaf(y.w, H.x, l3));
+                        }
                     }
                 } else {
                     float b0 = 0, b1 = 0, b2 = 0, b3 = 0;
@@ -902,7 +919,9 @@ static void launch_apply(Context& ctx, GmWorkspace& ws, int mode) {
         return;
     }
     dim3 grid = ws.bt.sys ? dim3((unsigned)ws.bt.ntiles) : dim3((unsigned)ws.rb, (unsigned)ws.cb, (unsigned)ws.bt.nsys);
-    if (ws.fp32) {
+    if (ws.bt.split_lo) {
+        gm_apply_kernel<float2, 2, 4><<<grid, MV_THREADS, 0, ctx.stream>>>(ws.bt, mode);
+    } else if (ws.fp32) {
         if (mode == MV_Q) {
             // columns per load batch (loads in flight per thread), tuned per size
             const int u = ctx.tuning.pick("gm_apply_fp32", "unroll", ws.bt.n, ws.bt.nsys, MV_UNROLL);

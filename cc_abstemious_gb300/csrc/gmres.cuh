@@ -48,6 +48,11 @@ struct GmBatch {
     double2* gs_part = nullptr;
     double* gs_norm = nullptr;
     int gs_chunks = 0;
+    // split FP64 operators (refined form): every system's FP32 matrix (the
+    // operator rounded to FP32, leading dimension lda) is followed, split_lo
+    // float2 entries further on, by the FP32 rounding of the remainder, and
+    // every mat-vec sums both in float-float (0: plain FP32 or FP64 operators)
+    int64_t split_lo = 0;
 };
 
 // Whether the operator application of `mode` has work for a system.

@@ -969,6 +969,9 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     const int nsys = ws.bt.nsys;
     std::vector<GmView> v((size_t)nsys);
     size_t entries = 0, dm = 0, wsz = 0, psz = 0;
+    // split FP64 operators: each occupies two FP32 planes, of which the
+    // factors copy the first (the operator's FP32 rounding) to half the offset
+    const size_t fdiv = ws.bt.split_lo ? 2 : 1;
     for (int s = 0; s < nsys; ++s) {
         v[(size_t)s] = ws.sys_host.empty() ? gm_view(ws.bt, s) : GmView{};
         if (!ws.sys_host.empty()) {
@@ -977,7 +980,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
             v[(size_t)s].lda = q.lda;
             v[(size_t)s].a = q.a_off;
         }
-        entries = std::max(entries, v[(size_t)s].a + (size_t)v[(size_t)s].lda * v[(size_t)s].n);
+        entries = std::max(entries, v[(size_t)s].a / fdiv + (size_t)v[(size_t)s].lda * v[(size_t)s].n);
         const int nb = (int)((v[(size_t)s].n + LB - 1) / LB);
         dm += (size_t)nb * LB * LB;
         wsz += (size_t)2 * v[(size_t)s].n * WK;
@@ -990,7 +993,19 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     c.w_lu_D.ensure(sizeof(float2) * std::max<size_t>(dm, 1));
     c.w_lu_W.ensure(sizeof(float) * std::max<size_t>(wsz, 4));
     c.w_lu_P.ensure(sizeof(float) * std::max<size_t>(psz, 4));
-    if (ws.fp32) {
+    if (ws.bt.split_lo) {
+        // one copy per distinct operator (several right-hand sides share one)
+        for (int s = 0; s < nsys; ++s) {
+            bool first = true;
+            for (int o = 0; o < s && first; ++o) first = v[(size_t)o].a != v[(size_t)s].a;
+            require(v[(size_t)s].a % 2 == 0, "LU: split operator offset", BEM_ERR_CUDA);
+            if (first)
+                BEM_CUDA(cudaMemcpyAsync(c.w_lu_F.as<float2>() + v[(size_t)s].a / 2,
+                                         static_cast<const float2*>(ws.bt.A) + v[(size_t)s].a,
+                                         sizeof(float2) * (size_t)v[(size_t)s].lda * v[(size_t)s].n,
+                                         cudaMemcpyDeviceToDevice, c.stream));
+        }
+    } else if (ws.fp32) {
         BEM_CUDA(cudaMemcpyAsync(c.w_lu_F.p, ws.bt.A, sizeof(float2) * entries, cudaMemcpyDeviceToDevice, c.stream));
     } else {
         // FP64 operator (refined form): factor its FP32 rounding
@@ -1033,7 +1048,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
             L = d->sys[(size_t)owner[(size_t)s]];
             continue;
         }
-        L.F = c.w_lu_F.as<float2>() + v[(size_t)s].a;
+        L.F = c.w_lu_F.as<float2>() + v[(size_t)s].a / fdiv;
         L.Dm = c.w_lu_D.as<float2>() + od;
         L.W = c.w_lu_W.as<float>() + ow;
         L.n = v[(size_t)s].n;

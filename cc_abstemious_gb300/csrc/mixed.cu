@@ -120,6 +120,10 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
     // the Hierarchical solver: ACA-compressed operators with FP32 factors
     // instead of dense ones (hmixed.cu)
     const bool hier = p.in.solver == 2 && !first_kind;
+    // FP64 operators assembled in one pass are kept split: their FP32
+    // rounding and the FP32 rounding of the remainder, the same 16 bytes per
+    // entry, applied in float-float on the FP32 pipe (gmres.cu)
+    const bool split = first_kind && !need_rowsum;
     if (!hier) c.w_mat.ensure((first_kind ? sizeof(double2) : sizeof(float2)) * mstride * nf);
     float2* A32 = c.w_mat.as<float2>();
     double2* A64 = c.w_mat.as<double2>();
@@ -149,12 +153,17 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
     if (hier) {
         gm_prepare(c, ws, (int)ns, n, m, nullptr, n, 0, true, false);
     } else if (R == 1) {
-        gm_prepare(c, ws, (int)nf, n, m, Aop, ld, mstride, !first_kind, false);
+        gm_prepare(c, ws, (int)nf, n, m, Aop, ld, split ? 2 * mstride : mstride, !first_kind || split, false);
     } else {
         std::vector<int64_t> nsz((size_t)ns, n), lds((size_t)ns, ld);
         std::vector<size_t> aoff((size_t)ns);
-        for (int64_t s = 0; s < ns; ++s) aoff[(size_t)s] = (size_t)(s / R) * mstride;
-        gm_prepare_ragged(c, ws, nsz, lds, aoff, m, Aop, !first_kind);
+        for (int64_t s = 0; s < ns; ++s) aoff[(size_t)s] = (size_t)(s / R) * (split ? 2 * mstride : mstride);
+        gm_prepare_ragged(c, ws, nsz, lds, aoff, m, Aop, !first_kind || split);
+    }
+    if (split) {
+        ws.bt.split_lo = (int64_t)mstride;
+        ws.mv_stage = "gmres_matvec_split";
+        ws.mv_bytes = 16.0 * (double)n * (double)n;
     }
 
     if (hier) {
@@ -174,7 +183,7 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
         // every frequency in one pass, norms accumulated by the kernel
         EventTimer t(c);
         assemble_system_fp64_multi(c, p, ks.data(), al.data(), be.data(), (int)nf, A64, ld, mstride,
-                                   R == 1 ? ws.anorm : normf);
+                                   R == 1 ? ws.anorm : normf, split);
         if (R > 1) {
             repeat_norms_kernel<<<(unsigned)((ns + 127) / 128), 128, 0, c.stream>>>(normf, (int)R, (int)ns, ws.anorm);
             BEM_CHECK_LAUNCH(&c);

@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <chrono>
 #include <cstring>
 #include <memory>
 #include <random>
@@ -765,7 +766,26 @@ static int learned_gate(Context& c, PcData& d, GmWorkspace& ws, uint64_t seed) {
     return kept;
 }
 
+namespace {
+// Wall time of a preconditioner set-up (it ends synchronised) for the
+// library's per-stage profile.
+struct SetupTimer {
+    Context& c;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    int64_t l0;
+    explicit SetupTimer(Context& ctx) : c(ctx), l0(ctx.launches) {}
+    ~SetupTimer() {
+        if (!c.profiling) return;
+        cudaStreamSynchronize(c.stream);
+        c.stage_add("precond_setup",
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(),
+                    c.launches - l0, 0);
+    }
+};
+}  // namespace
+
 bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks) {
+    SetupTimer timer(c);
     if (kind == BEM_PRECOND_LU) {
         lu_precond_setup(c, ws);  // FP64 operators are factored from their FP32 rounding
         return kind;
@@ -807,6 +827,7 @@ bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond k
 // system's blocks are stored back to back.
 bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies, const std::vector<int>& sys_body,
                                 GmWorkspace& ws, bem_precond kind, const double* ks) {
+    SetupTimer timer(c);
     if (kind == BEM_PRECOND_LU) {
         lu_precond_setup(c, ws);
         return kind;

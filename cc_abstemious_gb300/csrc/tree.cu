@@ -17,6 +17,7 @@
 // identical to a sequential FP64 construction.  The host only reads one
 // counter per level.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -416,8 +417,24 @@ void tree_error(int e) {
     if (e) throw Error(BEM_ERR_CUDA, "cluster tree: node storage exceeded");
 }
 
+// Wall time of a tree stage (it ends with a synchronisation) for the
+// library's per-stage profile.
+struct TreeTimer {
+    Context& c;
+    const char* name;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    int64_t l0;
+    TreeTimer(Context& ctx, const char* n) : c(ctx), name(n), l0(ctx.launches) {}
+    ~TreeTimer() {
+        if (c.profiling)
+            c.stage_add(name, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(),
+                        c.launches - l0, 0);
+    }
+};
+
 // The cluster trees of the points in d_xyz (F.pt0 set by the caller).
 void build_forest_dev(Context& c, Forest& F, const DevBuf& d_xyz) {
+    TreeTimer timer(c, "cluster_tree");
     const int nb = F.nbodies;
     const int64_t total = F.pt0[(size_t)nb];
     const int cap = (int)std::min<int64_t>(2 * total + 2 * nb + 2, INT32_MAX);
@@ -575,6 +592,7 @@ std::shared_ptr<Forest> build_forest(Context& c, const std::vector<const Problem
 }
 
 std::vector<BlockLeaf> forest_block_leaves(Context& c, const Forest& F, double eta) {
+    TreeTimer timer(c, "block_tree");
     const int nb = F.nbodies;
     DevBuf d_nodes, d_pr, d_kind, d_cb, d_cnt, d_off, d_ctr, d_out;
     // the block tree reads boxes, diameters and sons only

@@ -120,6 +120,21 @@ def test_refined_form(ctx, wd):
         assert r["iterations"] <= 12
 
 
+@pytest.mark.parametrize("precond", [None, "block_jacobi", "lu"])
+def test_refined_form_reaches_fp64_level(ctx, wd, precond):
+    """The refined form holds each FP64 operator as its FP32 rounding plus the
+    FP32 rounding of the remainder and applies it in float-float: at a tight
+    backward-error tolerance the answer agrees with the FP64 LU at FP64 level,
+    which neither an FP32 operator nor an operator error of 2^-24 allows."""
+    inp = workloads.perturbed_sphere_input(wd, 13, 900, [2.0, 5.0], tol=1e-12)
+    a = bem.Analysis(ctx)
+    a.set_input(inp)
+    a.run(form="refined", precond=precond, check_vs_lu=True)
+    for r in a.reports:
+        assert r["flag"] == 1, r
+        assert 0 <= r["rel_err_vs_lu"] < 1e-10, r
+
+
 @pytest.mark.parametrize("ntri", [700, 1030, 1300])
 def test_lu_partial_step_groups(ctx, wd, ntri):
     """Block counts that end inside a group of four delayed steps: 6, 9 and
