@@ -439,6 +439,19 @@ def run_batch(predatas, precond=None, check_vs_lu=False, max_operator_bytes=0, c
     return results
 
 
+def assemble_operator(pd, kind="split", f0=0, nf=None):
+    """The operators A_f = alpha_f H_f + beta_f G_f of frequencies f0 ..
+    f0 + nf - 1 of a problem as the batched forms assemble them: kind "fp32"
+    (the mixed form) or "split" (the refined form: FP32 rounding plus FP32
+    remainder, returned summed in FP64).  Returns an (nf, n, n) array."""
+    nf = len(pd.frequencies) - f0 if nf is None else nf
+    n = pd.n
+    A = np.zeros((nf, n, n), dtype=np.complex128)  # each [f] holds A_f^T (column-major fill)
+    k = {"fp32": 0, "split": 1}[kind]
+    pd.ctx.check(pd.ctx.lib.bem_assemble_operator(pd.ctx.h, pd.h, k, f0, nf, _ptr(A), n))
+    return np.ascontiguousarray(np.transpose(A, (0, 2, 1)))
+
+
 def cluster_tree(point_sets, leaf, eta=None, ctx=None):
     """Cluster trees (cluster.rs:35-105) of one or several point sets and,
     with eta, their block trees (block.rs:38-93), built on the device in one

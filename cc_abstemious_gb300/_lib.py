@@ -93,6 +93,7 @@ SIGNATURES = {
     "bem_learned_mlp_eval": (_i, [_vp, _i64, _vp, _vp, _vp, _vp]),
     "bem_learned_mlp_infer": (_i, [_vp, _i64, _vp, _vp]),
     "bem_lu32_factor_apply": (_i, [_vp, _i, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
+    "bem_assemble_operator": (_i, [_vp, _vp, _i, _i64, _i64, _vp, _i64]),
     "bem_cluster_tree": (_i, [_vp, _i, _vp, _vp, _i64, _i64, _d, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp]),
     "bem_hmatrix_build": (_i, [_vp, _vp, _i, _PP]),
     "bem_hmatrix_destroy": (None, [_vp]),

@@ -423,6 +423,54 @@ BEM_API bem_status bem_get_dense_surface_matrices(bem_ctx* ctx, const bem_proble
     });
 }
 
+BEM_API bem_status bem_assemble_operator(bem_ctx* ctx, const bem_problem* pp, int kind, int64_t f0, int64_t nf,
+                                         bem_cplx* A, int64_t lda) {
+    if (!ctx || !pp || !A || (kind != 0 && kind != 1)) return BEM_ERR_BAD_INPUT;
+    return guard(ctx, [&] {
+        Context& c = ctx->c;
+        Problem& p = const_cast<Problem&>(pp->p);
+        set_device(c);
+        const int64_t n = p.n, ld = p.geo.npad, NF = (int64_t)p.freqs.size();
+        require(lda >= n, "lda < n");
+        require(f0 >= 0 && nf >= 1 && f0 + nf <= NF, "frequency range outside the problem's list");
+        const int64_t saved = p.ifreq;
+        std::vector<double> ks((size_t)nf);
+        std::vector<cd> al((size_t)nf), be((size_t)nf), ga((size_t)nf), de((size_t)nf);
+        for (int64_t f = 0; f < nf; ++f) {
+            p.ifreq = f0 + f;
+            ks[(size_t)f] = p.wavenumber();
+            lhs_factors(p, al[(size_t)f], be[(size_t)f]);
+            rhs_factors(p, ga[(size_t)f], de[(size_t)f]);
+        }
+        p.ifreq = saved;
+        const size_t plane = (size_t)ld * n;
+        DevBuf d, norms;
+        d.ensure(sizeof(float2) * plane * (kind ? 2 : 1) * (size_t)nf);
+        norms.ensure(sizeof(double) * (size_t)nf);
+        if (kind == 0)
+            assemble_system_fp32_body(c, p, ks.data(), al.data(), be.data(), ga.data(), de.data(), (int)nf,
+                                      d.as<float2>(), ld, plane, nullptr, 0, norms.as<double>());
+        else
+            assemble_system_split(c, p, ks.data(), al.data(), be.data(), (int)nf, d.as<float2>(), ld, plane,
+                                  norms.as<double>());
+        std::vector<float2> h(plane * (kind ? 2 : 1) * (size_t)nf);
+        BEM_CUDA(cudaMemcpyAsync(h.data(), d.p, sizeof(float2) * h.size(), cudaMemcpyDeviceToHost, c.stream));
+        c.sync();
+        const size_t sstride = plane * (kind ? 2 : 1);
+        for (int64_t f = 0; f < nf; ++f)
+            for (int64_t j = 0; j < n; ++j)
+                for (int64_t i = 0; i < n; ++i) {
+                    const size_t o = (size_t)f * sstride + (size_t)j * ld + i;
+                    double re = h[o].x, im = h[o].y;
+                    if (kind) {
+                        re += (double)h[o + plane].x;
+                        im += (double)h[o + plane].y;
+                    }
+                    A[(size_t)f * lda * n + (size_t)j * lda + i] = bem_cplx{re, im};
+                }
+    });
+}
+
 BEM_API bem_status bem_get_dense_field_matrices(bem_ctx* ctx, const bem_problem* pp, bem_cplx* M, bem_cplx* L,
                                                 int64_t ld, bem_mem mem) {
     if (!ctx || !pp || !M || !L) return BEM_ERR_BAD_INPUT;

@@ -136,187 +136,6 @@ __global__ void __launch_bounds__(ASM_THREADS) assemble64_kernel(
     }
 }
 
-// Refined form: A_s = alpha_s H_s + beta_s G_s in FP64 for up to MAX_SYS64
-// frequencies per pass.  Not the parity kernel (that one follows the reference
-// arithmetic frequency by frequency): the pair geometry (separation, 1/r,
-// direction cosines, wt*area/(4 pi r)) is evaluated once, and when the
-// wavenumbers are evenly spaced, k_s = k_0 + s dk, e^{i k_s r} comes from
-// e^{i k_0 r} by repeated multiplication with e^{i dk r} (two sincos per pair
-// instead of one per frequency; the rounding grows by ~1e-16 per step).
-constexpr int MAX_SYS64 = 16;
-struct Sys64 {
-    double k, beta_im, gdiag_im;
-    z2 alpha, beta;
-};
-struct Asm64Params {
-    int nsys, bm, recur, pad;
-    double hdiag, k0, dk;
-    Sys64 s[MAX_SYS64];
-};
-
-// Stores entry a of system s at column-major offset o: as a double2 (plane =
-// 0; systems mat_stride entries apart), or split (plane = the FP32 matrix's
-// size): the FP32 rounding hi at float2 offset o and the rounding of the
-// exact remainder a - hi a plane further on (systems mat_stride float2 apart).
-__device__ __forceinline__ void store_a64(double2* A, size_t plane, size_t o, double2 a) {
-    if (!plane) {
-        A[o] = a;
-        return;
-    }
-    float2* F = reinterpret_cast<float2*>(A);
-    const float hx = __double2float_rn(a.x), hy = __double2float_rn(a.y);
-    F[o] = make_float2(hx, hy);
-    F[o + plane] = make_float2(__double2float_rn(a.x - (double)hx), __double2float_rn(a.y - (double)hy));
-}
-
-__global__ void __launch_bounds__(ASM_THREADS) assemble64_multi_kernel(int64_t n, int64_t npad,
-                                                                      const double* __restrict__ geo,
-                                                                      Asm64Params prm, double2* __restrict__ A,
-                                                                      int64_t ld, size_t mat_stride, size_t plane,
-                                                                      double* __restrict__ norm_part,
-                                                                      int* __restrict__ err) {
-    __shared__ __align__(128) TileGeo64 t;
-    __shared__ __align__(8) uint64_t bar;
-    __shared__ double red[ASM_THREADS / 32][MAX_SYS64];
-    const int64_t I0 = (int64_t)blockIdx.y * TILE, J0 = (int64_t)blockIdx.x * TILE;
-    if (!stage_tile64(t, &bar, geo, npad, I0, J0)) {
-        if (threadIdx.x == 0) atomicOr(err, DEVERR_MBAR_TIMEOUT);
-        mbar_wait_bounded(&bar, 0);
-        return;
-    }
-    const int tx = threadIdx.x & (TILE - 1), ty = threadIdx.x >> 6;
-    const int64_t i = I0 + tx;
-    const double yx = t.rx[tx], yy = t.ry[tx], yz = t.rz[tx];
-    const double eyx = t.rex[tx], eyy = t.rey[tx], eyz = t.rez[tx];
-    double nrm[MAX_SYS64];
-#pragma unroll
-    for (int s = 0; s < MAX_SYS64; ++s) nrm[s] = 0.0;
-#pragma unroll 1
-    for (int c = 0; c < TILE / 4; ++c) {
-        const int jj = ty + 4 * c;
-        const int64_t j = J0 + jj;
-        if (i >= n || j >= n) continue;
-        const size_t oij = (size_t)(j * ld + i);
-        if (i == j) {
-#pragma unroll
-            for (int s = 0; s < MAX_SYS64; ++s) {
-                if (s >= prm.nsys) break;
-                z2 g, h;
-                self_term64(t.carea[jj], t.cwt[jj], prm.bm, prm.s[s].beta_im, prm.hdiag, prm.s[s].gdiag_im, g, h);
-                z2 a = cmul(prm.s[s].alpha, h);
-                cfma(a, prm.s[s].beta, g);
-                store_a64(A, plane, s * mat_stride + oij, a);
-                nrm[s] += a.x * a.x + a.y * a.y;
-            }
-            continue;
-        }
-        const double rx = t.cx[jj] - yx, ry = t.cy[jj] - yy, rz = t.cz[jj] - yz;
-        const double r = sqrt(rx * rx + ry * ry + rz * rz);
-        const double inv = 1.0 / r;
-        const double erx = rx * inv, ery = ry * inv, erz = rz * inv;
-        const double rdoty = erx * eyx + ery * eyy + erz * eyz;
-        const double rdotx = erx * t.cex[jj] + ery * t.cey[jj] + erz * t.cez[jj];
-        const double nxy = eyx * t.cex[jj] + eyy * t.cey[jj] + eyz * t.cez[jj];
-        const double q = inv * t.cwa[jj] * (1.0 / (4.0 * PI_D));
-        z2 ph, step;
-        if (prm.recur) {
-            sincos(prm.k0 * r, &ph.y, &ph.x);
-            sincos(prm.dk * r, &step.y, &step.x);
-        }
-#pragma unroll
-        for (int s = 0; s < MAX_SYS64; ++s) {
-            if (s >= prm.nsys) break;
-            const double k = prm.s[s].k;
-            z2 e;
-            if (prm.recur) {
-                e = ph;
-                ph = cmul(ph, step);
-            } else {
-                sincos(k * r, &e.y, &e.x);
-            }
-            z2 g = make_double2(e.x * q, e.y * q);
-            const z2 f1 = make_double2(-inv, k);
-            const z2 gf1 = cmul(g, f1);
-            z2 h = cscale(gf1, -rdoty);
-            if (prm.bm) {
-                const z2 dg = cscale(gf1, rdotx);
-                const z2 t1 = make_double2(inv * nxy, -k * nxy);  // (-f1) nxy
-                const z2 t2 = cscale(make_double2(k * k * r + 3.0 * f1.x, 3.0 * f1.y), rdotx * rdoty);
-                const z2 dh = cmul(cscale(g, inv), csub(t1, t2));
-                const double bi = prm.s[s].beta_im;
-                g = cadd(g, make_double2(-bi * dg.y, bi * dg.x));
-                h = cadd(h, make_double2(-bi * dh.y, bi * dh.x));
-            }
-            z2 a = cmul(prm.s[s].alpha, h);
-            cfma(a, prm.s[s].beta, g);
-            store_a64(A, plane, s * mat_stride + oij, a);
-            nrm[s] += a.x * a.x + a.y * a.y;
-        }
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int s = 0; s < MAX_SYS64; ++s) {
-        if (s >= prm.nsys) break;
-        double v = nrm[s];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) red[warp][s] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < prm.nsys) {
-        double sum = 0;
-        for (int w = 0; w < ASM_THREADS / 32; ++w) sum += red[w][threadIdx.x];
-        norm_part[(size_t)threadIdx.x * gridDim.x * gridDim.y + (size_t)blockIdx.y * gridDim.x + blockIdx.x] = sum;
-    }
-}
-
-void assemble_system_fp64_multi(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
-                                const cd* betas, int nsys, double2* A, int64_t ld, size_t mat_stride,
-                                double* norms, bool split) {
-    // split: the systems' planes are ld * n float2 each, systems 2 ld n float2
-    // apart (the bytes of one double2 matrix)
-    const size_t plane = split ? (size_t)ld * p.n : 0;
-    const size_t stride = split ? 2 * plane : mat_stride;
-    require(!split || mat_stride == plane, "split FP64 assembly: systems must be ld * n entries apart");
-    int* err = device_err(ctx);
-    BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx.stream));
-    const int ntiles = (int)(p.geo.npad / TILE);
-    const int64_t nparts = (int64_t)ntiles * ntiles;
-    ctx.w_norm.ensure(sizeof(double) * (size_t)nparts * MAX_SYS64);
-    const KParams kp = kparams(p);
-    for (int s0 = 0; s0 < nsys; s0 += MAX_SYS64) {
-        Asm64Params prm{};
-        prm.nsys = std::min(MAX_SYS64, nsys - s0);
-        prm.bm = kp.bm;
-        prm.hdiag = kp.hdiag;
-        double kmax = 0;
-        for (int s = 0; s < prm.nsys; ++s) {
-            const double k = ks[s0 + s];
-            Sys64& S = prm.s[s];
-            S.k = k;
-            S.beta_im = kp.bm ? 1.0 / k : 0.0;
-            S.gdiag_im = kp.bm ? 0.5 * (1.0 / k) : 0.0;
-            S.alpha = make_double2(alphas[s0 + s].re, alphas[s0 + s].im);
-            S.beta = make_double2(betas[s0 + s].re, betas[s0 + s].im);
-            kmax = std::max(kmax, std::fabs(k));
-        }
-        // evenly spaced wavenumbers: the recurrence
-        prm.k0 = ks[s0];
-        prm.dk = prm.nsys > 1 ? (ks[s0 + prm.nsys - 1] - ks[s0]) / (prm.nsys - 1) : 0.0;
-        prm.recur = prm.nsys > 1;
-        for (int s = 0; s < prm.nsys && prm.recur; ++s)
-            if (std::fabs(ks[s0 + s] - (prm.k0 + s * prm.dk)) > 1e-13 * kmax) prm.recur = 0;
-        dim3 grid((unsigned)ntiles, (unsigned)ntiles);
-        // system s0 starts s0 * stride entries of the store's type in
-        double2* A0 = split ? reinterpret_cast<double2*>(reinterpret_cast<float2*>(A) + (size_t)s0 * stride)
-                            : A + (size_t)s0 * stride;
-        assemble64_multi_kernel<<<grid, ASM_THREADS, 0, ctx.stream>>>(p.n, p.geo.npad, p.geo.arr(0), prm, A0, ld,
-                                                                      stride, plane, ctx.w_norm.as<double>(), err);
-        BEM_CHECK_LAUNCH(&ctx);
-        finish_norms(ctx, ctx.w_norm.as<double>(), nparts, prm.nsys, norms + s0);
-    }
-    check_device_err(ctx);
-}
-
 // rowsum[i] = sum over column tiles of part[t][i] (fixed order).
 __global__ void reduce_parts_kernel(int64_t n, int64_t npad, int ntiles, const double2* __restrict__ part,
                                     double2* __restrict__ out) {

@@ -11,6 +11,7 @@
 // the GMRES stopping test) so the operators are never re-read for it.
 #include "common.cuh"
 #include "complex.cuh"
+#include "ff.cuh"
 #include "kernels.cuh"
 #include "tma.cuh"
 
@@ -404,6 +405,209 @@ __global__ void finish_norm_kernel(const double* __restrict__ part, int64_t npar
 void finish_norms(Context& ctx, const double* part, int64_t nparts, int nsys, double* out) {
     finish_norm_kernel<<<nsys, 256, 0, ctx.stream>>>(part, nparts, out);
     BEM_CHECK_LAUNCH(&ctx);
+}
+
+
+// ---------------------------------------------------------------------------
+// Split FP64 operators in float-float (refined form and first-kind systems).
+// The entry formula of the FP64 assembly (influence_matrix.rs:170-230: the
+// Burton-Miller combination alpha H + beta G) evaluated in float-float on the
+// FP32 pipe: separation, 1/r, direction cosines and phase in float-float,
+// e^{ik r} by ff_cossin (once per pair and the recurrence e^{ik_s r} =
+// e^{ik_0 r} e^{i dk r}^s for evenly spaced wavenumbers, as the FP64 kernel
+// does), the singular self term in FP64.  Each entry is stored as its float
+// pair: the high plane is the operator rounded to FP32, the low plane (plane
+// float2 further on) the remainder, ~2^-44 relative to the FP64 value.
+struct SysFF {
+    ff k, k2, bi;        // wavenumber, k^2, 1/k (Burton-Miller) or 0
+    cff alpha, beta;     // LHS factors
+    int alpha_one, beta_zero;
+    double kd, beta_im, gdiag_im;
+    double2 alpha_d, beta_d;
+};
+constexpr int MAX_SYSFF = 16;
+struct AsmFFParams {
+    int nsys, bm, recur, pad;
+    double hdiag;
+    ff k0, dk;           // recurrence: k_s = k0 + s dk
+    SysFF s[MAX_SYSFF];
+};
+
+__device__ __forceinline__ ff ffd(float h, float l) { return ff{h, l}; }
+
+__global__ void __launch_bounds__(ASM_THREADS, 2) assemble_ff_kernel(int64_t n, int64_t npad,
+                                                                    const float* __restrict__ g32,
+                                                                    const double* __restrict__ geo, AsmFFParams prm,
+                                                                    float2* __restrict__ A, int64_t ld, size_t stride,
+                                                                    size_t plane, double* __restrict__ norm_part,
+                                                                    int* __restrict__ err) {
+    __shared__ __align__(128) Asm32Smem sm;
+    TileGeo32& t = sm.t;
+    const int64_t I0 = (int64_t)blockIdx.y * TILE, J0 = (int64_t)blockIdx.x * TILE;
+    if (threadIdx.x == 0) {
+        mbar_init(&sm.bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const uint32_t B = TILE * sizeof(float);
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&sm.bar, 26 * B);
+        float* cdst[14] = {t.cxh,  t.cxl, t.cyh,  t.cyl,  t.czh,  t.czl,  t.cex,
+                           t.cey,  t.cez, t.cwa,  t.cexl, t.ceyl, t.cezl, t.cwal};
+        for (int a = 0; a < 14; ++a) bulk_g2s(cdst[a], g32 + a * npad + J0, B, &sm.bar);
+        float* rdst[13] = {t.rxh, t.rxl, t.ryh, t.ryl, t.rzh, t.rzl, t.rex, t.rey, t.rez, nullptr, t.rexl, t.reyl, t.rezl};
+        for (int a = 0; a < 13; ++a)
+            if (rdst[a]) bulk_g2s(rdst[a], g32 + a * npad + I0, B, &sm.bar);
+    }
+    if (!mbar_wait_bounded(&sm.bar, 0)) {
+        if (threadIdx.x == 0) atomicOr(err, DEVERR_MBAR_TIMEOUT);
+        mbar_wait_bounded(&sm.bar, 0);
+        return;
+    }
+    const int tx = threadIdx.x & (TILE - 1), ty = threadIdx.x >> 6;
+    const int64_t i = I0 + tx;
+    const float yxh = t.rxh[tx], yxl = t.rxl[tx], yyh = t.ryh[tx], yyl = t.ryl[tx], yzh = t.rzh[tx],
+                yzl = t.rzl[tx];
+    const ff eyx = ffd(t.rex[tx], t.rexl[tx]), eyy = ffd(t.rey[tx], t.reyl[tx]), eyz = ffd(t.rez[tx], t.rezl[tx]);
+    float nrm[MAX_SYSFF];
+#pragma unroll
+    for (int s = 0; s < MAX_SYSFF; ++s) nrm[s] = 0.f;
+#pragma unroll 1
+    for (int c = 0; c < TILE / 4; ++c) {
+        const int jj = ty + 4 * c;
+        const int64_t j = J0 + jj;
+        if (i >= n || j >= n) continue;
+        const size_t o = (size_t)(j * ld + i);
+        if (i == j) {
+            const double area = geo[GAREA * npad + j], wt = geo[GWT * npad + j];
+#pragma unroll 1
+            for (int s = 0; s < prm.nsys; ++s) {
+                z2 g, h;
+                self_term64(area, wt, prm.bm, prm.s[s].beta_im, prm.hdiag, prm.s[s].gdiag_im, g, h);
+                z2 a = cmul(prm.s[s].alpha_d, h);
+                cfma(a, prm.s[s].beta_d, g);
+                const float hx = __double2float_rn(a.x), hy = __double2float_rn(a.y);
+                A[s * stride + o] = make_float2(hx, hy);
+                A[s * stride + o + plane] =
+                    make_float2(__double2float_rn(a.x - (double)hx), __double2float_rn(a.y - (double)hy));
+                nrm[s] += hx * hx + hy * hy;
+            }
+            continue;
+        }
+        // separation d = x_j - y_i, r, 1/r, direction cosines (float-float)
+        const ff dx = ff_sub(t.cxh[jj], t.cxl[jj], yxh, yxl);
+        const ff dy = ff_sub(t.cyh[jj], t.cyl[jj], yyh, yyl);
+        const ff dz = ff_sub(t.czh[jj], t.czl[jj], yzh, yzl);
+        const ff r = ff_sqrt(dx * dx + dy * dy + dz * dz);
+        const ff inv = ff_recip(r);
+        const ff exj = ffd(t.cex[jj], t.cexl[jj]), eyj = ffd(t.cey[jj], t.ceyl[jj]), ezj = ffd(t.cez[jj], t.cezl[jj]);
+        const ff rdoty = (dx * eyx + dy * eyy + dz * eyz) * inv;
+        const ff rdotx = (dx * exj + dy * eyj + dz * ezj) * inv;
+        const ff nxy = eyx * exj + eyy * eyj + eyz * ezj;
+        const ff q = inv * ffd(t.cwa[jj], t.cwal[jj]);  // wt area / (4 pi r)
+        cff e, step;
+        if (prm.recur) {
+            ff_cossin(prm.k0 * r, e.re, e.im);
+            ff_cossin(prm.dk * r, step.re, step.im);
+        }
+        const ff rr = rdotx * rdoty;
+#pragma unroll 1
+        for (int s = 0; s < prm.nsys; ++s) {
+            const SysFF& S = prm.s[s];
+            if (prm.recur) {
+                if (s) e = e * step;
+            } else {
+                ff_cossin(S.k * r, e.re, e.im);
+            }
+            cff g = e * q;
+            // g f1 with f1 = i k - 1/r
+            const cff gf1 = times_i(g, S.k) - g * inv;
+            cff h = gf1 * (-rdoty);
+            if (prm.bm) {
+                const cff dg = gf1 * rdotx;
+                const cff t1 = cff{inv * nxy, -(S.k * nxy)};                  // (-f1) nxy
+                const cff t2 = cff{(S.k2 * r - 3.0f * inv) * rr, (3.0f * S.k) * rr};
+                const cff dh = (g * inv) * (t1 - t2);
+                g = g + times_i(dg, S.bi);
+                h = h + times_i(dh, S.bi);
+            }
+            cff a = S.alpha_one ? h : S.alpha * h;
+            if (!S.beta_zero) a = a + S.beta * g;
+            A[s * stride + o] = make_float2(a.re.h, a.im.h);
+            A[s * stride + o + plane] = make_float2(a.re.l, a.im.l);
+            nrm[s] += a.re.h * a.re.h + a.im.h * a.im.h;
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int s = 0; s < MAX_SYSFF; ++s) {
+        if (s >= prm.nsys) break;
+        float v = nrm[s];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sm.red[warp][s] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < prm.nsys) {
+        double sum = 0;
+        for (int w = 0; w < ASM_THREADS / 32; ++w) sum += sm.red[w][threadIdx.x];
+        norm_part[(size_t)threadIdx.x * gridDim.x * gridDim.y + (size_t)blockIdx.y * gridDim.x + blockIdx.x] = sum;
+    }
+}
+
+static ff host_ff(double v) {
+    const float h = (float)v;
+    return ff{h, (float)(v - (double)h)};
+}
+
+void assemble_system_split(Context& ctx, const Problem& p, const double* ks, const cd* alphas, const cd* betas,
+                           int nsys, float2* A, int64_t ld, size_t plane, double* norms) {
+    require(plane == (size_t)ld * p.n, "split assembly: planes must be ld * n entries");
+    int* err = device_err(ctx);
+    BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx.stream));
+    const int ntiles = (int)(p.geo.npad / TILE);
+    const int64_t nparts = (int64_t)ntiles * ntiles;
+    ctx.w_norm.ensure(sizeof(double) * (size_t)nparts * MAX_SYSFF);
+    const KParams kp = kparams(p);
+    for (int s0 = 0; s0 < nsys; s0 += MAX_SYSFF) {
+        AsmFFParams prm{};
+        prm.nsys = std::min(MAX_SYSFF, nsys - s0);
+        prm.bm = kp.bm;
+        prm.hdiag = kp.hdiag;
+        double kmax = 0;
+        for (int s = 0; s < prm.nsys; ++s) {
+            const double k = ks[s0 + s];
+            SysFF& S = prm.s[s];
+            S.k = host_ff(k);
+            S.k2 = host_ff(k * k);
+            S.bi = host_ff(kp.bm ? 1.0 / k : 0.0);
+            const cd al = alphas[s0 + s], be = betas[s0 + s];
+            S.alpha = cff{host_ff(al.re), host_ff(al.im)};
+            S.beta = cff{host_ff(be.re), host_ff(be.im)};
+            S.alpha_one = al.re == 1.0 && al.im == 0.0;
+            S.beta_zero = be.re == 0.0 && be.im == 0.0;
+            S.kd = k;
+            S.beta_im = kp.bm ? 1.0 / k : 0.0;
+            S.gdiag_im = kp.bm ? 0.5 * (1.0 / k) : 0.0;
+            S.alpha_d = make_double2(al.re, al.im);
+            S.beta_d = make_double2(be.re, be.im);
+            kmax = std::max(kmax, std::fabs(k));
+        }
+        // evenly spaced wavenumbers: the recurrence (the FP64 kernel's rule)
+        const double k0 = ks[s0];
+        const double dk = prm.nsys > 1 ? (ks[s0 + prm.nsys - 1] - ks[s0]) / (prm.nsys - 1) : 0.0;
+        prm.recur = prm.nsys > 1;
+        for (int s = 0; s < prm.nsys && prm.recur; ++s)
+            if (std::fabs(ks[s0 + s] - (k0 + s * dk)) > 1e-13 * kmax) prm.recur = 0;
+        prm.k0 = host_ff(k0);
+        prm.dk = host_ff(dk);
+        dim3 grid((unsigned)ntiles, (unsigned)ntiles);
+        assemble_ff_kernel<<<grid, ASM_THREADS, 0, ctx.stream>>>(p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0), prm,
+                                                                 A + (size_t)s0 * 2 * plane, ld, 2 * plane, plane,
+                                                                 ctx.w_norm.as<double>(), err);
+        BEM_CHECK_LAUNCH(&ctx);
+        finish_norms(ctx, ctx.w_norm.as<double>(), nparts, prm.nsys, norms + s0);
+    }
+    check_device_err(ctx);
 }
 
 void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks, const cd* alphas, const cd* betas,

@@ -247,15 +247,14 @@ void assemble_surface_fp64(Context& ctx, const Problem& p, double2* H, double2* 
 // A = alpha H + beta G and rowsum(gamma H + delta G) partials (fused solve path)
 void assemble_system_fp64(Context& ctx, const Problem& p, double2* A, int64_t ld, cd alpha, cd beta,
                           cd gamma, cd delta, double2* rowsum /* n, may be null */);
-// A_s = alpha_s H_s + beta_s G_s in FP64 for several frequencies (refined
-// form): geometry once per pair, e^{ik r} by recurrence when the wavenumbers
-// are evenly spaced; norms[s] = ||A_s||_F.
-// split: each operator stored as its FP32 rounding (float2, ld * n entries)
-// followed by the FP32 rounding of the remainder (the same size), operators
-// 2 ld n float2 apart (mat_stride must be ld * n).
-void assemble_system_fp64_multi(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
-                                const cd* betas, int nsys, double2* A, int64_t ld, size_t mat_stride,
-                                double* norms, bool split = false);
+// A_s = alpha_s H_s + beta_s G_s for several frequencies, split: the
+// operator's FP32 rounding (float2, ld * n entries) followed by the FP32
+// rounding of the remainder (`plane` = ld * n further on), evaluated in
+// float-float (~2^-44 relative) with the geometry once per pair and
+// e^{ik r} by recurrence for evenly spaced wavenumbers; systems 2 * plane
+// float2 apart; norms[s] = ||A_s||_F.
+void assemble_system_split(Context& ctx, const Problem& p, const double* ks, const cd* alphas, const cd* betas,
+                           int nsys, float2* A, int64_t ld, size_t plane, double* norms);
 void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
                                const cd* betas, const cd* gammas, const cd* deltas, int nsys, float2* A,
                                int64_t ld, size_t mat_stride, double2* rowsum, size_t vec_stride, double* norms);

@@ -179,16 +179,17 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
                 hmatrix_row_sums(c, p, 0, rowsum + f * n);
             }
         t.stop("hmatrix_build", nf, 8.0 * (double)hs.store_entries);
-    } else if (first_kind && !need_rowsum) {
-        // every frequency in one pass, norms accumulated by the kernel
+    } else if (split) {
+        // every frequency in one pass, in float-float, norms accumulated by
+        // the kernel
         EventTimer t(c);
-        assemble_system_fp64_multi(c, p, ks.data(), al.data(), be.data(), (int)nf, A64, ld, mstride,
-                                   R == 1 ? ws.anorm : normf, split);
+        assemble_system_split(c, p, ks.data(), al.data(), be.data(), (int)nf, reinterpret_cast<float2*>(A64), ld,
+                              mstride, R == 1 ? ws.anorm : normf);
         if (R > 1) {
             repeat_norms_kernel<<<(unsigned)((ns + 127) / 128), 128, 0, c.stream>>>(normf, (int)R, (int)ns, ws.anorm);
             BEM_CHECK_LAUNCH(&c);
         }
-        t.stop("assemble_fp64", (nf + 15) / 16, 16.0 * (double)n * n * nf);
+        t.stop("assemble_split", (nf + 15) / 16, 16.0 * (double)n * n * nf);
     } else if (first_kind) {
         EventTimer t(c);
         for (int64_t f = 0; f < nf; ++f) {

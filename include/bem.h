@@ -178,6 +178,17 @@ BEM_API bem_status bem_problem_set_frequency_index(bem_problem* p, int64_t index
  * preprocess.rs:126-153. */
 BEM_API bem_status bem_collocation(bem_ctx* ctx, const bem_problem* p, double* out);
 
+/* The operators A_f = alpha_f H_f + beta_f G_f of frequencies f0 .. f0 + nf - 1
+ * (the factors of influence_matrix.rs:130-162) as the batched forms assemble
+ * them, for checking them against bem_get_dense_surface_matrices: kind 0 the
+ * mixed form's single-precision assembly, kind 1 the refined form's split
+ * float-float assembly (FP32 rounding + FP32 remainder, summed here in FP64).
+ * A (host) receives nf matrices of n x n, column-major, leading dimension lda,
+ * lda * n entries apart.  No reference counterpart (the reference assembles
+ * FP64 only, influence_matrix.rs:64-98). */
+BEM_API bem_status bem_assemble_operator(bem_ctx* ctx, const bem_problem* p, int kind, int64_t f0, int64_t nf,
+                                         bem_cplx* A, int64_t lda);
+
 /* ---- influence matrices (influence_matrix.rs) ------------------------- */
 /* influence_matrix.rs:64-98 get_dense_surface_matrices -> (H, G), n x n. */
 BEM_API bem_status bem_get_dense_surface_matrices(bem_ctx* ctx, const bem_problem* p,
