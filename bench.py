@@ -180,29 +180,17 @@ def ncu_traffic_ratio():
     return None
 
 
-def tf32_peak():
-    """cuBLAS TF32 GEMM throughput measured in this run (8192^3, best of 5,
-    CUDA events): the denominator for the TF32 tensor-core LU update, since the
-    measured peaks file covers HBM and BF16 only."""
-    import torch
-    prev = torch.backends.cuda.matmul.allow_tf32
-    torch.backends.cuda.matmul.allow_tf32 = True
-    n = 8192
-    a = torch.randn(n, n, device="cuda")
-    b = torch.randn(n, n, device="cuda")
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    best = float("inf")
-    for i in range(7):
-        e0.record()
-        c = a @ b
-        e1.record()
-        e1.synchronize()
-        if i >= 2:
-            best = min(best, e0.elapsed_time(e1))
-    torch.backends.cuda.matmul.allow_tf32 = prev
-    del a, b, c
-    torch.cuda.empty_cache()
-    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+def tensor_peak():
+    """Dense 16-bit tensor throughput for the FP16 trailing update: the
+    sustained cuBLAS BF16 figure of MEASURED_PEAKS.json (FP16 and BF16 run at
+    one rate; the trailing updates run for seconds inside the factorization),
+    else the fallback."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        if d.get("bf16_tflops_sustained"):
+            return float(d["bf16_tflops_sustained"]), "measured (cuBLAS BF16 8192^3, sustained)"
+    return 1700.0, "fallback (sustained BF16)"
 
 
 def lu_traffic_ratio():
@@ -220,18 +208,19 @@ def lu_traffic_ratio():
     return None
 
 
-def lu_roofline(prof, sizes, what, peak=None):
+def lu_roofline(prof, sizes, what):
     """Roofline entry of the LU preconditioner's trailing update (the dominant
-    kernel of the LU forms): TF32 flop rate of the lu_gemm launches (event-timed
-    by the library's profiling pass; 8 n^3 / 3 complex flop per factored
-    operator) against cuBLAS TF32 measured here.  Block steps run in groups of
+    kernel of the LU forms): flop rate of the trailing-update launches
+    (event-timed by the library's profiling pass; 8 n^3 / 3 complex flop per
+    factored operator; FP16 operands, FP32 accumulation) against the measured
+    dense 16-bit tensor peak.  Block steps run in groups of
     four: one K = 1024 launch per group reads and writes the rest of the
     trailing block once, so its algorithmic bytes are 16 B (FP32 complex, read
     + write) per entry of that block (reported per operator: a launch covers
     every operator of a frequency chunk)."""
-    lu = prof.get("lu_gemm_tf32", {})
+    lu = prof.get("lu_gemm_trail", {})
     achieved = lu["bytes"] / (lu["ms"] * 1e-3) / 1e12 if lu.get("ms") else None
-    peak = tf32_peak() if peak is None else peak
+    peak, peak_kind = tensor_peak()
     lb, group = 128, 4
     tot, cnt = 0.0, 0
     for n in sizes:
@@ -246,9 +235,9 @@ def lu_roofline(prof, sizes, what, peak=None):
     return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak if achieved else None,
             "traffic": ratio * alg if (ratio and alg) else None,
-            "kernel": "lu_gemm_kernel<TRAIL> (TF32 tcgen05 trailing update of the LU preconditioner, " + what + ")",
+            "kernel": "lu_gemm_kernel<TRAIL> (FP16 tcgen05 trailing update of the LU preconditioner, " + what + ")",
             "algorithmic_bytes_per_operator_launch": alg,
-            "peak_kind": "measured in this run (cuBLAS TF32 GEMM 8192^3, burst)",
+            "peak_kind": peak_kind,
             "traffic_note": "ncu dram read+write / algorithmic A22 bytes of one K = 1024 launch "
                             "(profiles/lu_gemm_tf32_group_rigid_sphere.md), times the mean algorithmic bytes "
                             "of this workload's K = 1024 launches, per operator"}
@@ -586,13 +575,7 @@ class _Shared:
         self.ctx = bem.Context(local)
         self.stream = torch.cuda.ExternalStream(self.ctx.stream)
         self.wd = tempfile.mkdtemp(prefix="bem_targets_")
-        self._tf32 = None
         self.training = None
-
-    def tf32(self):
-        if self._tf32 is None:
-            self._tf32 = tf32_peak()
-        return self._tf32
 
     def train(self):
         """The learned preconditioner's network, trained on the GPU on
@@ -614,7 +597,7 @@ class _Shared:
         return self.training
 
     def lu_roofline(self, prof, sizes, what):
-        return lu_roofline(prof, sizes, what, self.tf32())
+        return lu_roofline(prof, sizes, what)
 
 
 def target_held_out(sh):

@@ -281,9 +281,9 @@ void run_mixed_batch(Context& c, const std::vector<Problem*>& probs, bem_precond
         std::vector<BodyPlan*> chunk;
         size_t bytes = 0;
         // the LU preconditioner keeps a factored copy of every operator and,
-        // per unknown, the diagonal blocks and the panel workspaces (13 KB)
+        // per unknown, the diagonal blocks and the panel workspaces (19 KB)
         auto need = [&](const BodyPlan* p) {
-            return precond == BEM_PRECOND_LU ? 2.0 * (double)p->op_bytes + 13400.0 * (double)p->n * (double)p->nf
+            return precond == BEM_PRECOND_LU ? 2.0 * (double)p->op_bytes + 19600.0 * (double)p->n * (double)p->nf
                                              : (double)p->op_bytes;
         };
         while (i < batched.size() && (chunk.empty() || (double)bytes + need(batched[i]) <= (double)budget_bytes)) {

@@ -213,7 +213,7 @@ struct Context {
     // batched GMRES workspace and Krylov-preconditioned basis, LU factors,
     // diagonal-block inverses and panel workspace (grow-only, reused by
     // every mixed solve)
-    DevBuf w_gm, w_gmz, w_lu_F, w_lu_D, w_lu_W, w_lu_P;
+    DevBuf w_gm, w_gmz, w_lu_F, w_lu_D, w_lu_W, w_lu_P, w_lu_H;
     DevBuf w_upload;  // mesh staging of problem construction
     DevBuf w_piv;     // row pivots of the plain form's FP64 LU
     // results of the last bem_run

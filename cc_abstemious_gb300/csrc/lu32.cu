@@ -16,8 +16,13 @@
 //          also writes L21 in natural form into the factors.
 //   u12    U12 = L11^-1 A12 on the tensor cores into a side buffer (the
 //          trailing update's second operand), copied into the factors after.
-//   gemm   A22 -= L21 U12 on the tensor cores (tcgen05, kind::tf32, FP32
-//          accumulation in tensor memory).  The complex product is one real
+//   gemm   A22 -= L21 U12 on the tensor cores (tcgen05, kind::f16 with FP16
+//          operands, FP32 accumulation in tensor memory).  FP16 keeps TF32's
+//          11-bit significand at half the operand bytes and twice the MMA
+//          rate; the panel GEMMs write FP16 copies of L21 (clamped to the FP16
+//          range) and of U12 scaled by a power of two per system (2^10 over
+//          the operator's largest entry, undone in the epilogue), so the
+//          entries that matter stay normal numbers.  The complex product is one real
 //          GEMM: with A' the 2m x 2k real matrix holding [[ar, -ai], [ai, ar]]
 //          per complex entry, A' times the natural real view of U12
 //          (2k x n, re/im interleaved along the rows, which is how the
@@ -37,6 +42,7 @@
 // preconditioner: the FP64 outer GMRES with exact residuals decides the
 // answer, the factors only decide the iteration count.
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -56,8 +62,10 @@ namespace {
 
 constexpr int LB = 128;                 // block size (complex unknowns)
 constexpr int GM = 128, GN = 256;       // GEMM tile: real rows x columns
-constexpr int GK = 32;                  // real K per pipeline chunk
+constexpr int GK = 32;                  // real K per pipeline chunk (FP32 operands, panel GEMMs)
 constexpr int GCHUNKS = 2 * LB / GK;    // 8 chunks: K = 256, one block step
+constexpr int GK16 = 64;                // real K per pipeline chunk (FP16 operands, trailing update)
+constexpr int GCHUNKS16 = 2 * LB / GK16;  // 4 chunks: K = 256, one block step
 constexpr int LU_GROUP = 4;             // block steps per delayed trailing update
 constexpr int WK = 2 * LB * LU_GROUP;   // panel workspace width: K = 1024 (the group's steps)
 constexpr int GS = 4;                   // pipeline stages
@@ -79,6 +87,11 @@ struct LuSys {
     const CUtensorMap* tmY;  // Y: n columns x WK floats, 32 x 256 boxes
     const CUtensorMap* tmL;  // Li: 256 rows, 32 x 128 boxes
     const CUtensorMap* tmU;  // UiT: 256 rows, 32 x 256 boxes
+    __half* W16;  // W after the L21 GEMM in FP16 (the trailing update's A operand)
+    __half* Y16;  // ysc Y in FP16 (its B operand)
+    const CUtensorMap* tmW16;  // W16: 2n rows x WK halves, 64 x 128 boxes
+    const CUtensorMap* tmY16;  // Y16: n columns x WK halves, 64 x 256 boxes
+    float ysc, yinv;  // power-of-two scale of Y16 and its inverse
     int64_t n, ld;
     int nblk, pad;
 };
@@ -369,6 +382,20 @@ __device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint6
         : "memory");
 }
 
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Instruction descriptor, kind::f16: FP16 A and B (format 0, both K-major), FP32 D.
+__host__ __device__ constexpr uint32_t umma_idesc_f16_f32(int M, int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
 // Instruction descriptor, kind::tf32: TF32 A and B (both K-major), FP32 D.
 __host__ __device__ constexpr uint32_t umma_idesc_tf32_f32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
@@ -396,6 +423,8 @@ struct GemmTile {
     const CUtensorMap *tmA, *tmB;
     int ax, ay, bx, by;  // tensor-copy coordinates of chunk 0 (x advances by GK per chunk)
     float *F, *Y, *W;
+    __half *Y16, *W16;
+    float ysc, yinv;
     int64_t n, ld, ld2, k0, ktw, row0, rows_end, col0, col_end;
 };
 
@@ -428,6 +457,10 @@ __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, con
     g.F = reinterpret_cast<float*>(S.F);
     g.Y = S.Y;
     g.W = S.W;
+    g.Y16 = S.Y16;
+    g.W16 = S.W16;
+    g.ysc = S.ysc;
+    g.yinv = S.yinv;
     g.n = S.n;
     g.ld = S.ld;
     g.ld2 = 2 * S.ld;
@@ -440,10 +473,10 @@ __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, con
         g.rows_end = w.r1;
         g.col0 = w.c0 + tj * GN;
         g.col_end = w.c1;
-        g.tmA = S.tmW;
+        g.tmA = S.tmW16;
         g.ax = 0;
         g.ay = (int)g.row0;
-        g.tmB = S.tmY;
+        g.tmB = S.tmY16;
         g.bx = 0;
         g.by = (int)g.col0;
     } else if (MODE == G_U12) {
@@ -527,8 +560,9 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                     }
                     const uint32_t As = base + st * GSTAGE, Bs = As + GA_BYTES;
                     mbar_arrive_expect_tx(&full[st], GSTAGE);
-                    tma_load_2d_hint(As, g.tmA, g.ax + c * GK, g.ay, &full[st], keep);
-                    tma_load_2d_hint(Bs, g.tmB, g.bx + c * GK, g.by, &full[st], keep);
+                    const int kx = c * (MODE == G_TRAIL ? GK16 : GK);  // 128 bytes per chunk row
+                    tma_load_2d_hint(As, g.tmA, g.ax + kx, g.ay, &full[st], keep);
+                    tma_load_2d_hint(Bs, g.tmB, g.bx + kx, g.by, &full[st], keep);
                 }
             }
             if (*abort_flag) {
@@ -540,7 +574,7 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
         __syncwarp();
     } else if (warp == 1) {
         // ---- MMA issuer
-        const uint32_t idesc = umma_idesc_tf32_f32(GM, GN);
+        const uint32_t idesc = MODE == G_TRAIL ? umma_idesc_f16_f32(GM, GN) : umma_idesc_tf32_f32(GM, GN);
         int64_t it = 0, tc = 0;
         for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, ++tc) {
             const int acc = (int)(tc & 1);
@@ -556,10 +590,17 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                     else {
                         tc_fence_after();
                         const uint32_t a = base + st * GSTAGE, b = a + GA_BYTES;
+                        // four MMAs per 128-byte chunk row: K = 8 (TF32) or 16 (FP16),
+                        // 32 bytes of the row each
 #pragma unroll
-                        for (int kk = 0; kk < GK / 8; ++kk)
-                            umma_tf32(tmem + (uint32_t)(acc * GN), umma_desc_sw128(a + kk * 32),
-                                      umma_desc_sw128(b + kk * 32), idesc, (c | kk) ? 1u : 0u);
+                        for (int kk = 0; kk < 4; ++kk) {
+                            if (MODE == G_TRAIL)
+                                umma_f16(tmem + (uint32_t)(acc * GN), umma_desc_sw128(a + kk * 32),
+                                         umma_desc_sw128(b + kk * 32), idesc, (c | kk) ? 1u : 0u);
+                            else
+                                umma_tf32(tmem + (uint32_t)(acc * GN), umma_desc_sw128(a + kk * 32),
+                                          umma_desc_sw128(b + kk * 32), idesc, (c | kk) ? 1u : 0u);
+                        }
                         umma_commit(&empty[st]);
                     }
                 }
@@ -604,13 +645,17 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                     for (int q = 0; q < 32; ++q) cv[q] = q < nq ? __ldcs(p0 + q * g.ld2) : 0.f;
 #pragma unroll
                     for (int q = 0; q < 32; ++q)
-                        if (q < nq) __stcs(p0 + q * g.ld2, cv[q] - v[q]);
+                        if (q < nq) __stcs(p0 + q * g.ld2, fmaf(-v[q], g.yinv, cv[q]));
                 } else if (MODE == G_U12) {
                     const int nq = (int)min((int64_t)32, g.col_end - jb);
                     float* p0 = g.Y + jb * WK + yoff + r;
+                    __half* h0 = g.Y16 + jb * WK + yoff + r;
 #pragma unroll
                     for (int q = 0; q < 32; ++q)
-                        if (q < nq) p0[q * WK] = v[q];
+                        if (q < nq) {
+                            p0[q * WK] = v[q];
+                            h0[q * WK] = __float2half_rn(fminf(fmaxf(v[q] * g.ysc, -65504.f), 65504.f));
+                        }
                 } else {
                     // L21: the embedded row back into W, and the natural
                     // entries (row 2i holds re, row 2i + 1 im of column 2p)
@@ -621,6 +666,18 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                     float4* wrow = reinterpret_cast<float4*>(g.W + r * WK + woff + cc * 32);
 #pragma unroll
                     for (int q = 0; q < 8; ++q) wrow[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                    uint4* hrow = reinterpret_cast<uint4*>(g.W16 + r * WK + woff + cc * 32);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        uint32_t h[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const __half2 x = __floats2half2_rn(fminf(fmaxf(v[8 * q + 2 * e], -65504.f), 65504.f),
+                                                                fminf(fmaxf(v[8 * q + 2 * e + 1], -65504.f), 65504.f));
+                            h[e] = *reinterpret_cast<const uint32_t*>(&x);
+                        }
+                        hrow[q] = make_uint4(h[0], h[1], h[2], h[3]);
+                    }
                     if ((lane & 1) == 0) {
                         const int64_t i = g.ktw + (r >> 1);
                         float2* F2 = reinterpret_cast<float2*>(g.F);
@@ -968,7 +1025,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     auto d = std::make_shared<LuData>();
     const int nsys = ws.bt.nsys;
     std::vector<GmView> v((size_t)nsys);
-    size_t entries = 0, dm = 0, wsz = 0, psz = 0;
+    size_t entries = 0, dm = 0, wsz = 0, psz = 0, hsz = 0;
     // split FP64 operators: each occupies two FP32 planes, of which the
     // factors copy the first (the operator's FP32 rounding) to half the offset
     const size_t fdiv = ws.bt.split_lo ? 2 : 1;
@@ -985,6 +1042,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         dm += (size_t)nb * LB * LB;
         wsz += (size_t)2 * v[(size_t)s].n * WK;
         psz += (size_t)2 * (2 * LB) * (2 * LB) + (size_t)WK * v[(size_t)s].n;
+        hsz += (size_t)3 * v[(size_t)s].n * WK;  // W16 (2n x WK) and Y16 (n x WK)
         d->nblk_max = std::max(d->nblk_max, nb);
     }
     // the factors, block inverses and panel workspace live in grow-only
@@ -993,6 +1051,12 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     c.w_lu_D.ensure(sizeof(float2) * std::max<size_t>(dm, 1));
     c.w_lu_W.ensure(sizeof(float) * std::max<size_t>(wsz, 4));
     c.w_lu_P.ensure(sizeof(float) * std::max<size_t>(psz, 4));
+    c.w_lu_H.ensure(sizeof(__half) * std::max<size_t>(hsz, 8));
+    // the FP16 copy of U12 is scaled by 2^10 over the operator's Frobenius
+    // norm (a bound on its largest entry; a power of two, so exact)
+    std::vector<double> anorm((size_t)nsys);
+    BEM_CUDA(cudaMemcpyAsync(anorm.data(), ws.anorm, sizeof(double) * nsys, cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
     if (ws.bt.split_lo) {
         // one copy per distinct operator (several right-hand sides share one)
         for (int s = 0; s < nsys; ++s) {
@@ -1025,7 +1089,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
             }
     }
     d->sys.resize((size_t)nsys);
-    constexpr int NMAP = 5;
+    constexpr int NMAP = 7;
     d->maps.ensure(sizeof(CUtensorMap) * NMAP * nsys);
     std::vector<CUtensorMap> maps((size_t)(NMAP * nsys));
     const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
@@ -1041,7 +1105,19 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         require(r == CUDA_SUCCESS, std::string("LU: tensor map of ") + what);
     };
-    size_t od = 0, ow = 0, op = 0;
+    // the same for FP16 with boxes of 64 halves x rows (128-byte rows)
+    auto map2d16 = [&](CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint64_t stride_halves,
+                       uint32_t box_rows, const char* what) {
+        const cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+        const cuuint64_t strides[1] = {(cuuint64_t)(stride_halves * sizeof(__half))};
+        const cuuint32_t box[2] = {(cuuint32_t)GK16, (cuuint32_t)box_rows};
+        const cuuint32_t es[2] = {1, 1};
+        const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+                                  es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        require(r == CUDA_SUCCESS, std::string("LU: tensor map of ") + what);
+    };
+    size_t od = 0, ow = 0, op = 0, oh = 0;
     for (int s = 0; s < nsys; ++s) {
         LuSys& L = d->sys[(size_t)s];
         if (owner[(size_t)s] != s) {
@@ -1057,21 +1133,33 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         L.Li = c.w_lu_P.as<float>() + op;
         L.UiT = L.Li + (2 * LB) * (2 * LB);
         L.Y = L.UiT + (2 * LB) * (2 * LB);
+        L.W16 = c.w_lu_H.as<__half>() + oh;
+        L.Y16 = L.W16 + (size_t)2 * L.n * WK;
+        const double an = anorm[(size_t)s];
+        const int e = (std::isfinite(an) && an > 0) ? std::max(-100, std::min(100, 10 - (int)std::ceil(std::log2(an))))
+                                                    : 0;
+        L.ysc = std::ldexp(1.0f, e);
+        L.yinv = std::ldexp(1.0f, -e);
         od += (size_t)L.nblk * LB * LB;
         ow += (size_t)2 * L.n * WK;
         op += (size_t)2 * (2 * LB) * (2 * LB) + (size_t)WK * L.n;
+        oh += (size_t)3 * L.n * WK;
         CUtensorMap* ms = maps.data() + (size_t)NMAP * s;
         map2d(ms + 0, L.W, WK, 2 * L.n, WK, GM, "the panel workspace");                // W
         map2d(ms + 1, L.F, 2 * L.n, L.n, 2 * L.ld, GN, "the factors");                 // F, natural real view
         map2d(ms + 2, L.Y, WK, L.n, WK, GN, "the row panel");                          // Y
         map2d(ms + 3, L.Li, 2 * LB, 2 * LB, 2 * LB, GM, "the lower inverse");          // Li
         map2d(ms + 4, L.UiT, 2 * LB, 2 * LB, 2 * LB, GN, "the upper inverse");         // UiT
+        map2d16(ms + 5, L.W16, WK, 2 * L.n, WK, GM, "the FP16 column panels");       // W16
+        map2d16(ms + 6, L.Y16, WK, L.n, WK, GN, "the FP16 row panels");              // Y16
         CUtensorMap* md = d->maps.as<CUtensorMap>() + (size_t)NMAP * s;
         L.tmW = md + 0;
         L.tmF = md + 1;
         L.tmY = md + 2;
         L.tmL = md + 3;
         L.tmU = md + 4;
+        L.tmW16 = md + 5;
+        L.tmY16 = md + 6;
     }
     BEM_CUDA(cudaMemcpyAsync(d->maps.p, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice,
                              c.stream));
@@ -1107,7 +1195,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
                 u12.push_back(Entry{s, 2 * ((mts + GN - 1) / GN), 0, 0, 0, kts, L.n});
                 copy.push_back(Entry{s, (mts + 31) / 32, 0, 0, 0, 0, 0});
             }
-            plan(LuData::TRAIL, st, k, 0, 0, GCHUNKS * j, thin);
+            plan(LuData::TRAIL, st, k, 0, 0, GCHUNKS16 * j, thin);
             plan(LuData::DIAG, st, k, 0, 0, 0, diag);
             plan(LuData::EXPAND, st, k, 2 * LB * j, 0, 0, expd);
             plan(LuData::L21, st, k, 2 * LB * j, 0, GCHUNKS, l21);
@@ -1121,7 +1209,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
             if (owner[(size_t)s] != s || c0 >= L.n) continue;
             rest.push_back(trail_entry(s, 2 * (LU_GROUP - 1) * LB, 2 * (L.n - ktw), c0, L.n));
         }
-        plan(LuData::TRAIL, k + LU_GROUP - 1, k, 0, 0, GCHUNKS * LU_GROUP, rest);
+        plan(LuData::TRAIL, k + LU_GROUP - 1, k, 0, 0, GCHUNKS16 * LU_GROUP, rest);
     }
     // substitution tickets: forward rows by ascending block, then backward
     // rows by descending block, the groups interleaved.  A group is up to
@@ -1247,7 +1335,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         c.stage_add("lu_panel_l21", tsum[LuData::L21], d->nblk_max, 0);
         c.stage_add("lu_panel_u12", tsum[LuData::U12], d->nblk_max, 0);
         c.stage_add("lu_panel_copy", tsum[LuData::COPY], d->nblk_max, 0);
-        c.stage_add("lu_gemm_tf32", tsum[LuData::TRAIL], d->nblk_max, fl);
+        c.stage_add("lu_gemm_trail", tsum[LuData::TRAIL], d->nblk_max, fl);
         cudaEventDestroy(ev0);
         cudaEventDestroy(ev1);
     }
@@ -1314,6 +1402,7 @@ extern "C" BEM_API bem_status bem_lu32_factor_apply(bem_ctx* ctx, int nsys, cons
         BEM_CUDA(cudaMemcpyAsync(dA.p, A, sizeof(float2) * (size_t)a_entries, cudaMemcpyHostToDevice, c.stream));
         GmWorkspace ws;
         gm_prepare_ragged(c, ws, ns, lds, offs, 1, dA.p, true);
+        gm_matrix_norms(c, ws);  // the scale of the FP16 row panels
         // every system active at Krylov step 0 (the state the application reads)
         BEM_CUDA(cudaMemsetAsync(ws.bt.st, 0, sizeof(GmState) * (size_t)nsys, c.stream));
         if (q) {

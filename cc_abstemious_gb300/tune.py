@@ -11,7 +11,7 @@ default's, so the gain of the table is on file.  A context reads the table
 (tuning.json beside the library) at creation.
 
   lu_gemm_trail  (sb_r, sb_c): tile raster of the TF32 trailing update (stage
-                 lu_gemm_tf32) -- mixed form with the LU preconditioner, one
+                 lu_gemm_trail) -- mixed form with the LU preconditioner, one
                  frequency of cube-spheres of 1944 .. 40344 quads, and a batch
                  of 64 perturbed spheres.
   gm_apply_fp32  unroll: columns per load batch of the Krylov mat-vec (stage
@@ -98,11 +98,11 @@ def main():
         def run(pd=pd, sc=sc, nf=nf):
             ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_MIXED, bem.PRECOND_LU, bem._ptr(sc), bem._ptr(sc),
                                       None, 0))
-        cases.append((pd.n, 1, ctx, run, "lu_gemm_tf32"))
+        cases.append((pd.n, 1, ctx, run, "lu_gemm_trail"))
     bodies = workloads.perturbed_spheres(wd, count=64, seed=3, nfreq=1, tol=1e-8)
     bpds = [bem.PreData.from_dict(d, ctx=ctx) for d in bodies]
     cases.append((int(max(p.n for p in bpds)), 64, ctx, lambda: bem.run_batch(bpds, precond="lu", ctx=ctx),
-                  "lu_gemm_tf32"))
+                  "lu_gemm_trail"))
     entries += sweep("lu_gemm_trail", [{"sb_r": r, "sb_c": c} for r, c in RASTERS], cases,
                      {"sb_r": 8, "sb_c": 32})
 
