@@ -196,7 +196,7 @@ def tensor_peak():
 def lu_traffic_ratio():
     """DRAM traffic / algorithmic A22 bytes of one K = 1024 trailing update, from
     the committed ncu summary (profiles/)."""
-    p = os.path.join(ROOT, "profiles", "lu_gemm_tf32_group_rigid_sphere.md")
+    p = os.path.join(ROOT, "profiles", "lu_gemm_trail_group_rigid_sphere.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -239,7 +239,7 @@ def lu_roofline(prof, sizes, what):
             "algorithmic_bytes_per_operator_launch": alg,
             "peak_kind": peak_kind,
             "traffic_note": "ncu dram read+write / algorithmic A22 bytes of one K = 1024 launch "
-                            "(profiles/lu_gemm_tf32_group_rigid_sphere.md), times the mean algorithmic bytes "
+                            "(profiles/lu_gemm_trail_group_rigid_sphere.md), times the mean algorithmic bytes "
                             "of this workload's K = 1024 launches, per operator"}
 
 
