@@ -565,7 +565,7 @@ def _pick_best(forms, tol=1e-6):
 
 class _Shared:
     """What the targets share in one run: the context, its stream, a work
-    directory, the cuBLAS TF32 peak (measured once) and the trained network."""
+    directory, and the trained network."""
 
     def __init__(self, args, local):
         import torch
@@ -773,7 +773,7 @@ def target_ellipsoid(sh):
     """Config 3: ellipsoid (2, 1, 0.5) m with 40960 triangles, Burton-Miller,
     a plane wave along a seeded direction and a point source at (0, 0, 3),
     ka (a = 2) 2.5..20 at 8 frequencies: 16 solves per step.  The forms solve
-    the dense operators with the TF32 LU preconditioner, both waves per
+    the dense operators with the tensor-core LU preconditioner, both waves per
     operator (extension key additional_incident_waves), GMRES at backward
     error 1e-8: mixed (FP32 operators) and, when its error exceeds 1e-6,
     refined (FP64 operators).  The plain FP64 denominator and the error

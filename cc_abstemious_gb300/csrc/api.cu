@@ -274,6 +274,8 @@ BEM_API bem_status bem_ctx_set_tuning(bem_ctx* ctx, const char* kernel, const ch
 
 BEM_API int bem_ctx_get_tuning(const bem_ctx* ctx, const char* kernel, const char* param, int64_t n, int64_t nsys) {
     if (!ctx || !kernel || !param) return -1;
+    // the LU step-group size: the rule of lu_group (8 from 12000 unknowns on)
+    if (std::string(kernel) == "lu_gemm_trail" && std::string(param) == "group") return lu_group(ctx->c, n, nsys);
     return ctx->c.tuning.pick(kernel, param, n, nsys, tuning_default(kernel, param));
 }
 

@@ -281,10 +281,12 @@ void run_mixed_batch(Context& c, const std::vector<Problem*>& probs, bem_precond
         std::vector<BodyPlan*> chunk;
         size_t bytes = 0;
         // the LU preconditioner keeps a factored copy of every operator and,
-        // per unknown, the diagonal blocks and the panel workspaces (19 KB)
+        // per unknown, the diagonal blocks and the panel workspaces (19 KB, or
+        // 38 KB where eight-step groups are allowed)
         auto need = [&](const BodyPlan* p) {
-            return precond == BEM_PRECOND_LU ? 2.0 * (double)p->op_bytes + 19600.0 * (double)p->n * (double)p->nf
-                                             : (double)p->op_bytes;
+            return precond == BEM_PRECOND_LU
+                       ? 2.0 * (double)p->op_bytes + lu_bytes_per_unknown(p->n) * (double)p->n * (double)p->nf
+                       : (double)p->op_bytes;
         };
         while (i < batched.size() && (chunk.empty() || (double)bytes + need(batched[i]) <= (double)budget_bytes)) {
             bytes += (size_t)need(batched[i]);

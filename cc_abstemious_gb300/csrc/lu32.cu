@@ -3,7 +3,7 @@
 // Every operator of the batch (FP32 complex, column-major) is copied and
 // factored A = L U without pivoting, in blocks of LB = 128 unknowns, all
 // systems of a (possibly ragged) batch advancing block step k together, the
-// trailing updates delayed over groups of LU_GROUP steps:
+// trailing updates delayed over groups of G steps (4 or 8, by size):
 //
 //   diag   one CTA per system: L11^-1 and U11^-1 of the diagonal block in one
 //          register-tiled elimination sweep (tiny pivots are replaced and
@@ -66,8 +66,16 @@ constexpr int GK = 32;                  // real K per pipeline chunk (FP32 opera
 constexpr int GCHUNKS = 2 * LB / GK;    // 8 chunks: K = 256, one block step
 constexpr int GK16 = 64;                // real K per pipeline chunk (FP16 operands, trailing update)
 constexpr int GCHUNKS16 = 2 * LB / GK16;  // 4 chunks: K = 256, one block step
-constexpr int LU_GROUP = 4;             // block steps per delayed trailing update
-constexpr int WK = 2 * LB * LU_GROUP;   // panel workspace width: K = 1024 (the group's steps)
+// Block steps per delayed trailing update (a factorization's group size G):
+// the panel workspace is WK = 2 LB G wide (K = 256 G per pass over A22).
+// Eight steps halve the A22 traffic per flop of four at twice the workspace
+// and longer in-group updates, which pay off for large systems only.
+constexpr int LU_GROUP_MAX = 8;
+}  // namespace
+// smallest system size for which eight-step groups are allowed (the memory
+// budgets of the batched forms reserve their workspace from this size on)
+constexpr int64_t LU_GROUP8_MIN_N = 4096;
+namespace {
 constexpr int GS = 4;                   // pipeline stages
 constexpr int GTHREADS = 320;           // producer warp, MMA warp, eight epilogue warps
 constexpr int GEPI = GTHREADS - 64;     // epilogue threads
@@ -93,7 +101,7 @@ struct LuSys {
     const CUtensorMap* tmY16;  // Y16: n columns x WK halves, 64 x 256 boxes
     float ysc, yinv;  // power-of-two scale of Y16 and its inverse
     int64_t n, ld;
-    int nblk, pad;
+    int nblk, wk;     // blocks; panel workspace width 2 LB G
 };
 
 // One entry per (system, launch): the system, its first CTA in the flattened
@@ -307,8 +315,8 @@ __global__ void __launch_bounds__(256) lu_expand_kernel(const LuSys* __restrict_
     for (int t = threadIdx.x; t < nrow * LB; t += blockDim.x) {
         const int i = t / LB, c = t % LB;
         const float2 v = Y[c * 65 + i];
-        float2* w0 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i) * WK + woff);
-        float2* w1 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i + 1) * WK + woff);
+        float2* w0 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i) * S.wk + woff);
+        float2* w1 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i + 1) * S.wk + woff);
         w0[c] = make_float2(v.x, -v.y);
         w1[c] = make_float2(v.y, v.x);
     }
@@ -324,24 +332,16 @@ __global__ void __launch_bounds__(256) lu_copy_u12_kernel(const LuSys* __restric
     const int ncol = (int)min((int64_t)32, S.n - j0);
     for (int t = threadIdx.x; t < ncol * (LB / 2); t += blockDim.x) {
         const int c = t / (LB / 2), q = t % (LB / 2);  // 64 float4 per column
-        const float4 v = reinterpret_cast<const float4*>(S.Y + (j0 + c) * WK + yoff)[q];
+        const float4 v = reinterpret_cast<const float4*>(S.Y + (j0 + c) * S.wk + yoff)[q];
         reinterpret_cast<float4*>(S.F + (j0 + c) * S.ld + k0)[q] = v;
     }
 }
 
 // ---------------------------------------------------------------------------
 // Trailing update on the tensor cores.
-// 2-D tensor copy global -> shared (tensor map in global memory), completing
-// on the mbarrier.
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* tmap, int x, int y, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            dst),
-        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
-}
 
-// The same copy with an L2 eviction policy (createpolicy): the GEMM operands
+// 2-D tensor copy global -> shared (tensor map in global memory), completing
+// on the mbarrier, with an L2 eviction policy (createpolicy): the GEMM operands
 // are panels that every tile of a launch re-reads, so they are kept in L2
 // (evict_last) while the trailing block streams past them.
 __device__ __forceinline__ uint64_t l2_policy_evict_last() {
@@ -425,7 +425,7 @@ struct GemmTile {
     float *F, *Y, *W;
     __half *Y16, *W16;
     float ysc, yinv;
-    int64_t n, ld, ld2, k0, ktw, row0, rows_end, col0, col_end;
+    int64_t n, ld, ld2, k0, ktw, row0, rows_end, col0, col_end, wk;
 };
 
 // Raster of a TRAIL region's tiles (tiles_i row tiles x tiles_j column
@@ -461,6 +461,7 @@ __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, con
     g.W16 = S.W16;
     g.ysc = S.ysc;
     g.yinv = S.yinv;
+    g.wk = S.wk;
     g.n = S.n;
     g.ld = S.ld;
     g.ld2 = 2 * S.ld;
@@ -648,13 +649,13 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                         if (q < nq) __stcs(p0 + q * g.ld2, fmaf(-v[q], g.yinv, cv[q]));
                 } else if (MODE == G_U12) {
                     const int nq = (int)min((int64_t)32, g.col_end - jb);
-                    float* p0 = g.Y + jb * WK + yoff + r;
-                    __half* h0 = g.Y16 + jb * WK + yoff + r;
+                    float* p0 = g.Y + jb * g.wk + yoff + r;
+                    __half* h0 = g.Y16 + jb * g.wk + yoff + r;
 #pragma unroll
                     for (int q = 0; q < 32; ++q)
                         if (q < nq) {
-                            p0[q * WK] = v[q];
-                            h0[q * WK] = __float2half_rn(fminf(fmaxf(v[q] * g.ysc, -65504.f), 65504.f));
+                            p0[q * g.wk] = v[q];
+                            h0[q * g.wk] = __float2half_rn(fminf(fmaxf(v[q] * g.ysc, -65504.f), 65504.f));
                         }
                 } else {
                     // L21: the embedded row back into W, and the natural
@@ -663,10 +664,10 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
 #pragma unroll
                     for (int q = 0; q < 16; ++q) im[q] = __shfl_down_sync(0xffffffffu, v[2 * q], 1);
                     if (!rok) continue;
-                    float4* wrow = reinterpret_cast<float4*>(g.W + r * WK + woff + cc * 32);
+                    float4* wrow = reinterpret_cast<float4*>(g.W + r * g.wk + woff + cc * 32);
 #pragma unroll
                     for (int q = 0; q < 8; ++q) wrow[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-                    uint4* hrow = reinterpret_cast<uint4*>(g.W16 + r * WK + woff + cc * 32);
+                    uint4* hrow = reinterpret_cast<uint4*>(g.W16 + r * g.wk + woff + cc * 32);
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         uint32_t h[4];
@@ -928,6 +929,7 @@ struct LuData {
     DevBuf sysbuf, work, info, maps;
     std::vector<LuSys> sys;
     int nblk_max = 0;
+    int group = 4;  // block steps per delayed trailing update
     // work lists: per launch, [offset, count, ctas] into `work`
     struct Seg {
         int64_t off = 0;
@@ -1014,6 +1016,20 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
+int lu_group(const Context& c, int64_t nmin, int64_t nsys) {
+    // eight steps only where every factored system is large: the workspace
+    // doubles and the in-group updates of a small system grow with G^2
+    const int g = c.tuning.pick("lu_gemm_trail", "group", nmin, nsys, nmin >= 12000 ? 8 : 4);
+    return (g >= 8 && nmin >= LU_GROUP8_MIN_N) ? 8 : 4;
+}
+
+double lu_bytes_per_unknown(int64_t n) {
+    // W (2 WK floats), Y (WK floats), their FP16 copies (3 WK halves) and the
+    // diagonal-block inverses (LB complex floats) per unknown
+    const double wk = 2.0 * LB * (n >= LU_GROUP8_MIN_N ? LU_GROUP_MAX : 4);
+    return 18.0 * wk + 8.0 * LB + 64.0;
+}
+
 // Factors every operator of the batch and installs the preconditioner hook.
 void lu_precond_setup(Context& c, GmWorkspace& ws) {
     cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -1029,6 +1045,15 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     // split FP64 operators: each occupies two FP32 planes, of which the
     // factors copy the first (the operator's FP32 rounding) to half the offset
     const size_t fdiv = ws.bt.split_lo ? 2 : 1;
+    int64_t nmin = INT64_MAX, nmax_all = 0;
+    for (int s = 0; s < nsys; ++s) {
+        const int64_t ns_ = ws.sys_host.empty() ? ws.bt.n : ws.sys_host[(size_t)s].n;
+        nmin = std::min(nmin, ns_);
+        nmax_all = std::max(nmax_all, ns_);
+    }
+    const int G = lu_group(c, nmin, nsys);
+    const int WK = 2 * LB * G;
+    d->group = G;
     for (int s = 0; s < nsys; ++s) {
         v[(size_t)s] = ws.sys_host.empty() ? gm_view(ws.bt, s) : GmView{};
         if (!ws.sys_host.empty()) {
@@ -1140,6 +1165,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
                                                     : 0;
         L.ysc = std::ldexp(1.0f, e);
         L.yinv = std::ldexp(1.0f, -e);
+        L.wk = WK;
         od += (size_t)L.nblk * LB * LB;
         ow += (size_t)2 * L.n * WK;
         op += (size_t)2 * (2 * LB) * (2 * LB) + (size_t)WK * L.n;
@@ -1174,9 +1200,9 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         LuData::Launch l{kind, ks, kw, woff, yoff, nchunks, add_segment(*d, e)};
         if (l.seg.ctas) d->plan.push_back(l);
     };
-    for (int k = 0; k < d->nblk_max; k += LU_GROUP) {
+    for (int k = 0; k < d->nblk_max; k += G) {
         const int64_t ktw = (int64_t)(k + 1) * LB;  // trailing origin of the group: W row 0
-        for (int j = 0; j < LU_GROUP; ++j) {
+        for (int j = 0; j < G; ++j) {
             const int st = k + j;
             std::vector<Entry> thin, diag, expd, l21, u12, copy;
             for (int s = 0; s < nsys; ++s) {
@@ -1205,11 +1231,11 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         std::vector<Entry> rest;
         for (int s = 0; s < nsys; ++s) {
             const LuSys& L = d->sys[(size_t)s];
-            const int64_t c0 = (int64_t)(k + LU_GROUP) * LB;
+            const int64_t c0 = (int64_t)(k + G) * LB;
             if (owner[(size_t)s] != s || c0 >= L.n) continue;
-            rest.push_back(trail_entry(s, 2 * (LU_GROUP - 1) * LB, 2 * (L.n - ktw), c0, L.n));
+            rest.push_back(trail_entry(s, 2 * (G - 1) * LB, 2 * (L.n - ktw), c0, L.n));
         }
-        plan(LuData::TRAIL, k + LU_GROUP - 1, k, 0, 0, GCHUNKS16 * LU_GROUP, rest);
+        plan(LuData::TRAIL, k + G - 1, k, 0, 0, GCHUNKS16 * G, rest);
     }
     // substitution tickets: forward rows by ascending block, then backward
     // rows by descending block, the groups interleaved.  A group is up to

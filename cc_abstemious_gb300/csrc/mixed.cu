@@ -316,7 +316,7 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     // device memory the context can use
     const bool op64 = fp64_operator || (p.in.method_type == 0 && p.in.bc_type == 0);
     const double ent = (double)p.geo.npad * (double)n;
-    const double per = ent * (op64 ? 16.0 : 8.0) + (precond == BEM_PRECOND_LU ? ent * 8.0 + 19600.0 * n : 0.0);
+    const double per = ent * (op64 ? 16.0 : 8.0) + (precond == BEM_PRECOND_LU ? ent * 8.0 + lu_bytes_per_unknown(n) * n : 0.0);
     size_t fr = 0, tot = 0;
     BEM_CUDA(cudaMemGetInfo(&fr, &tot));
     const double budget = 0.6 * (double)(fr + c.w_mat.bytes + c.w_lu_F.bytes);

@@ -44,7 +44,15 @@ void near_pattern(const Forest& F, int body, NearPattern& P, bool diag_only);
 // Installs the preconditioner on the batch; returns the kind actually used
 // (the learned form falls back to block-Jacobi when no network is available).
 bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks);
-// TF32 tensor-core LU of every FP32 operator of the batch (lu32.cu).
+// Block steps per delayed trailing update of an LU factorization whose
+// smallest system has nmin unknowns (4 or 8; the tuning table may choose 4
+// where 8 is the default and 8 only from 4096 unknowns on).
+int lu_group(const Context& c, int64_t nmin, int64_t nsys);
+// Device bytes of the LU workspace per unknown of a system of n unknowns,
+// beyond its FP32 factors (the most its group size may need).
+double lu_bytes_per_unknown(int64_t n);
+// Tensor-core LU of every operator of the batch, factored from its FP32
+// rounding (lu32.cu).
 void lu_precond_setup(Context& c, GmWorkspace& ws);
 // Several bodies in a ragged batch: system s belongs to bodies[sys_body[s]].
 bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies, const std::vector<int>& sys_body,

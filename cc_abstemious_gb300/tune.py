@@ -10,7 +10,7 @@ table entry; the entry also records every candidate's time and the built-in
 default's, so the gain of the table is on file.  A context reads the table
 (tuning.json beside the library) at creation.
 
-  lu_gemm_trail  (sb_r, sb_c): tile raster of the TF32 trailing update (stage
+  lu_gemm_trail  (sb_r, sb_c): tile raster of the trailing update (stage
                  lu_gemm_trail) -- mixed form with the LU preconditioner, one
                  frequency of cube-spheres of 1944 .. 40344 quads, and a batch
                  of 64 perturbed spheres.

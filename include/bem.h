@@ -57,11 +57,13 @@ typedef enum { BEM_SIDE_RHS = 0, BEM_SIDE_LHS = 1 } bem_side;
  *              reduction, FP64 restarted GMRES over the FP32 operator with
  *              compensated mat-vecs, optional preconditioner; each result
  *              reports its error against an FP64 LU when requested.
- *  REFINED:    as MIXED, but every operator is assembled and kept in FP64
- *              (residuals and the answer at FP64 accuracy; for operators whose
- *              condition number makes FP32 storage miss 1e-6), while the
- *              preconditioner is built from its FP32 rounding (the TF32
- *              tensor-core LU of BEM_PRECOND_LU). */
+ *  REFINED:    as MIXED, but every operator is carried at FP64 accuracy
+ *              (assembled in float-float and stored as its FP32 rounding plus
+ *              the FP32 remainder, applied in float-float: residuals and the
+ *              answer at FP64 accuracy, for operators whose condition number
+ *              makes FP32 storage miss 1e-6), while the preconditioner is
+ *              built from its FP32 rounding (the tensor-core LU of
+ *              BEM_PRECOND_LU). */
 typedef enum { BEM_FORM_PLAIN_FP64 = 0, BEM_FORM_MIXED = 1, BEM_FORM_REFINED = 2 } bem_form;
 
 /* Preconditioners of the mixed form (no counterpart in the reference, whose
@@ -71,10 +73,11 @@ typedef enum { BEM_FORM_PLAIN_FP64 = 0, BEM_FORM_MIXED = 1, BEM_FORM_REFINED = 2
  *  BLOCK_JACOBI: inverses of the diagonal cluster-leaf blocks.
  *  LEARNED:      block-Jacobi plus a network-predicted near-field correction
  *                (falls back to BLOCK_JACOBI without a trained network).
- *  LU:           a TF32 tensor-core LU (no pivoting) of each FP32 operator,
- *                applied by blocked triangular solves; for hard systems (high
- *                frequency, fine meshes) where GMRES alone stalls.  FP32
- *                operators only (none for first-kind operators). */
+ *  LU:           a tensor-core LU (no pivoting) of each operator's FP32
+ *                rounding (TF32 panels, FP16 trailing updates with FP32
+ *                accumulation), applied by blocked triangular solves; for
+ *                hard systems (high frequency, fine meshes) where GMRES
+ *                alone stalls. */
 typedef enum {
     BEM_PRECOND_NONE = 0,
     BEM_PRECOND_BLOCK_JACOBI = 1,
@@ -333,7 +336,7 @@ BEM_API bem_status bem_learned_mlp_eval(bem_ctx* ctx, int64_t P, const float* fe
 BEM_API bem_status bem_learned_mlp_infer(bem_ctx* ctx, int64_t P, const float* features, float* out);
 
 /* ---- LU preconditioner kernels (instrumentation; no reference counterpart) */
-/* The LU preconditioner's factorization (TF32 tensor-core trailing updates,
+/* The LU preconditioner's factorization (tensor-core panel and trailing updates,
  * no pivoting, blocks of 128) and one application z = U^-1 L^-1 q, on
  * caller-given operators, with everything read back, so the device kernels
  * can be compared entry by entry with an FP64 LU.  System s has n[s] unknowns

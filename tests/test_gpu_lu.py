@@ -1,5 +1,5 @@
 """LU preconditioner of the mixed form: FP32 operators factored without
-pivoting (TF32 tensor-core trailing updates), applied by blocked triangular
+pivoting (tensor-core panel and FP16 trailing updates), applied by blocked triangular
 solves inside the FP64 GMRES.  The answer is decided by the FP64 residual, so
 the checks are: every solve within 1e-6 of an FP64 LU, and far fewer
 iterations than without a preconditioner."""
@@ -106,7 +106,7 @@ def test_lu_first_kind(ctx, wd):
 
 
 def test_refined_form(ctx, wd):
-    """FP64 operator + TF32 LU preconditioner: FP64-level agreement with the
+    """Operator at FP64 accuracy + tensor-core LU preconditioner: FP64-level agreement with the
     FP64 LU where the FP32 operator of the mixed form stops near 1e-7."""
     inp = workloads.perturbed_sphere_input(wd, 12, 2500, [4.0, 9.0], tol=1e-11)
     a = bem.Analysis(ctx)

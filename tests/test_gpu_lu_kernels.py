@@ -1,6 +1,6 @@
 """The LU preconditioner's kernels checked entry by entry (csrc/lu32.cu):
 lu_diag_kernel (diagonal-block inverses), lu_gemm_kernel in its three modes
-(TF32 tcgen05 trailing update, L21 and U12 panels) with the expand / copy
+(tcgen05 trailing update on FP16 operands, TF32 L21 and U12 panels) with the expand / copy
 kernels around them, and lu_trsv_kernel (one-launch block substitutions, one
 to four right-hand sides per operator).
 
@@ -8,8 +8,8 @@ bem_lu32_factor_apply runs the same factorization and application as the
 mixed form's BEM_PRECOND_LU on caller-given FP32 operators and returns the
 factors.  They are compared with an FP64 no-pivot LU of the same FP32
 matrices: per 128 x 128 block, the relative Frobenius error of the factors
-must stay at the TF32 level (the emulated TF32 algorithm gives ~1e-3; the
-bound is 5e-3), while a tile shifted by one row or column gives O(1) -- the
+must stay at the level of an 11-bit significand (TF32 and FP16 both carry
+one; the emulated TF32 algorithm gives ~1e-3; the bound is 5e-3), while a tile shifted by one row or column gives O(1) -- the
 CPU test at the end plants such a shift in the expected factors and checks
 that the comparison rejects it.  The substitutions are checked against the
 same block recurrences evaluated in FP64 on the returned factors (FP32
@@ -248,6 +248,24 @@ def test_factors_single_operator(ctx, n):
     (1100)."""
     a = operator(n, n)
     (res,), piv = factor_apply(ctx, [a], [1])
+    assert piv == 0
+    check_operator(a, *res)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("group", [4, 8])
+def test_factors_step_groups_of_eight(ctx, group):
+    """Systems from 4096 unknowns on may take eight block steps per pass over
+    A22 (K = 2048): 4600 unknowns (36 blocks, the last partial: groups of
+    8 + 8 + 8 + 8 + 4) factored with both group sizes, through the tuning
+    table's override."""
+    n = 4600
+    a = operator(n, 5)
+    ctx.check(ctx.lib.bem_ctx_set_tuning(ctx.h, b"lu_gemm_trail", b"group", group))
+    try:
+        (res,), piv = factor_apply(ctx, [a], [2], seed=9)
+    finally:
+        ctx.check(ctx.lib.bem_ctx_set_tuning(ctx.h, b"lu_gemm_trail", b"group", -1))
     assert piv == 0
     check_operator(a, *res)
 
