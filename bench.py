@@ -775,8 +775,9 @@ def target_ellipsoid(sh):
     ka (a = 2) 2.5..20 at 8 frequencies: 16 solves per step.  The forms solve
     the dense operators with the tensor-core LU preconditioner, both waves per
     operator (extension key additional_incident_waves), GMRES at backward
-    error 1e-8: mixed (FP32 operators) and, when its error exceeds 1e-6,
-    refined (FP64 operators).  The plain FP64 denominator and the error
+    error 1e-8, in order of cost until one meets 1e-6: mixed (FP32 operators
+    of the single-precision assembly), mixed_rounded (FP32 operators rounded
+    once from float-float values) and refined (operators at FP64 accuracy).  The plain FP64 denominator and the error
     reference are the reference's dense solver (FP64 partial-pivot LU, both
     waves from one factorization) at the lowest and highest ka."""
     import numpy as np
@@ -811,7 +812,8 @@ def target_ellipsoid(sh):
              "note": "the input's own solver (H-matrix, leaf 64, eta 1, ACA 1e-5, GMRES(32) tol 1e-6) does not "
                      "converge on this body (992 iterations at every frequency)"}
     forms = {}
-    for name, form in (("mixed+lu", bem.FORM_MIXED), ("refined+lu", bem.FORM_REFINED)):
+    codes = {"mixed+lu": bem.FORM_MIXED, "mixed_rounded+lu": bem.FORM_MIXED_ROUNDED, "refined+lu": bem.FORM_REFINED}
+    for name, form in codes.items():
         reps = (bem.SolveReport * (R * nf))()
 
         def step():
@@ -827,11 +829,11 @@ def target_ellipsoid(sh):
                        "gpu_launches": launches, "iterations": [reps[i].iterations for i in range(R * nf)],
                        "converged": all(reps[i].flag == 1 for i in range(R * nf)), "rel_err_vs_fp64_lu": errs,
                        "max_rel_err_vs_fp64_lu": max(errs.values())}
-        if name == "mixed+lu" and forms[name]["converged"] and forms[name]["max_rel_err_vs_fp64_lu"] <= 1e-6:
-            break  # the refined form is only needed when the mixed one misses 1e-6
+        if forms[name]["converged"] and forms[name]["max_rel_err_vs_fp64_lu"] <= 1e-6:
+            break  # the costlier forms are only needed when this one misses 1e-6
     best = _pick_best(forms)
     ctx.set_profiling(True)
-    ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_REFINED if best == "refined+lu" else bem.FORM_MIXED, 3,
+    ctx.check(ctx.lib.bem_run(ctx.h, pd.h, codes[best or "refined+lu"], 3,
                               bem._ptr(out), bem._ptr(inc), (bem.SolveReport * (R * nf))(), 0))
     prof = ctx.profile()
     ctx.set_profiling(False)

@@ -18,8 +18,8 @@ import os
 import numpy as np
 
 from . import _lib
-from ._lib import (BemError, FORM_MIXED, FORM_PLAIN_FP64, FORM_REFINED, MEM_DEVICE, MEM_HOST, PRECOND_BLOCK_JACOBI,
-                   PRECOND_LEARNED, PRECOND_LU, PRECOND_NONE, SIDE_LHS, SIDE_RHS, SolveReport)
+from ._lib import (BemError, FORM_MIXED, FORM_MIXED_ROUNDED, FORM_PLAIN_FP64, FORM_REFINED, MEM_DEVICE, MEM_HOST,
+                   PRECOND_BLOCK_JACOBI, PRECOND_LEARNED, PRECOND_LU, PRECOND_NONE, SIDE_LHS, SIDE_RHS, SolveReport)
 
 __all__ = ["Analysis", "Context", "PreData", "FPResult", "BemError", "get_dense_surface_matrices",
            "get_dense_field_matrices", "get_surface_row_or_column", "get_incident_surface", "get_incident_field",
@@ -368,7 +368,8 @@ class Analysis:
         sc = np.zeros((R * nf, max(nfp, 1)), dtype=np.complex128)
         inc = np.zeros((R * nf, max(nfp, 1)), dtype=np.complex128)
         reps = (SolveReport * max(R * nf, 1))()
-        f = {"plain": FORM_PLAIN_FP64, "mixed": FORM_MIXED, "refined": FORM_REFINED}[form]
+        f = {"plain": FORM_PLAIN_FP64, "mixed": FORM_MIXED, "refined": FORM_REFINED,
+             "mixed_rounded": FORM_MIXED_ROUNDED}[form]
         pc = {None: PRECOND_NONE, "none": PRECOND_NONE, "block_jacobi": PRECOND_BLOCK_JACOBI,
               "learned": PRECOND_LEARNED, "lu": PRECOND_LU}[precond]
         st = ctx.lib.bem_run(ctx.h, pd.h, f, pc, _ptr(sc), _ptr(inc), reps, 1 if check_vs_lu else 0)
@@ -442,12 +443,13 @@ def run_batch(predatas, precond=None, check_vs_lu=False, max_operator_bytes=0, c
 def assemble_operator(pd, kind="split", f0=0, nf=None):
     """The operators A_f = alpha_f H_f + beta_f G_f of frequencies f0 ..
     f0 + nf - 1 of a problem as the batched forms assemble them: kind "fp32"
-    (the mixed form) or "split" (the refined form: FP32 rounding plus FP32
-    remainder, returned summed in FP64).  Returns an (nf, n, n) array."""
+    (the mixed form), "split" (the refined form: FP32 rounding plus FP32
+    remainder, returned summed in FP64) or "rounded" (the mixed_rounded form:
+    that FP32 rounding alone).  Returns an (nf, n, n) array."""
     nf = len(pd.frequencies) - f0 if nf is None else nf
     n = pd.n
     A = np.zeros((nf, n, n), dtype=np.complex128)  # each [f] holds A_f^T (column-major fill)
-    k = {"fp32": 0, "split": 1}[kind]
+    k = {"fp32": 0, "split": 1, "rounded": 2}[kind]
     pd.ctx.check(pd.ctx.lib.bem_assemble_operator(pd.ctx.h, pd.h, k, f0, nf, _ptr(A), n))
     return np.ascontiguousarray(np.transpose(A, (0, 2, 1)))
 

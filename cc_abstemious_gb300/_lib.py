@@ -14,7 +14,7 @@ STATUS_NAMES = {0: "OK", 1: "BAD_INPUT", 2: "SINGULAR", 3: "NOT_CONVERGED", 4: "
                 7: "TIMEOUT"}
 MEM_HOST, MEM_DEVICE = 0, 1
 SIDE_RHS, SIDE_LHS = 0, 1
-FORM_PLAIN_FP64, FORM_MIXED, FORM_REFINED = 0, 1, 2
+FORM_PLAIN_FP64, FORM_MIXED, FORM_REFINED, FORM_MIXED_ROUNDED = 0, 1, 2, 3
 PRECOND_NONE, PRECOND_BLOCK_JACOBI, PRECOND_LEARNED, PRECOND_LU = 0, 1, 2, 3
 
 

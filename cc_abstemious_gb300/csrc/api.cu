@@ -427,7 +427,7 @@ BEM_API bem_status bem_get_dense_surface_matrices(bem_ctx* ctx, const bem_proble
 
 BEM_API bem_status bem_assemble_operator(bem_ctx* ctx, const bem_problem* pp, int kind, int64_t f0, int64_t nf,
                                          bem_cplx* A, int64_t lda) {
-    if (!ctx || !pp || !A || (kind != 0 && kind != 1)) return BEM_ERR_BAD_INPUT;
+    if (!ctx || !pp || !A || kind < 0 || kind > 2) return BEM_ERR_BAD_INPUT;
     return guard(ctx, [&] {
         Context& c = ctx->c;
         Problem& p = const_cast<Problem&>(pp->p);
@@ -447,24 +447,25 @@ BEM_API bem_status bem_assemble_operator(bem_ctx* ctx, const bem_problem* pp, in
         p.ifreq = saved;
         const size_t plane = (size_t)ld * n;
         DevBuf d, norms;
-        d.ensure(sizeof(float2) * plane * (kind ? 2 : 1) * (size_t)nf);
+        const bool two = kind == 1;  // the split store has a remainder plane
+        d.ensure(sizeof(float2) * plane * (two ? 2 : 1) * (size_t)nf);
         norms.ensure(sizeof(double) * (size_t)nf);
         if (kind == 0)
             assemble_system_fp32_body(c, p, ks.data(), al.data(), be.data(), ga.data(), de.data(), (int)nf,
                                       d.as<float2>(), ld, plane, nullptr, 0, norms.as<double>());
         else
             assemble_system_split(c, p, ks.data(), al.data(), be.data(), (int)nf, d.as<float2>(), ld, plane,
-                                  norms.as<double>());
-        std::vector<float2> h(plane * (kind ? 2 : 1) * (size_t)nf);
+                                  norms.as<double>(), two);
+        std::vector<float2> h(plane * (two ? 2 : 1) * (size_t)nf);
         BEM_CUDA(cudaMemcpyAsync(h.data(), d.p, sizeof(float2) * h.size(), cudaMemcpyDeviceToHost, c.stream));
         c.sync();
-        const size_t sstride = plane * (kind ? 2 : 1);
+        const size_t sstride = plane * (two ? 2 : 1);
         for (int64_t f = 0; f < nf; ++f)
             for (int64_t j = 0; j < n; ++j)
                 for (int64_t i = 0; i < n; ++i) {
                     const size_t o = (size_t)f * sstride + (size_t)j * ld + i;
                     double re = h[o].x, im = h[o].y;
-                    if (kind) {
+                    if (two) {
                         re += (double)h[o + plane].x;
                         im += (double)h[o + plane].y;
                     }
@@ -787,8 +788,9 @@ BEM_API bem_status bem_run(bem_ctx* ctx, bem_problem* pp, bem_form form, bem_pre
                 std::memset(&reports[f], 0, sizeof(bem_solve_report));
                 reports[f].rel_err_vs_lu = -1;
             }
-        if (form == BEM_FORM_MIXED || form == BEM_FORM_REFINED) {
-            run_mixed(c, p, precond, scattered, incident, reports, check_vs_lu != 0, form == BEM_FORM_REFINED);
+        if (form == BEM_FORM_MIXED || form == BEM_FORM_REFINED || form == BEM_FORM_MIXED_ROUNDED) {
+            run_mixed(c, p, precond, scattered, incident, reports, check_vs_lu != 0, form == BEM_FORM_REFINED,
+                      form == BEM_FORM_MIXED_ROUNDED);
             return;
         }
         // analysis.rs:87-111, one frequency at a time

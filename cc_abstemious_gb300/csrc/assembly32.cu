@@ -435,6 +435,7 @@ struct AsmFFParams {
 
 __device__ __forceinline__ ff ffd(float h, float l) { return ff{h, l}; }
 
+template <bool SPLIT>
 __global__ void __launch_bounds__(ASM_THREADS, 2) assemble_ff_kernel(int64_t n, int64_t npad,
                                                                     const float* __restrict__ g32,
                                                                     const double* __restrict__ geo, AsmFFParams prm,
@@ -488,8 +489,9 @@ __global__ void __launch_bounds__(ASM_THREADS, 2) assemble_ff_kernel(int64_t n, 
                 cfma(a, prm.s[s].beta_d, g);
                 const float hx = __double2float_rn(a.x), hy = __double2float_rn(a.y);
                 A[s * stride + o] = make_float2(hx, hy);
-                A[s * stride + o + plane] =
-                    make_float2(__double2float_rn(a.x - (double)hx), __double2float_rn(a.y - (double)hy));
+                if (SPLIT)
+                    A[s * stride + o + plane] =
+                        make_float2(__double2float_rn(a.x - (double)hx), __double2float_rn(a.y - (double)hy));
                 nrm[s] += hx * hx + hy * hy;
             }
             continue;
@@ -534,7 +536,7 @@ __global__ void __launch_bounds__(ASM_THREADS, 2) assemble_ff_kernel(int64_t n, 
             cff a = S.alpha_one ? h : S.alpha * h;
             if (!S.beta_zero) a = a + S.beta * g;
             A[s * stride + o] = make_float2(a.re.h, a.im.h);
-            A[s * stride + o + plane] = make_float2(a.re.l, a.im.l);
+            if (SPLIT) A[s * stride + o + plane] = make_float2(a.re.l, a.im.l);
             nrm[s] += a.re.h * a.re.h + a.im.h * a.im.h;
         }
     }
@@ -560,7 +562,7 @@ static ff host_ff(double v) {
 }
 
 void assemble_system_split(Context& ctx, const Problem& p, const double* ks, const cd* alphas, const cd* betas,
-                           int nsys, float2* A, int64_t ld, size_t plane, double* norms) {
+                           int nsys, float2* A, int64_t ld, size_t plane, double* norms, bool remainder) {
     require(plane == (size_t)ld * p.n, "split assembly: planes must be ld * n entries");
     int* err = device_err(ctx);
     BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx.stream));
@@ -601,9 +603,17 @@ void assemble_system_split(Context& ctx, const Problem& p, const double* ks, con
         prm.k0 = host_ff(k0);
         prm.dk = host_ff(dk);
         dim3 grid((unsigned)ntiles, (unsigned)ntiles);
-        assemble_ff_kernel<<<grid, ASM_THREADS, 0, ctx.stream>>>(p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0), prm,
-                                                                 A + (size_t)s0 * 2 * plane, ld, 2 * plane, plane,
-                                                                 ctx.w_norm.as<double>(), err);
+        // split: systems 2 plane apart, the remainder a plane after each;
+        // rounded only: systems a plane apart
+        const size_t stride = remainder ? 2 * plane : plane;
+        if (remainder)
+            assemble_ff_kernel<true><<<grid, ASM_THREADS, 0, ctx.stream>>>(
+                p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0), prm, A + (size_t)s0 * stride, ld, stride, plane,
+                ctx.w_norm.as<double>(), err);
+        else
+            assemble_ff_kernel<false><<<grid, ASM_THREADS, 0, ctx.stream>>>(
+                p.n, p.geo.npad, p.geo.arr32(0), p.geo.arr(0), prm, A + (size_t)s0 * stride, ld, stride, plane,
+                ctx.w_norm.as<double>(), err);
         BEM_CHECK_LAUNCH(&ctx);
         finish_norms(ctx, ctx.w_norm.as<double>(), nparts, prm.nsys, norms + s0);
     }

@@ -252,9 +252,11 @@ void assemble_system_fp64(Context& ctx, const Problem& p, double2* A, int64_t ld
 // rounding of the remainder (`plane` = ld * n further on), evaluated in
 // float-float (~2^-44 relative) with the geometry once per pair and
 // e^{ik r} by recurrence for evenly spaced wavenumbers; systems 2 * plane
-// float2 apart; norms[s] = ||A_s||_F.
+// float2 apart; norms[s] = ||A_s||_F.  remainder false: the FP32 roundings
+// alone (the operator rounded once from its float-float value), systems
+// `plane` float2 apart.
 void assemble_system_split(Context& ctx, const Problem& p, const double* ks, const cd* alphas, const cd* betas,
-                           int nsys, float2* A, int64_t ld, size_t plane, double* norms);
+                           int nsys, float2* A, int64_t ld, size_t plane, double* norms, bool remainder = true);
 void assemble_system_fp32_body(Context& ctx, const Problem& p, const double* ks, const cd* alphas,
                                const cd* betas, const cd* gammas, const cd* deltas, int nsys, float2* A,
                                int64_t ld, size_t mat_stride, double2* rowsum, size_t vec_stride, double* norms);

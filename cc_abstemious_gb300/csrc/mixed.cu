@@ -93,7 +93,7 @@ __global__ void repeat_norms_kernel(const double* __restrict__ in, int R, int ns
 // layout; the LU preconditioner factors it once.
 static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_precond precond,
                             bem_cplx* scattered, bem_cplx* incident, bem_solve_report* reports, bool check_vs_lu,
-                            bool fp64_operator) {
+                            bool fp64_operator, bool rounded) {
     const int64_t n = p.n, nfp = p.nfp, R = p.nrhs(), ns = nf * R, NF = (int64_t)p.freqs.size();
     const int64_t ld = p.geo.npad;  // multiple of 64: aligned float4 loads
     const size_t mstride = (size_t)ld * n;
@@ -199,6 +199,17 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
         }
         gm_matrix_norms(c, ws);
         t.stop("assemble_fp64", nf, 16.0 * (double)n * n * nf);
+    } else if (rounded && !need_rowsum) {
+        // the FP32 operator rounded once from its float-float value (the
+        // refined form's assembly without the remainder plane)
+        EventTimer t(c);
+        assemble_system_split(c, p, ks.data(), al.data(), be.data(), (int)nf, A32, ld, mstride,
+                              R == 1 ? ws.anorm : normf, false);
+        if (R > 1) {
+            repeat_norms_kernel<<<(unsigned)((ns + 127) / 128), 128, 0, c.stream>>>(normf, (int)R, (int)ns, ws.anorm);
+            BEM_CHECK_LAUNCH(&c);
+        }
+        t.stop("assemble_rounded", (nf + 15) / 16, 8.0 * (double)n * n * nf);
     } else {
         // the assembly kernel also writes ||A_f||_F for the stopping test
         EventTimer t(c);
@@ -304,7 +315,7 @@ static void run_mixed_range(Context& c, Problem& p, int64_t F0, int64_t nf, bem_
 }
 
 void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered, bem_cplx* incident,
-               bem_solve_report* reports, bool check_vs_lu, bool fp64_operator) {
+               bem_solve_report* reports, bool check_vs_lu, bool fp64_operator, bool rounded) {
     c.stages.clear();
     const int64_t nf = (int64_t)p.freqs.size(), n = p.n;
     require(nf >= 1, "no frequencies");
@@ -325,7 +336,7 @@ void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered,
     const int64_t chunk = hier ? nf : std::max<int64_t>(1, std::min<int64_t>(nf, (int64_t)(budget / per)));
     for (int64_t f0 = 0; f0 < nf; f0 += chunk)
         run_mixed_range(c, p, f0, std::min(chunk, nf - f0), precond, scattered, incident, reports, check_vs_lu,
-                        fp64_operator);
+                        fp64_operator, rounded);
 }
 
 }  // namespace bem

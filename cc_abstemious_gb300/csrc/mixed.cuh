@@ -4,8 +4,11 @@
 
 namespace bem {
 
+// fp64_operator: the refined form (operators at FP64 accuracy, split);
+// rounded: FP32 operators rounded once from their float-float values instead
+// of the single-precision assembly (about half its error, ~4x its cost).
 void run_mixed(Context& c, Problem& p, bem_precond precond, bem_cplx* scattered, bem_cplx* incident,
-               bem_solve_report* reports, bool check_vs_lu, bool fp64_operator = false);
+               bem_solve_report* reports, bool check_vs_lu, bool fp64_operator = false, bool rounded = false);
 // Several bodies: every frequency of every body in one ragged batch (chunks
 // of at most budget_bytes of operators; 0: a share of the free memory).
 void run_mixed_batch(Context& c, const std::vector<Problem*>& probs, bem_precond precond,

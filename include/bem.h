@@ -63,8 +63,15 @@ typedef enum { BEM_SIDE_RHS = 0, BEM_SIDE_LHS = 1 } bem_side;
  *              answer at FP64 accuracy, for operators whose condition number
  *              makes FP32 storage miss 1e-6), while the preconditioner is
  *              built from its FP32 rounding (the tensor-core LU of
- *              BEM_PRECOND_LU). */
-typedef enum { BEM_FORM_PLAIN_FP64 = 0, BEM_FORM_MIXED = 1, BEM_FORM_REFINED = 2 } bem_form;
+ *              BEM_PRECOND_LU).
+ *  MIXED_ROUNDED: as MIXED, over operators rounded to FP32 once from their
+ *              float-float values (the REFINED assembly without the
+ *              remainder): about half the FP32 operator error of MIXED at
+ *              several times its assembly cost, for operators whose
+ *              conditioning puts MIXED just above the required accuracy.
+ *              Inputs with row sums on the right-hand side (nonzero
+ *              pressure or velocity conditions) use the MIXED assembly. */
+typedef enum { BEM_FORM_PLAIN_FP64 = 0, BEM_FORM_MIXED = 1, BEM_FORM_REFINED = 2, BEM_FORM_MIXED_ROUNDED = 3 } bem_form;
 
 /* Preconditioners of the mixed form (no counterpart in the reference, whose
  * GMRES is unpreconditioned, gmres.rs:80-140).  Flexible right
@@ -185,7 +192,8 @@ BEM_API bem_status bem_collocation(bem_ctx* ctx, const bem_problem* p, double* o
  * (the factors of influence_matrix.rs:130-162) as the batched forms assemble
  * them, for checking them against bem_get_dense_surface_matrices: kind 0 the
  * mixed form's single-precision assembly, kind 1 the refined form's split
- * float-float assembly (FP32 rounding + FP32 remainder, summed here in FP64).
+ * float-float assembly (FP32 rounding + FP32 remainder, summed here in FP64),
+ * kind 2 the MIXED_ROUNDED form's operator (that FP32 rounding alone).
  * A (host) receives nf matrices of n x n, column-major, leading dimension lda,
  * lda * n entries apart.  No reference counterpart (the reference assembles
  * FP64 only, influence_matrix.rs:64-98). */

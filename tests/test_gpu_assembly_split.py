@@ -50,6 +50,27 @@ def _check(ctx, inp):
     print("split max/fro, fp32 fro:", ["%.2e %.2e %.2e" % w for w in worst])
 
 
+def test_rounded_operator_is_the_fp32_rounding(ctx, tmp_path):
+    """The mixed_rounded form's operator (the split assembly's first plane) is
+    the FP32 rounding of the FP64 entry: equal to numpy's rounding of the
+    oracle's FP64 operator except where the float-float value and the oracle
+    fall on opposite sides of a rounding boundary (then one FP32 ulp)."""
+    inp = workloads.perturbed_sphere_input(str(tmp_path), 23, 700, [1.0, 4.0, 7.0])
+    pd = bem.PreData.from_dict(inp, ctx=ctx)
+    op = O.Problem(inp)
+    R = bem.assemble_operator(pd, "rounded")
+    for f in range(len(pd.frequencies)):
+        op.set_frequency_index(f)
+        H, G = op.dense_surface(nthreads=8)
+        a, b = op.lhs_factors()
+        ref = (a * H + b * G).astype(np.complex64)
+        got = R[f].astype(np.complex64)
+        same = np.mean((got.real == ref.real) & (got.imag == ref.imag))
+        assert same > 0.9999, same
+        ulp = np.spacing(np.maximum(np.abs(ref.real), np.abs(ref.imag)).astype(np.float32))
+        assert np.all(np.abs(got.real - ref.real) <= ulp) and np.all(np.abs(got.imag - ref.imag) <= ulp)
+
+
 @pytest.mark.parametrize("kw", [{}, {"method_type": "BurtonMiller"},
                                 {"surface_bc": {"bc_type": "Pressure", "value": [0.0, 0.0]}},
                                 {"method_type": "BurtonMiller", "surface_bc": {"bc_type": "Pressure",

@@ -120,6 +120,23 @@ def test_refined_form(ctx, wd):
         assert r["iterations"] <= 12
 
 
+def test_mixed_rounded_form(ctx, wd):
+    """The mixed form over operators rounded once from their float-float
+    values: within 1e-6 of FP64 LU, and closer than the mixed form over the
+    single-precision assembly (whose entries carry a few FP32 ulps)."""
+    inp = workloads.perturbed_sphere_input(wd, 17, 2400, [2.0, 6.0, 10.0], tol=1e-10)
+    rm = _run(ctx, inp, "lu")
+    a = bem.Analysis(ctx)
+    a.set_input(inp)
+    a.run(form="mixed_rounded", precond="lu", check_vs_lu=True)
+    e_mixed = max(r["rel_err_vs_lu"] for r in rm)
+    e_round = max(r["rel_err_vs_lu"] for r in a.reports)
+    for r in a.reports:
+        assert r["flag"] == 1 and 0 <= r["rel_err_vs_lu"] < 1e-6, r
+    assert e_round < e_mixed, (e_round, e_mixed)
+    print("max error vs FP64 LU: mixed %.3g, mixed_rounded %.3g" % (e_mixed, e_round))
+
+
 @pytest.mark.parametrize("precond", [None, "block_jacobi", "lu"])
 def test_refined_form_reaches_fp64_level(ctx, wd, precond):
     """The refined form holds each FP64 operator as its FP32 rounding plus the
