@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--nfreq", type=int, default=16)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="one mixed run (for ncu launch lists)")
+    ap.add_argument("--form", default="mixed", choices=["mixed", "refined", "mixed_rounded"],
+                    help="--profile-only: the batched form to run")
     ap.add_argument("--hierarchical", action="store_true",
                     help="with --profile-only: the H-matrix operators (leaf 64, eta 1, ACA 1e-5) instead of dense")
     ap.add_argument("--workload", default=WORKLOAD,
@@ -323,8 +325,11 @@ def main():
     inc = np.zeros((nf, pd.nfp), dtype=np.complex128)
     reps = (bem.SolveReport * nf)()
 
+    form = {"mixed": bem.FORM_MIXED, "refined": bem.FORM_REFINED, "mixed_rounded": bem.FORM_MIXED_ROUNDED}[
+        args.form if args.profile_only else "mixed"]
+
     def run_mixed(check=0):
-        ctx.check(ctx.lib.bem_run(ctx.h, pd.h, bem.FORM_MIXED, precond, bem._ptr(sc), bem._ptr(inc), reps, check))
+        ctx.check(ctx.lib.bem_run(ctx.h, pd.h, form, precond, bem._ptr(sc), bem._ptr(inc), reps, check))
 
     if args.profile_only:
         # the library's per-stage timing runs GMRES iteration by iteration:
