@@ -86,11 +86,11 @@ constexpr uint32_t G_TMEM_COLS = 512;           // two accumulators of GN column
 struct LuSys {
     float2* F;    // factors (copy of the operator), column-major, leading dimension ld
     float2* Dm;   // per block: L11^-1 (strict lower) and U11^-1 (upper), LB x LB column-major
-    float* W;     // real embeddings of the group's column panels (A21, then L21): 2n rows x WK floats
+    float* W;     // real embedding of the current step's column panel A21: 2n rows x 2 LB floats
     float* Li;    // real embedding of L11^-1: 2 LB x 2 LB, row-major
     float* UiT;   // transposed real embedding of U11^-1: 2 LB x 2 LB, row-major
     float* Y;     // the group's U12, natural real view: column j at Y + WK j (step k + j at rows 256 j ..)
-    const CUtensorMap* tmW;  // W: 2n rows x WK floats, 128-byte swizzled 32 x 128 boxes
+    const CUtensorMap* tmW;  // W: 2n rows x 2 LB floats, 128-byte swizzled 32 x 128 boxes
     const CUtensorMap* tmF;  // F's natural real view: n columns x 2n floats, 32 x 256 boxes
     const CUtensorMap* tmY;  // Y: n columns x WK floats, 32 x 256 boxes
     const CUtensorMap* tmL;  // Li: 256 rows, 32 x 128 boxes
@@ -296,11 +296,12 @@ __global__ void __launch_bounds__(DIAG_THREADS) lu_diag_kernel(const LuSys* __re
 }
 
 // W <- real embedding of step ks's column panel A21 (64 rows per CTA): rows
-// 2(i - kt_w) and 2(i - kt_w) + 1 of W, columns woff .. woff + 256, hold
-// [ar, -ai] and [ai, ar] for every column of A21's row i; kt_w = (kw + 1) LB
-// is the trailing origin of the step group.
+// 2(i - kt_w) and 2(i - kt_w) + 1 of W hold [ar, -ai] and [ai, ar] for every
+// column of A21's row i; kt_w = (kw + 1) LB is the trailing origin of the
+// step group.  (The L21 GEMM reads it once; the trailing updates read the
+// FP16 copy of L21 the GEMM writes into W16 at column woff.)
 __global__ void __launch_bounds__(256) lu_expand_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
-                                                        int nw, int ks, int kw, int woff) {
+                                                        int nw, int ks, int kw) {
     extern __shared__ float2 Y[];  // 64 x LB, column stride 65: Y[p * 65 + i] (no bank conflicts either way)
     int64_t tile;
     const LuSys S = sys[lu_locate(wl, nw, blockIdx.x, tile)];
@@ -315,8 +316,8 @@ __global__ void __launch_bounds__(256) lu_expand_kernel(const LuSys* __restrict_
     for (int t = threadIdx.x; t < nrow * LB; t += blockDim.x) {
         const int i = t / LB, c = t % LB;
         const float2 v = Y[c * 65 + i];
-        float2* w0 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i) * S.wk + woff);
-        float2* w1 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i + 1) * S.wk + woff);
+        float2* w0 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i) * (2 * LB));
+        float2* w1 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i + 1) * (2 * LB));
         w0[c] = make_float2(v.x, -v.y);
         w1[c] = make_float2(v.y, v.x);
     }
@@ -409,14 +410,15 @@ __host__ __device__ constexpr uint32_t umma_idesc_tf32_f32(int M, int N) {
 // accumulators of 256 tensor-memory columns) while the next tile's MMAs run.
 // GEMM modes (D = A' B over K = 32 nchunks real), for block step ks of the
 // step group starting at kw (trailing origin kt_w = (kw + 1) LB, the row origin
-// of W and of the TRAIL work regions):
-//   TRAIL  A22 -= W Y        128 rows of W x 256 columns of Y inside each work
-//                            entry's region; K = 256 per step of the group
-//                            applied (up to 1024 for the rest of A22)
+// of W, W16 and of the TRAIL work regions):
+//   TRAIL  A22 -= W16 Y16    128 rows of W16 x 256 columns of Y16 (FP16) inside
+//                            each work entry's region; K = 256 per step of the
+//                            group applied (up to 256 G for the rest of A22)
 //   U12    Y = Li U12raw     the two 128-row halves of Li x 256 columns of the
-//                            step's row panel, into Y's rows yoff .. yoff + 256
-//   L21    W = W UiT^T       128 rows of W x all 256 columns at W column woff, in
-//                            place; L21 in natural form into the factors
+//                            step's row panel, into Y's (and scaled into Y16's)
+//                            rows yoff .. yoff + 256
+//   L21    W16 = W UiT^T     128 rows of W x all 256 columns, into W16 at column
+//                            woff; L21 in natural form into the factors
 enum { G_TRAIL = 0, G_U12 = 1, G_L21 = 2 };
 
 struct GemmTile {
@@ -497,7 +499,7 @@ __device__ __forceinline__ GemmTile gemm_tile(const LuSys* __restrict__ sys, con
         g.col0 = 0;
         g.col_end = 2 * LB;
         g.tmA = S.tmW;
-        g.ax = woff;
+        g.ax = 0;
         g.ay = (int)g.row0;
         g.tmB = S.tmU;
         g.bx = 0;
@@ -658,15 +660,13 @@ __global__ void __launch_bounds__(GTHREADS, 1) lu_gemm_kernel(const LuSys* __res
                             h0[q * g.wk] = __float2half_rn(fminf(fmaxf(v[q] * g.ysc, -65504.f), 65504.f));
                         }
                 } else {
-                    // L21: the embedded row back into W, and the natural
-                    // entries (row 2i holds re, row 2i + 1 im of column 2p)
+                    // L21: the embedded row in FP16 into W16 (the trailing
+                    // updates' operand), and the natural entries into the
+                    // factors (row 2i holds re, row 2i + 1 im of column 2p)
                     float im[16];
 #pragma unroll
                     for (int q = 0; q < 16; ++q) im[q] = __shfl_down_sync(0xffffffffu, v[2 * q], 1);
                     if (!rok) continue;
-                    float4* wrow = reinterpret_cast<float4*>(g.W + r * g.wk + woff + cc * 32);
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) wrow[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
                     uint4* hrow = reinterpret_cast<uint4*>(g.W16 + r * g.wk + woff + cc * 32);
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
@@ -1024,10 +1024,10 @@ int lu_group(const Context& c, int64_t nmin, int64_t nsys) {
 }
 
 double lu_bytes_per_unknown(int64_t n) {
-    // W (2 WK floats), Y (WK floats), their FP16 copies (3 WK halves) and the
-    // diagonal-block inverses (LB complex floats) per unknown
+    // W (2 x 2 LB floats), Y (WK floats), the FP16 panels (3 WK halves) and
+    // the diagonal-block inverses (LB complex floats) per unknown
     const double wk = 2.0 * LB * (n >= LU_GROUP8_MIN_N ? LU_GROUP_MAX : 4);
-    return 18.0 * wk + 8.0 * LB + 64.0;
+    return 10.0 * wk + 16.0 * LB + 8.0 * LB + 64.0;
 }
 
 // Factors every operator of the batch and installs the preconditioner hook.
@@ -1065,7 +1065,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         entries = std::max(entries, v[(size_t)s].a / fdiv + (size_t)v[(size_t)s].lda * v[(size_t)s].n);
         const int nb = (int)((v[(size_t)s].n + LB - 1) / LB);
         dm += (size_t)nb * LB * LB;
-        wsz += (size_t)2 * v[(size_t)s].n * WK;
+        wsz += (size_t)2 * v[(size_t)s].n * (2 * LB);
         psz += (size_t)2 * (2 * LB) * (2 * LB) + (size_t)WK * v[(size_t)s].n;
         hsz += (size_t)3 * v[(size_t)s].n * WK;  // W16 (2n x WK) and Y16 (n x WK)
         d->nblk_max = std::max(d->nblk_max, nb);
@@ -1167,11 +1167,11 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
         L.yinv = std::ldexp(1.0f, -e);
         L.wk = WK;
         od += (size_t)L.nblk * LB * LB;
-        ow += (size_t)2 * L.n * WK;
+        ow += (size_t)2 * L.n * (2 * LB);
         op += (size_t)2 * (2 * LB) * (2 * LB) + (size_t)WK * L.n;
         oh += (size_t)3 * L.n * WK;
         CUtensorMap* ms = maps.data() + (size_t)NMAP * s;
-        map2d(ms + 0, L.W, WK, 2 * L.n, WK, GM, "the panel workspace");                // W
+        map2d(ms + 0, L.W, 2 * LB, 2 * L.n, 2 * LB, GM, "the panel workspace");        // W
         map2d(ms + 1, L.F, 2 * L.n, L.n, 2 * L.ld, GN, "the factors");                 // F, natural real view
         map2d(ms + 2, L.Y, WK, L.n, WK, GN, "the row panel");                          // Y
         map2d(ms + 3, L.Li, 2 * LB, 2 * LB, 2 * LB, GM, "the lower inverse");          // Li
@@ -1323,7 +1323,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
                 break;
             case LuData::EXPAND:
                 lu_expand_kernel<<<(unsigned)sg.ctas, 256, expand_smem, c.stream>>>(sys, wk + sg.off, sg.count, l.ks,
-                                                                                    l.kw, l.woff);
+                                                                                    l.kw);
                 break;
             case LuData::L21:
                 lu_gemm_kernel<G_L21><<<persistent(sg.ctas), GTHREADS, G_SMEM, c.stream>>>(
