@@ -718,36 +718,100 @@ static void pc_hook(Context& c, GmWorkspace& ws, int mode, void* user) {
 constexpr int GATE_PROBES = 2;
 constexpr double GATE_KEEP = 0.95;
 
+// One system of the gate's batch: size, leading dimension, operator offset
+// (float2 entries) and the offset of its probe vectors.
+struct GateSys {
+    int64_t n, lda, aoff, voff;
+};
+
+// Y = M_s Z for every system s (blockIdx.z) and probe (blockIdx.y).
+__global__ void __launch_bounds__(PC_LEAF) gate_apply_kernel(PcDev pc, const GateSys* __restrict__ gs,
+                                                             const double2* __restrict__ Z, double2* __restrict__ Y) {
+    const int s = blockIdx.z, q = blockIdx.y;
+    const int c = pc_leaf(pc, s, blockIdx.x);
+    if (c < 0) return;
+    const GateSys g = gs[s];
+    const size_t v = (size_t)g.voff + (size_t)q * g.n;
+    pc_block_apply(c, pc.cl_off, pc.cl_idx, pc.nb_off, pc.nb_d, pc.nb_blk, pc.M + pc_moff(pc, s), Z + v, Y + v,
+                   pc.offdiag);
+}
+
+// W = A_s Y and the residual partials |W - Z|^2, |Z|^2 of every system and
+// probe in one launch: a thread per row, FP32 arithmetic (the gate compares
+// two estimates), the sums accumulated per system.
+__global__ void gate_residual_kernel(const float2* __restrict__ A, const GateSys* __restrict__ gs,
+                                     const double2* __restrict__ Y, const double2* __restrict__ Z,
+                                     double* __restrict__ acc) {
+    __shared__ double sr[128], sz[128];
+    const int s = blockIdx.z, q = blockIdx.y;
+    const GateSys g = gs[s];
+    const int64_t i = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    double a = 0, b = 0;
+    if (i < g.n) {
+        const size_t v = (size_t)g.voff + (size_t)q * g.n;
+        const float2* As = A + g.aoff + i;
+        float ax = 0.f, ay = 0.f;
+        for (int64_t j = 0; j < g.n; ++j) {
+            const float2 e = As[j * g.lda];
+            const double2 y = Y[v + j];
+            const float yx = (float)y.x, yy = (float)y.y;
+            ax = fmaf(e.x, yx, fmaf(-e.y, yy, ax));
+            ay = fmaf(e.x, yy, fmaf(e.y, yx, ay));
+        }
+        const double2 z = Z[v + i];
+        const double rx = (double)ax - z.x, ry = (double)ay - z.y;
+        a = rx * rx + ry * ry;
+        b = z.x * z.x + z.y * z.y;
+    }
+    sr[threadIdx.x] = a;
+    sz[threadIdx.x] = b;
+    __syncthreads();
+    for (int o = 64; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            sr[threadIdx.x] += sr[threadIdx.x + o];
+            sz[threadIdx.x] += sz[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(acc + 2 * s, sr[0]);
+        atomicAdd(acc + 2 * s + 1, sz[0]);
+    }
+}
+
 static int learned_gate(Context& c, PcData& d, GmWorkspace& ws, uint64_t seed) {
     const int nsys = ws.bt.nsys;
     if (!ws.fp32) return nsys;
-    int64_t nmax = 0;
-    for (int s = 0; s < nsys; ++s) nmax = std::max(nmax, ws.sys_host.empty() ? ws.bt.n : ws.sys_host[(size_t)s].n);
-    DevBuf Z, Y, W, R, acc;
-    for (DevBuf* v : {&Z, &Y, &W, &R}) v->ensure(sizeof(double2) * (size_t)nmax * GATE_PROBES);
-    acc.ensure(sizeof(double) * 4 * (size_t)nsys);
-    BEM_CUDA(cudaMemsetAsync(acc.p, 0, sizeof(double) * 4 * (size_t)nsys, c.stream));
-    const int nleaf = d.multi ? d.nc_max : d.pat.nc;
+    std::vector<GateSys> gs((size_t)nsys);
+    int64_t tot = 0, nmax = 0;
     for (int s = 0; s < nsys; ++s) {
-        const int64_t n = ws.sys_host.empty() ? ws.bt.n : ws.sys_host[(size_t)s].n;
-        const int64_t lda = ws.sys_host.empty() ? ws.bt.lda : ws.sys_host[(size_t)s].lda;
-        const size_t aoff = ws.sys_host.empty() ? (size_t)s * ws.bt.mat_stride : ws.sys_host[(size_t)s].a_off;
-        const float2* As = static_cast<const float2*>(ws.bt.A) + aoff;
-        const int64_t tot = n * GATE_PROBES;
-        probes_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(tot, seed * 2654435761ull + (uint64_t)s,
-                                                                            Z.as<double2>());
+        GateSys& g = gs[(size_t)s];
+        g.n = ws.sys_host.empty() ? ws.bt.n : ws.sys_host[(size_t)s].n;
+        g.lda = ws.sys_host.empty() ? ws.bt.lda : ws.sys_host[(size_t)s].lda;
+        g.aoff = (int64_t)(ws.sys_host.empty() ? (size_t)s * ws.bt.mat_stride : ws.sys_host[(size_t)s].a_off);
+        g.voff = tot;
+        tot += g.n * GATE_PROBES;
+        nmax = std::max(nmax, g.n);
+    }
+    DevBuf Z, Y, acc, dgs;
+    Z.ensure(sizeof(double2) * (size_t)tot);
+    Y.ensure(sizeof(double2) * (size_t)tot);
+    acc.ensure(sizeof(double) * 4 * (size_t)nsys);
+    dgs.ensure(sizeof(GateSys) * (size_t)nsys);
+    BEM_CUDA(cudaMemcpyAsync(dgs.p, gs.data(), sizeof(GateSys) * nsys, cudaMemcpyHostToDevice, c.stream));
+    BEM_CUDA(cudaMemsetAsync(acc.p, 0, sizeof(double) * 4 * (size_t)nsys, c.stream));
+    // the same probes for block-Jacobi (use 0) and the learned form (use 1)
+    probes_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(tot, seed * 2654435761ull, Z.as<double2>());
+    BEM_CHECK_LAUNCH(&c);
+    const int nleaf = d.multi ? d.nc_max : d.pat.nc;
+    for (int use = 0; use < 2; ++use) {
+        gate_apply_kernel<<<dim3((unsigned)nleaf, (unsigned)GATE_PROBES, (unsigned)nsys), PC_LEAF, 0, c.stream>>>(
+            d.dev(use), dgs.as<GateSys>(), Z.as<double2>(), Y.as<double2>());
         BEM_CHECK_LAUNCH(&c);
-        for (int use = 0; use < 2; ++use) {
-            pc_apply_probes_kernel<<<dim3((unsigned)nleaf, (unsigned)GATE_PROBES), PC_LEAF, 0, c.stream>>>(
-                d.dev(use), s, Z.as<double2>(), Y.as<double2>(), n);
-            BEM_CHECK_LAUNCH(&c);
-            probe_matvec_kernel<<<dim3((unsigned)((n + 127) / 128), (unsigned)GATE_PROBES), 128, 0, c.stream>>>(
-                n, As, lda, Y.as<double2>(), W.as<double2>(), 0);
-            BEM_CHECK_LAUNCH(&c);
-            probe_residual_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(
-                tot, W.as<double2>(), Z.as<double2>(), R.as<double2>(), acc.as<double>() + 4 * (size_t)s + 2 * use);
-            BEM_CHECK_LAUNCH(&c);
-        }
+        gate_residual_kernel<<<dim3((unsigned)((nmax + 127) / 128), (unsigned)GATE_PROBES, (unsigned)nsys), 128, 0,
+                               c.stream>>>(static_cast<const float2*>(ws.bt.A), dgs.as<GateSys>(), Y.as<double2>(),
+                                           Z.as<double2>(), acc.as<double>() + 2 * (size_t)nsys * use);
+        BEM_CHECK_LAUNCH(&c);
     }
     std::vector<double> h(4 * (size_t)nsys);
     BEM_CUDA(cudaMemcpyAsync(h.data(), acc.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c.stream));
@@ -755,7 +819,9 @@ static int learned_gate(Context& c, PcData& d, GmWorkspace& ws, uint64_t seed) {
     std::vector<int8_t> keep((size_t)nsys);
     int kept = 0;
     for (int s = 0; s < nsys; ++s) {
-        const double bj = h[4 * (size_t)s] / h[4 * (size_t)s + 1], ln = h[4 * (size_t)s + 2] / h[4 * (size_t)s + 3];
+        const double* u0 = h.data() + 2 * (size_t)s;                  // block-Jacobi
+        const double* u1 = h.data() + 2 * ((size_t)nsys + (size_t)s);  // learned
+        const double bj = u0[0] / u0[1], ln = u1[0] / u1[1];
         keep[(size_t)s] = (int8_t)(std::isfinite(ln) && ln < GATE_KEEP * bj);
         kept += keep[(size_t)s];
     }
@@ -782,6 +848,19 @@ struct SetupTimer {
                     c.launches - l0, 0);
     }
 };
+// Wall time of one part of a set-up (synchronised at its end) when profiling.
+struct PartTimer {
+    Context& c;
+    const char* name;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    PartTimer(Context& ctx, const char* n) : c(ctx), name(n) {}
+    ~PartTimer() {
+        if (!c.profiling) return;
+        cudaStreamSynchronize(c.stream);
+        c.stage_add(name, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(),
+                    0, 0);
+    }
+};
 }  // namespace
 
 bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks) {
@@ -796,22 +875,30 @@ bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond k
     auto h = std::make_shared<PcHookData>();
     // block-Jacobi needs the diagonal blocks only
     {
+        PartTimer pt(c, "pc_patterns");
         std::vector<NearPattern> pats;
         build_patterns(c, std::vector<const Problem*>{&p}, pats, kind != BEM_PRECOND_LEARNED);
         h->data.pat = std::move(pats[0]);
+        upload_pattern(c, h->data);
     }
-    upload_pattern(c, h->data);
     const int nsys = ws.bt.nsys;
-    diag_inverses(c, h->data, nsys, ws.bt.A, ws.fp32, ws.bt.lda, ws.bt.mat_stride, ws.bt.sys);
+    {
+        PartTimer pt(c, "pc_diag_inverses");
+        diag_inverses(c, h->data, nsys, ws.bt.A, ws.fp32, ws.bt.lda, ws.bt.mat_stride, ws.bt.sys);
+    }
     h->use_off = false;
     if (kind == BEM_PRECOND_LEARNED) {
-        PairBufs pb;
-        upload_pairs(c, h->data.pat, pb);
-        for (int s = 0; s < nsys; ++s)
-            learned_entries(c, p, *c.net, h->data.pat, pb, ks[s],
-                            h->data.M.as<float2>() + (size_t)s * h->data.pat.entries);
-        h->use_off = true;
-        c.sync();
+        {
+            PartTimer pt(c, "pc_learned_entries");
+            PairBufs pb;
+            upload_pairs(c, h->data.pat, pb);
+            for (int s = 0; s < nsys; ++s)
+                learned_entries(c, p, *c.net, h->data.pat, pb, ks[s],
+                                h->data.M.as<float2>() + (size_t)s * h->data.pat.entries);
+            h->use_off = true;
+            c.sync();
+        }
+        PartTimer pt(c, "pc_gate");
         learned_gate(c, h->data, ws, 17);
     }
     ws.zb().ensure(sizeof(double2) * gm_q_total(ws));
@@ -840,7 +927,10 @@ bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies,
     PcData& d = h->data;
     const int nb = (int)bodies.size(), nsys = ws.bt.nsys;
     std::vector<NearPattern> pats;
-    build_patterns(c, std::vector<const Problem*>(bodies.begin(), bodies.end()), pats, !learned);
+    {
+        PartTimer pt(c, "pc_patterns");
+        build_patterns(c, std::vector<const Problem*>(bodies.begin(), bodies.end()), pats, !learned);
+    }
     std::vector<int32_t> leaf0(1, 0);
     NearPattern& P = d.pat;
     P.cl_off.assign(1, 0);
@@ -877,9 +967,13 @@ bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies,
     BEM_CUDA(cudaMemcpyAsync(d.body_leaf0.p, leaf0.data(), sizeof(int32_t) * leaf0.size(), cudaMemcpyHostToDevice,
                              c.stream));
     BEM_CUDA(cudaMemcpyAsync(d.sys_moff.p, moff.data(), sizeof(size_t) * nsys, cudaMemcpyHostToDevice, c.stream));
-    diag_inverses(c, d, nsys, ws.bt.A, ws.fp32, 0, 0, ws.bt.sys);
+    {
+        PartTimer pt(c, "pc_diag_inverses");
+        diag_inverses(c, d, nsys, ws.bt.A, ws.fp32, 0, 0, ws.bt.sys);
+    }
     h->use_off = false;
     if (learned) {
+        PartTimer pt(c, "pc_learned_entries");
         PairBufs pb;
         for (int b = 0; b < nb; ++b) {
             if (pats[(size_t)b].npairs == 0) continue;
@@ -891,6 +985,9 @@ bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies,
             c.sync();  // the pair buffers are reused by the next body
         }
         h->use_off = true;
+    }
+    if (learned) {
+        PartTimer pt(c, "pc_gate");
         learned_gate(c, d, ws, 17);
     }
     c.sync();
