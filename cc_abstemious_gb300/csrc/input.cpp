@@ -608,11 +608,15 @@ std::vector<TuneEntry> parse_tuning(const std::string& text) {
 }
 
 int TuningTable::get(const char* kernel, const char* param, int64_t n, int64_t nsys, int dflt) const {
-    // the entry of this kernel nearest in log(n), then log(nsys)
+    // the entry of this kernel that sets the parameter, nearest in log(n),
+    // then log(nsys)
     const TuneEntry* best = nullptr;
     double bd = 0;
     for (const TuneEntry& e : entries) {
         if (e.kernel != kernel) continue;
+        bool has = false;
+        for (auto& kv : e.params) has = has || kv.first == param;
+        if (!has) continue;
         const double d = std::fabs(std::log((double)std::max<int64_t>(n, 1) / (double)std::max<int64_t>(e.n, 1))) +
                          0.25 * std::fabs(std::log((double)std::max<int64_t>(nsys, 1) /
                                                    (double)std::max<int64_t>(e.nsys, 1)));

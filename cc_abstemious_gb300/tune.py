@@ -13,7 +13,9 @@ default's, so the gain of the table is on file.  A context reads the table
   lu_gemm_trail  (sb_r, sb_c): tile raster of the trailing update (stage
                  lu_gemm_trail) -- mixed form with the LU preconditioner, one
                  frequency of cube-spheres of 1944 .. 40344 quads, and a batch
-                 of 64 perturbed spheres.
+                 of 64 perturbed spheres; group: block steps per pass over A22
+                 (4 or 8; stage lu_setup_total, the whole factorization) on the
+                 spheres from 12000 quads.
   gm_apply_fp32  unroll: columns per load batch of the Krylov mat-vec (stage
                  gmres_matvec_fp32) -- the rigid sphere, 16 frequencies.
   assemble32     min_ctas: occupancy bound of the FP32 assembly (stage
@@ -105,6 +107,8 @@ def main():
                   "lu_gemm_trail"))
     entries += sweep("lu_gemm_trail", [{"sb_r": r, "sb_c": c} for r, c in RASTERS], cases,
                      {"sb_r": 8, "sb_c": 32})
+    big = [(n, ns, cx, run, "lu_setup_total") for n, ns, cx, run, _ in cases if n >= 12000 and ns == 1]
+    entries += sweep("lu_gemm_trail", [{"group": g} for g in (4, 8)], big, {"group": 8})
 
     # the Krylov mat-vec and the FP32 assembly on the rigid sphere
     cases_mv, cases_as = [], []
