@@ -849,8 +849,11 @@ def target_ellipsoid(sh):
         "config": {"n_unknowns": n, "frequencies": nf, "rhs": R, "ka_a2": [2.5, 20.0],
                    "solver": "GMRES tol 1e-8 (backward error) with the LU preconditioner, dense operators "
                              "(input: Hierarchical tol 1e-6)",
-                   "learned": "not run: the near-field learned and block-Jacobi preconditioners need thousands of "
-                              "iterations at ka 20 on this body; the LU preconditioner needs 3-4"},
+                   "learned": "not in the timed forms: measured separately (bench's network, mixed form, both "
+                              "waves, GMRES tol 1e-8 up to 20000 iterations), the near-field learned and "
+                              "block-Jacobi preconditioners do not converge at ka 2.5 (20000 iterations, 91 s "
+                              "per frequency) and take 424-620 iterations at ka 20, the learned one the same "
+                              "count as block-Jacobi; the LU preconditioner takes 4-6"},
         "forms": forms, "plain_fp64": plain,
         "speedup_vs_plain_fp64": forms[best]["value"] / plain["value"] if best else None,
         "max_rel_err_vs_fp64_lu": forms[best]["max_rel_err_vs_fp64_lu"] if best else None,
