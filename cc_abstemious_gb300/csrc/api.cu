@@ -115,6 +115,71 @@ void unpack_solution(Context& c, const Problem& p, const double2* x, double2* ph
     }
 }
 
+// unpack_solution for several systems in one launch.
+struct UnpackJob {
+    int64_t n, blk0;
+    int bc_type, pad;
+    double2 bcv, f;  // boundary value; impedance factor
+    const double2* x;
+    double2 *phi, *vn;
+};
+
+__global__ void unpack_batch_kernel(const UnpackJob* __restrict__ jobs, int njobs) {
+    const int64_t b = blockIdx.x;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].blk0 <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const UnpackJob& J = jobs[lo];
+    const int64_t i = (b - J.blk0) * 256 + threadIdx.x;
+    if (i >= J.n) return;
+    const double2 x = J.x[i];
+    if (J.bc_type == 0) {
+        J.phi[i] = J.bcv;
+        J.vn[i] = x;
+    } else if (J.bc_type == 1) {
+        J.phi[i] = x;
+        J.vn[i] = J.bcv;
+    } else {
+        J.phi[i] = x;
+        J.vn[i] = cmul(J.f, x);
+    }
+}
+
+void unpack_batch(Context& c, const std::vector<UnpackItem>& items) {
+    std::vector<UnpackJob> jobs;
+    int64_t blk = 0;
+    for (const UnpackItem& it : items) {
+        Problem& p = const_cast<Problem&>(*it.p);
+        const int64_t f0 = p.ifreq;
+        p.ifreq = it.ifreq;
+        UnpackJob J{};
+        J.n = p.n;
+        J.blk0 = blk;
+        J.bc_type = p.in.bc_type;
+        J.bcv = make_double2(p.in.bc_value[0], p.in.bc_value[1]);
+        if (p.in.bc_type == 2) {
+            const cd f = impedance_factor(p);
+            J.f = make_double2(f.re, f.im);
+        }
+        p.ifreq = f0;
+        J.x = it.x;
+        J.phi = it.phi;
+        J.vn = it.vn;
+        blk += (J.n + 255) / 256;
+        jobs.push_back(J);
+    }
+    if (jobs.empty()) return;
+    DevBuf d;
+    d.ensure(sizeof(UnpackJob) * jobs.size());
+    BEM_CUDA(cudaMemcpyAsync(d.p, jobs.data(), sizeof(UnpackJob) * jobs.size(), cudaMemcpyHostToDevice, c.stream));
+    unpack_batch_kernel<<<(unsigned)blk, 256, 0, c.stream>>>(d.as<UnpackJob>(), (int)jobs.size());
+    BEM_CHECK_LAUNCH(&c);
+    c.sync();  // the job list is freed on return
+}
+
 // Dense plain-FP64 surface solve on device vectors (solve.rs:24-71 and
 // :153-171): the fused kernel assembles the system matrix alpha H + beta G and
 // the uniform-BC right-hand side in one pass.

@@ -9,6 +9,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <optional>
 
 #include "common.cuh"
 #include "complex.cuh"
@@ -67,6 +68,24 @@ void plan_body(Problem& p, BodyPlan& b) {
     b.op_bytes = sizeof(float2) * (size_t)b.ld * (size_t)b.n * (size_t)b.nf;
 }
 
+namespace {
+// Wall time of one part of a batch solve (synchronised at its end) for the
+// library's per-stage profile.
+struct BatchStage {
+    Context& c;
+    const char* name;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    int64_t l0;
+    BatchStage(Context& ctx, const char* n) : c(ctx), name(n), l0(ctx.launches) {}
+    ~BatchStage() {
+        if (!c.profiling) return;
+        cudaStreamSynchronize(c.stream);
+        c.stage_add(name, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(),
+                    c.launches - l0, 0);
+    }
+};
+}  // namespace
+
 void solve_chunk(Context& c, std::vector<BodyPlan*>& bodies, bem_precond precond, bem_cplx* const* scattered,
                  bem_cplx* const* incident, bem_solve_report* const* reports, bool check_vs_lu) {
     auto t_start = std::chrono::steady_clock::now();
@@ -121,6 +140,7 @@ void solve_chunk(Context& c, std::vector<BodyPlan*>& bodies, bem_precond precond
     // ---- assembly: one launch for every body without a boundary-value term;
     // bodies that need rowsum(gamma H + delta G) use the one-body kernel
     {
+        BatchStage bs(c, "batch_assembly");
         std::vector<BodyAsm32> multi;
         std::vector<size_t> multi_sys0;
         for (size_t b = 0; b < bodies.size(); ++b) {
@@ -159,15 +179,21 @@ void solve_chunk(Context& c, std::vector<BodyPlan*>& bodies, bem_precond precond
         }
     }
     // ---- right-hand sides
-    for (size_t s = 0; s < nsys; ++s) {
-        BodyPlan& B = *bodies[(size_t)sys_body[s]];
-        Problem& p = *B.p;
-        p.ifreq = (int64_t)(s - body_sys0[(size_t)sys_body[s]]);
-        incident_surface(c, p, inc + L[s].v_off);
-        const double sg = p.in.bc_type == 0 ? 1.0 : -1.0;
-        launch_rhs_combine(c, B.n, sg, inc + L[s].v_off, {p.in.bc_value[0], p.in.bc_value[1]},
-                           B.need_rowsum ? rowsum + L[s].v_off : nullptr, ws.bt.B + L[s].v_off);
+    std::optional<BatchStage> part;
+    part.emplace(c, "batch_rhs");
+    {
+        std::vector<IncItem> items;
+        for (size_t s = 0; s < nsys; ++s) {
+            BodyPlan& B = *bodies[(size_t)sys_body[s]];
+            const Problem& p = *B.p;
+            items.push_back(IncItem{&p, (int64_t)(s - body_sys0[(size_t)sys_body[s]]), 0, false,
+                                    inc + L[s].v_off, ws.bt.B + L[s].v_off, p.in.bc_type == 0 ? 1.0 : -1.0,
+                                    {p.in.bc_value[0], p.in.bc_value[1]},
+                                    B.need_rowsum ? rowsum + L[s].v_off : nullptr});
+        }
+        incident_batch(c, items);
     }
+    part.reset();
     // ---- batched GMRES over every system
     gm_init_each(c, ws, tols, maxr, ms);
     if (precond != BEM_PRECOND_NONE) {
@@ -177,16 +203,25 @@ void solve_chunk(Context& c, std::vector<BodyPlan*>& bodies, bem_precond precond
     }
     int64_t cap = 0;
     for (size_t s = 0; s < nsys; ++s) cap = std::max(cap, maxr[s] * (int64_t)ms[s] + 1);
-    gm_run(c, ws, c.profiling ? 0 : 4, cap);
     std::vector<GmState> st;
-    gm_read_states(c, ws, st);
+    {
+        BatchStage bs(c, "batch_gmres");
+        gm_run(c, ws, c.profiling ? 0 : 4, cap);
+        gm_read_states(c, ws, st);
+    }
     // ---- surface unknowns and field points
-    for (size_t s = 0; s < nsys; ++s) {
-        BodyPlan& B = *bodies[(size_t)sys_body[s]];
-        Problem& p = *B.p;
-        p.ifreq = (int64_t)(s - body_sys0[(size_t)sys_body[s]]);
-        unpack_solution(c, p, ws.bt.X + L[s].v_off, phi + L[s].v_off, vn + L[s].v_off);
-        if (B.nfp) incident_field(c, p, finc + fpoff[s]);
+    part.emplace(c, "batch_field");
+    {
+        std::vector<UnpackItem> un;
+        std::vector<IncItem> fi;
+        for (size_t s = 0; s < nsys; ++s) {
+            BodyPlan& B = *bodies[(size_t)sys_body[s]];
+            const int64_t f = (int64_t)(s - body_sys0[(size_t)sys_body[s]]);
+            un.push_back(UnpackItem{B.p, f, ws.bt.X + L[s].v_off, phi + L[s].v_off, vn + L[s].v_off});
+            if (B.nfp) fi.push_back(IncItem{B.p, f, 0, true, finc + fpoff[s], nullptr, 0.0, {0, 0}, nullptr});
+        }
+        unpack_batch(c, un);
+        incident_batch(c, fi);
     }
     for (size_t b = 0; b < bodies.size(); ++b) {
         BodyPlan& B = *bodies[b];
@@ -205,6 +240,7 @@ void solve_chunk(Context& c, std::vector<BodyPlan*>& bodies, bem_precond precond
         BEM_CUDA(cudaMemcpyAsync(hvn.data(), vn, sizeof(double2) * vtot, cudaMemcpyDeviceToHost, c.stream));
     }
     c.sync();
+    part.reset();
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     for (size_t s = 0; s < nsys; ++s) {
         const int bi = sys_body[s];

@@ -280,6 +280,20 @@ void evaluate_field(Context& ctx, const Problem& p, const double2* phi, const do
 void row_or_column(Context& ctx, const Problem& p, const int64_t* dI, int64_t ni, const int64_t* dJ,
                    int64_t nj, int side, double2* out, int64_t diag_pos);
 void incident_surface(Context& ctx, const Problem& p, double2* out);
+// Incident values of several problems (frequency ifreq, incident wave rhs) in
+// one launch: at the collocation points (field = false; with rhs_out, also the
+// right-hand side sgn * inc + bc * rowsum) or at the field points.
+struct IncItem {
+    const Problem* p;
+    int64_t ifreq, rhs;
+    bool field;
+    double2* out;
+    double2* rhs_out;
+    double sgn;
+    cd bc;
+    const double2* rowsum;
+};
+void incident_batch(Context& ctx, const std::vector<IncItem>& items);
 void incident_field(Context& ctx, const Problem& p, double2* out);
 
 // Dense linear algebra (dense.cu)

@@ -236,11 +236,10 @@ static IncParams inc_params(const Problem& p) {
 }
 
 // incident_wave.rs:7-63 (surface, with the Burton-Miller term) and :66-99
-// (field points, no normal).
-__global__ void incident_kernel(int64_t n, int64_t stride, const double* __restrict__ pts, IncParams q,
-                                int with_normal, double2* __restrict__ out) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// (field points, no normal): the value at point i of pts (x y z, then the
+// normal, arrays `stride` apart).
+__device__ __forceinline__ z2 incident_value(int64_t i, int64_t stride, const double* __restrict__ pts,
+                                             const IncParams& q, int with_normal) {
     double x = pts[i], y = pts[stride + i], z = pts[2 * stride + i];
     z2 amp = {q.amp_re, q.amp_im};
     z2 val;
@@ -270,7 +269,49 @@ __global__ void incident_kernel(int64_t n, int64_t stride, const double* __restr
             val = cadd(val, cmul(z2{0.0, q.beta_im}, vn));
         }
     }
-    out[i] = val;
+    return val;
+}
+
+__global__ void incident_kernel(int64_t n, int64_t stride, const double* __restrict__ pts, IncParams q,
+                                int with_normal, double2* __restrict__ out) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = incident_value(i, stride, pts, q, with_normal);
+}
+
+// Several systems in one launch: a flattened grid of 128-point blocks, the
+// job of a block found by bisection on blk0.  Surface jobs also form the
+// GMRES right-hand side out2 = s inc + bc rowsum (solve.rs:35-69).
+struct IncJob {
+    const double* pts;
+    int64_t n, stride, blk0;
+    IncParams q;
+    int with_normal, pad;
+    double sgn;
+    double2 bc;
+    const double2* rowsum;
+    double2* out;   // the incident values
+    double2* out2;  // the right-hand side (surface jobs; may be null)
+};
+
+__global__ void incident_batch_kernel(const IncJob* __restrict__ jobs, int njobs) {
+    const int64_t b = blockIdx.x;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].blk0 <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const IncJob& J = jobs[lo];
+    const int64_t i = (b - J.blk0) * 128 + threadIdx.x;
+    if (i >= J.n) return;
+    const z2 v = incident_value(i, J.stride, J.pts, J.q, J.with_normal);
+    J.out[i] = v;
+    if (J.out2) {
+        double2 r = cscale(v, J.sgn);
+        if (J.rowsum) cfma(r, J.bc, J.rowsum[i]);
+        J.out2[i] = r;
+    }
 }
 
 void incident_surface(Context& ctx, const Problem& p, double2* out) {
@@ -279,6 +320,42 @@ void incident_surface(Context& ctx, const Problem& p, double2* out) {
     int blocks = (int)((p.n + threads - 1) / threads);
     incident_kernel<<<blocks, threads, 0, ctx.stream>>>(p.n, p.geo.npad, p.geo.arr(0), q, 1, out);
     BEM_CHECK_LAUNCH(&ctx);
+}
+
+void incident_batch(Context& ctx, const std::vector<IncItem>& items) {
+    if (items.empty()) return;
+    std::vector<IncJob> jobs;
+    int64_t blk = 0;
+    for (const IncItem& it : items) {
+        Problem& p = const_cast<Problem&>(*it.p);
+        const int64_t f0 = p.ifreq;
+        p.ifreq = it.ifreq;
+        p.select_rhs(it.rhs);
+        IncJob J{};
+        J.q = inc_params(p);
+        p.select_rhs(0);
+        p.ifreq = f0;
+        J.with_normal = it.field ? 0 : 1;
+        J.pts = it.field ? p.d_fp.as<double>() : p.geo.arr(0);
+        J.n = it.field ? p.nfp : p.n;
+        J.stride = it.field ? p.nfp_pad : p.geo.npad;
+        J.blk0 = blk;
+        J.sgn = it.sgn;
+        J.bc = make_double2(it.bc.re, it.bc.im);
+        J.rowsum = it.rowsum;
+        J.out = it.out;
+        J.out2 = it.rhs_out;
+        if (J.n == 0) continue;
+        blk += (J.n + 127) / 128;
+        jobs.push_back(J);
+    }
+    if (jobs.empty()) return;
+    DevBuf d;
+    d.ensure(sizeof(IncJob) * jobs.size());
+    BEM_CUDA(cudaMemcpyAsync(d.p, jobs.data(), sizeof(IncJob) * jobs.size(), cudaMemcpyHostToDevice, ctx.stream));
+    incident_batch_kernel<<<(unsigned)blk, 128, 0, ctx.stream>>>(d.as<IncJob>(), (int)jobs.size());
+    BEM_CHECK_LAUNCH(&ctx);
+    ctx.sync();  // the job list is freed on return
 }
 
 void incident_field(Context& ctx, const Problem& p, double2* out) {

@@ -21,6 +21,14 @@ double lu_reference_error(Context& c, const Problem& p, const double* phi_host, 
 // shared helpers (api.cu)
 cd impedance_factor(const Problem& p);
 void unpack_solution(Context& c, const Problem& p, const double2* x, double2* phi, double2* vn);
+// The same for several systems (problem p at frequency ifreq) in one launch.
+struct UnpackItem {
+    const Problem* p;
+    int64_t ifreq;
+    const double2* x;
+    double2 *phi, *vn;
+};
+void unpack_batch(Context& c, const std::vector<UnpackItem>& items);
 void launch_rhs_combine(Context& c, int64_t n, double s, const double2* inc, cd bc, const double2* rowsum,
                         double2* out);
 void solve_surface_dense_fp64(Context& c, const Problem& p, const double2* d_rhs_inc, double2* d_phi,
