@@ -156,12 +156,9 @@ void mlp_infer_tc(Context& c, const LearnedNet& net, int64_t P, const float* F, 
     if (P <= 0) return;
     int* err = device_err(c);
     BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c.stream));
-    static bool attr_set = false;
-    if (!attr_set) {
-        BEM_CUDA(cudaFuncSetAttribute(mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)SMEM_BYTES));
-        attr_set = true;
-    }
+    // the same constant on every call: safe from any thread and on every
+    // device (the attribute is per device)
+    BEM_CUDA(cudaFuncSetAttribute(mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     int sms = 0;
     BEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
     const int64_t ntiles = (P + TM - 1) / TM;
