@@ -195,14 +195,16 @@ def tensor_peak():
     return 1700.0, "fallback (sustained BF16)"
 
 
-def lu_traffic_ratio():
-    """DRAM traffic / algorithmic A22 bytes of one K = 1024 trailing update, from
-    the committed ncu summary (profiles/)."""
+def lu_traffic_ratio(group=4):
+    """DRAM traffic / algorithmic A22 bytes of one trailing update over a group
+    of four (K = 1024) or eight (K = 2048) block steps, from the committed ncu
+    summary (profiles/)."""
     p = os.path.join(ROOT, "profiles", "lu_gemm_trail_group_rigid_sphere.md")
     if not os.path.exists(p):
         return None
+    key = "traffic_over_algorithmic:" if group == 4 else "traffic_over_algorithmic_k2048:"
     for line in open(p):
-        if line.startswith("traffic_over_algorithmic:"):
+        if line.startswith(key):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -215,15 +217,17 @@ def lu_roofline(prof, sizes, what):
     kernel of the LU forms): flop rate of the trailing-update launches
     (event-timed by the library's profiling pass; 8 n^3 / 3 complex flop per
     factored operator; FP16 operands, FP32 accumulation) against the measured
-    dense 16-bit tensor peak.  Block steps run in groups of
-    four: one K = 1024 launch per group reads and writes the rest of the
-    trailing block once, so its algorithmic bytes are 16 B (FP32 complex, read
-    + write) per entry of that block (reported per operator: a launch covers
-    every operator of a frequency chunk)."""
+    dense 16-bit tensor peak.  Block steps run in groups of four (eight from
+    12000 unknowns): one K = 1024 (2048) launch per group reads and writes the
+    rest of the trailing block once, so its algorithmic bytes are 16 B (FP32
+    complex, read + write) per entry of that block (reported per operator: a
+    launch covers every operator of a frequency chunk)."""
     lu = prof.get("lu_gemm_trail", {})
     achieved = lu["bytes"] / (lu["ms"] * 1e-3) / 1e12 if lu.get("ms") else None
     peak, peak_kind = tensor_peak()
-    lb, group = 128, 4
+    # the library's step-group rule: eight steps per pass when every factored
+    # system has at least 12000 unknowns
+    lb, group = 128, (8 if min(sizes) >= 12000 else 4)
     tot, cnt = 0.0, 0
     for n in sizes:
         nblk = (n + lb - 1) // lb
@@ -233,16 +237,16 @@ def lu_roofline(prof, sizes, what):
                 tot += 16.0 * m1 * m1
                 cnt += 1
     alg = tot / cnt if cnt else None
-    ratio = lu_traffic_ratio()
+    ratio = lu_traffic_ratio(group)
     return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak if achieved else None,
             "traffic": ratio * alg if (ratio and alg) else None,
             "kernel": "lu_gemm_kernel<TRAIL> (FP16 tcgen05 trailing update of the LU preconditioner, " + what + ")",
             "algorithmic_bytes_per_operator_launch": alg,
             "peak_kind": peak_kind,
-            "traffic_note": "ncu dram read+write / algorithmic A22 bytes of one K = 1024 launch "
-                            "(profiles/lu_gemm_trail_group_rigid_sphere.md), times the mean algorithmic bytes "
-                            "of this workload's K = 1024 launches, per operator"}
+            "traffic_note": ("ncu dram read+write / algorithmic A22 bytes of one K = %d launch "
+                             "(profiles/lu_gemm_trail_group_rigid_sphere.md), times the mean algorithmic bytes "
+                             "of this workload's K = %d launches, per operator" % (256 * group, 256 * group))}
 
 
 def cpu_reference(inp, nfreq_sample, threads):
