@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <cstdio>
+#include <functional>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -35,6 +36,12 @@ struct Error : std::runtime_error {
 inline void require(bool ok, const std::string& msg, bem_status s = BEM_ERR_BAD_INPUT) {
     if (!ok) throw Error(s, msg);
 }
+
+// f(i) for every i in [0, n) on the process's host worker threads, the
+// calling thread among them, items handed out one at a time; returns when all
+// are done and rethrows the first exception an item raised.  Calls for
+// distinct i must be safe to run at the same time.
+void host_parallel_for(int64_t n, const std::function<void(int64_t)>& f);
 
 // ---------------------------------------------------------------------------
 // Input model: UserInput of input_data.rs:80-92.

@@ -3,6 +3,7 @@
 // dialect (mesh_data.rs:96-175) and the frequency lists (preprocess.rs:155-167,
 // tools.rs:1-24).  Host C++; no JSON library is available, so a small
 // recursive-descent parser is included.
+#include <atomic>
 #include <charconv>
 #include <cstdio>
 #include <type_traits>
@@ -10,6 +11,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <fstream>
 #include <map>
 #include <memory>
@@ -469,6 +471,25 @@ inline std::string first_word(const char* b, const char* e) {
     return std::string(b, w);
 }
 }  // namespace
+
+void host_parallel_for(int64_t n, const std::function<void(int64_t)>& f) {
+    if (n <= 0) return;
+    const int nt = (int)std::min<int64_t>(RowPool::get().size(), n);
+    std::atomic<int64_t> next{0};
+    std::mutex m;
+    std::exception_ptr err;
+    RowPool::get().run(nt, [&](int) {
+        for (int64_t i; (i = next.fetch_add(1)) < n;) {
+            try {
+                f(i);
+            } catch (...) {
+                std::lock_guard<std::mutex> lk(m);
+                if (!err) err = std::current_exception();
+            }
+        }
+    });
+    if (err) std::rethrow_exception(err);
+}
 
 Mesh read_vtk(const std::string& path) {
     std::string text;

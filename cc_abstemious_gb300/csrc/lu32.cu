@@ -171,6 +171,7 @@ __global__ void lu_round_kernel(const double2* __restrict__ A, size_t n, float2*
 // no register indexing, and the final region i < j, c < j is skipped by whole
 // tile blocks.
 constexpr int DIAG_THREADS = 512;
+constexpr int DIAG_TS = LB + 1;  // column stride of the block in shared memory
 constexpr int DW = DIAG_THREADS / 32, DB = LB / DW;  // warps (column stride), columns per thread
 static_assert(32 % DW == 0 || DW % 32 == 0, "a group of DW columns lies in one 32-row tile block");
 
@@ -252,7 +253,9 @@ __device__ __forceinline__ void lu_diag_sweep(float2 (&z)[4][DB], int nb, int tx
 __global__ void __launch_bounds__(DIAG_THREADS) lu_diag_kernel(const LuSys* __restrict__ sys,
                                                                const LuWork* __restrict__ wl, int k,
                                                                int* __restrict__ small_pivots) {
-    extern __shared__ float2 T[];  // LB x LB, column-major: T[c * LB + r]
+    // LB x LB, column-major with a padded column stride: T[c * DIAG_TS + r]
+    // (reads along a row then fall in distinct banks)
+    extern __shared__ float2 T[];
     __shared__ float2 colbuf[2][LB], rowbuf[2][LB];
     const LuSys S = sys[wl[blockIdx.x].sys];
     const int64_t k0 = (int64_t)k * LB;
@@ -273,23 +276,23 @@ __global__ void __launch_bounds__(DIAG_THREADS) lu_diag_kernel(const LuSys* __re
 #pragma unroll
     for (int b = 0; b < DB; ++b)
 #pragma unroll
-        for (int a = 0; a < 4; ++a) T[(ty + DW * b) * LB + tx + 32 * a] = z[a][b];
+        for (int a = 0; a < 4; ++a) T[(ty + DW * b) * DIAG_TS + tx + 32 * a] = z[a][b];
     __syncthreads();
     float2* Dk = S.Dm + (size_t)k * LB * LB;
     for (int c = ty; c < nb; c += DIAG_THREADS / 32)
-        for (int r = tx; r < nb; r += 32) Dk[c * LB + r] = T[c * LB + r];
+        for (int r = tx; r < nb; r += 32) Dk[c * LB + r] = T[c * DIAG_TS + r];
     if (nb < LB || S.n <= k0 + LB) return;  // no panels after the last block
     // real embeddings for the panel GEMMs: Li = [[re, -im], [im, re]] of
     // L11^-1 (unit lower), UiT = the transpose of that of U11^-1 (upper)
     float2* Li2 = reinterpret_cast<float2*>(S.Li);
     float2* Ui2 = reinterpret_cast<float2*>(S.UiT);
     for (int t = threadIdx.x; t < LB * LB; t += blockDim.x) {
-        const int i = t % LB, p = t / LB;  // Li: element (i, p), consecutive threads down a column of T
-        const float2 l = p < i ? T[p * LB + i] : make_float2(p == i ? 1.f : 0.f, 0.f);
+        const int i = t / LB, p = t % LB;  // Li: element (i, p), consecutive threads along a row of Li
+        const float2 l = p < i ? T[p * DIAG_TS + i] : make_float2(p == i ? 1.f : 0.f, 0.f);
         Li2[(2 * i) * LB + p] = make_float2(l.x, -l.y);
         Li2[(2 * i + 1) * LB + p] = make_float2(l.y, l.x);
         const int pu = t % LB, q = t / LB;  // UiT rows 2q, 2q + 1 from U11^-1 (pu, q)
-        const float2 u = pu <= q ? T[q * LB + pu] : make_float2(0.f, 0.f);
+        const float2 u = pu <= q ? T[q * DIAG_TS + pu] : make_float2(0.f, 0.f);
         Ui2[(2 * q) * LB + pu] = make_float2(u.x, u.y);
         Ui2[(2 * q + 1) * LB + pu] = make_float2(-u.y, u.x);
     }
@@ -302,24 +305,39 @@ __global__ void __launch_bounds__(DIAG_THREADS) lu_diag_kernel(const LuSys* __re
 // FP16 copy of L21 the GEMM writes into W16 at column woff.)
 __global__ void __launch_bounds__(256) lu_expand_kernel(const LuSys* __restrict__ sys, const LuWork* __restrict__ wl,
                                                         int nw, int ks, int kw) {
-    extern __shared__ float2 Y[];  // 64 x LB, column stride 65: Y[p * 65 + i] (no bank conflicts either way)
+    extern __shared__ float2 Y[];  // 64 x LB, column stride 65: Y[p * 65 + i] (at most two-way bank conflicts)
+    constexpr int NT = 256, PAIRS = 32 * LB / NT;  // row pairs per thread
     int64_t tile;
     const LuSys S = sys[lu_locate(wl, nw, blockIdx.x, tile)];
     const int64_t k0 = (int64_t)ks * LB, kt = k0 + LB, ktw = (int64_t)(kw + 1) * LB, i0 = kt + 64 * tile;
     const int nrow = (int)min((int64_t)64, S.n - i0);
-    for (int t = threadIdx.x; t < 64 * LB; t += blockDim.x) {
-        const int p = t / 64, i = t % 64;
-        Y[p * 65 + i] = i < nrow ? S.F[(k0 + p) * S.ld + i0 + i] : make_float2(0.f, 0.f);
+    // rows i, i + 1 of column p in one 16-byte load, all of a thread's loads
+    // in flight together.  Aligned: ld is even (the factors' tensor map has a
+    // 16-byte column stride) and i0 + i is even.  In bounds: row i + 1 = n
+    // only for odd n, where ld >= n + 1.
+    float4 v[PAIRS];
+#pragma unroll
+    for (int q = 0; q < PAIRS; ++q) {
+        const int t = threadIdx.x + NT * q, p = t / 32, i = 2 * (t % 32);
+        v[q] = i < nrow ? *reinterpret_cast<const float4*>(S.F + (k0 + p) * S.ld + i0 + i)
+                        : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int q = 0; q < PAIRS; ++q) {
+        const int t = threadIdx.x + NT * q, p = t / 32, i = 2 * (t % 32);
+        Y[p * 65 + i] = make_float2(v[q].x, v[q].y);
+        Y[p * 65 + i + 1] = make_float2(v[q].z, v[q].w);
     }
     __syncthreads();
+    // two columns per thread: 16-byte stores into both rows of the embedding
     const int64_t wr0 = 2 * (i0 - ktw);
-    for (int t = threadIdx.x; t < nrow * LB; t += blockDim.x) {
-        const int i = t / LB, c = t % LB;
-        const float2 v = Y[c * 65 + i];
-        float2* w0 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i) * (2 * LB));
-        float2* w1 = reinterpret_cast<float2*>(S.W + (wr0 + 2 * i + 1) * (2 * LB));
-        w0[c] = make_float2(v.x, -v.y);
-        w1[c] = make_float2(v.y, v.x);
+    for (int t = threadIdx.x; t < nrow * (LB / 2); t += NT) {
+        const int i = t / (LB / 2), c = 2 * (t % (LB / 2));
+        const float2 a = Y[c * 65 + i], b = Y[(c + 1) * 65 + i];
+        float4* w0 = reinterpret_cast<float4*>(S.W + (wr0 + 2 * i) * (2 * LB));
+        float4* w1 = reinterpret_cast<float4*>(S.W + (wr0 + 2 * i + 1) * (2 * LB));
+        w0[c / 2] = make_float4(a.x, -a.y, b.x, -b.y);
+        w1[c / 2] = make_float4(a.y, a.x, b.y, b.x);
     }
 }
 
@@ -1285,7 +1303,7 @@ void lu_precond_setup(Context& c, GmWorkspace& ws) {
     BEM_CUDA(cudaMemsetAsync(d->info.p, 0, sizeof(int), c.stream));
     int* err = device_err(c);
     BEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c.stream));
-    const size_t diag_smem = sizeof(float2) * LB * LB, expand_smem = sizeof(float2) * 65 * LB;
+    const size_t diag_smem = sizeof(float2) * LB * DIAG_TS, expand_smem = sizeof(float2) * 65 * LB;
     BEM_CUDA(cudaFuncSetAttribute(lu_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_smem));
     BEM_CUDA(cudaFuncSetAttribute(lu_expand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)expand_smem));
     BEM_CUDA(cudaFuncSetAttribute(lu_gemm_kernel<G_TRAIL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));

@@ -31,6 +31,7 @@
 #include "complex.cuh"
 #include "gmres.cuh"
 #include "hmatrix.cuh"
+#include "kernels.cuh"
 #include "precond.cuh"
 #include "tree.cuh"
 
@@ -41,58 +42,93 @@ constexpr double PC_ETA = 2.0;
 
 // ---------------------------------------------------------------------------
 // Near-field leaf patterns: the cluster trees of all bodies in one device
-// pass, then per body its leaves and their near neighbours.
+// pass, then per body its leaves and their near neighbours.  Several bodies
+// are built on parallel host threads (each writes only its own pattern); a
+// single body spreads its leaves over the threads instead.
 void build_patterns(Context& c, const std::vector<const Problem*>& bodies, std::vector<NearPattern>& pats,
                     bool diag_only) {
     auto F = build_forest(c, bodies, PC_LEAF);
     pats.resize(bodies.size());
-    for (size_t b = 0; b < bodies.size(); ++b)
-        near_pattern(*F, (int)b, pats[b], diag_only);
+    if (bodies.size() == 1) {
+        near_pattern(*F, 0, pats[0], diag_only, true);
+        return;
+    }
+    host_parallel_for((int64_t)bodies.size(),
+                      [&](int64_t b) { near_pattern(*F, (int)b, pats[(size_t)b], diag_only, false); });
 }
 
-void near_pattern(const Forest& F, int body, NearPattern& P, bool diag_only) {
+void near_pattern(const Forest& F, int body, NearPattern& P, bool diag_only, bool parallel) {
     const int l0 = F.leaf0[(size_t)body], l1 = F.leaf0[(size_t)body + 1];
     std::vector<const TreeNode*> leaves;
     for (int l = l0; l < l1; ++l) leaves.push_back(&F.nodes[(size_t)F.leaves[(size_t)l]]);
     P.n = F.n(body);
     P.nc = (int)leaves.size();
+    const int nc = P.nc;
     // the leaves are consecutive ranges of the body's cluster order
     P.cl_idx.assign(F.perm.begin() + F.pt0[(size_t)body], F.perm.begin() + F.pt0[(size_t)body + 1]);
     P.cl_off.assign(1, 0);
     for (const TreeNode* l : leaves) P.cl_off.push_back(l->end);
-    P.nb_off.assign(1, 0);
-    P.nb_d.clear();
-    P.nb_blk.clear();
-    int64_t entries = 0;
-    P.pair_i.clear();
-    P.pair_j.clear();
-    P.pair_dst.clear();
-    for (int c = 0; c < P.nc; ++c) {
-        std::vector<int> near{c};
-        for (int d = 0; d < P.nc && !diag_only; ++d) {
+    auto size_of = [&](int c) { return P.cl_off[(size_t)c + 1] - P.cl_off[(size_t)c]; };
+    auto each_leaf = [&](const std::function<void(int64_t)>& f) {
+        if (parallel) host_parallel_for(nc, f);
+        else
+            for (int64_t c = 0; c < nc; ++c) f(c);
+    };
+    // near neighbours of every leaf (itself first, then the inadmissible
+    // partners in leaf order) with their block entries and pair counts
+    std::vector<std::vector<int>> near((size_t)nc);
+    std::vector<int64_t> ent((size_t)nc + 1, 0), pairs((size_t)nc + 1, 0);
+    each_leaf([&](int64_t c) {
+        std::vector<int>& nr = near[(size_t)c];
+        nr.push_back((int)c);
+        const int64_t bc = size_of((int)c);
+        int64_t e = bc * bc, q = 0;
+        for (int d = 0; d < nc && !diag_only; ++d) {
             if (d == c) continue;
-            bool adm = std::fmin(leaves[c]->diam, leaves[d]->diam) <= PC_ETA * node_distance(*leaves[c], *leaves[d]);
-            if (!adm) near.push_back(d);
-        }
-        const int64_t bc = P.cl_off[c + 1] - P.cl_off[c];
-        for (int d : near) {
-            const int64_t bd = P.cl_off[d + 1] - P.cl_off[d];
-            P.nb_d.push_back(d);
-            P.nb_blk.push_back(entries);
-            if (d != c) {
-                for (int64_t jj = 0; jj < bd; ++jj)
-                    for (int64_t ii = 0; ii < bc; ++ii) {
-                        P.pair_i.push_back((int32_t)P.cl_idx[(size_t)(P.cl_off[c] + ii)]);
-                        P.pair_j.push_back((int32_t)P.cl_idx[(size_t)(P.cl_off[d] + jj)]);
-                        P.pair_dst.push_back(entries + jj * bc + ii);
-                    }
+            if (!(std::fmin(leaves[(size_t)c]->diam, leaves[(size_t)d]->diam) <=
+                  PC_ETA * node_distance(*leaves[(size_t)c], *leaves[(size_t)d]))) {
+                nr.push_back(d);
+                e += bc * size_of(d);
+                q += bc * size_of(d);
             }
-            entries += bc * bd;
         }
-        P.nb_off.push_back((int32_t)P.nb_d.size());
+        ent[(size_t)c + 1] = e;
+        pairs[(size_t)c + 1] = q;
+    });
+    P.nb_off.assign((size_t)nc + 1, 0);
+    for (int c = 0; c < nc; ++c) {
+        P.nb_off[(size_t)c + 1] = P.nb_off[(size_t)c] + (int32_t)near[(size_t)c].size();
+        ent[(size_t)c + 1] += ent[(size_t)c];
+        pairs[(size_t)c + 1] += pairs[(size_t)c];
     }
-    P.entries = entries;
-    P.npairs = (int64_t)P.pair_i.size();
+    P.entries = ent[(size_t)nc];
+    P.npairs = pairs[(size_t)nc];
+    P.nb_d.resize((size_t)P.nb_off[(size_t)nc]);
+    P.nb_blk.resize((size_t)P.nb_off[(size_t)nc]);
+    P.pair_i.resize((size_t)P.npairs);
+    P.pair_j.resize((size_t)P.npairs);
+    P.pair_dst.resize((size_t)P.npairs);
+    // blocks stored back to back in (leaf, neighbour) order, each b_c x b_d
+    // column-major; the pairs of the off-diagonal ones in storage order
+    each_leaf([&](int64_t c) {
+        const int64_t bc = size_of((int)c), oc = P.cl_off[(size_t)c];
+        int64_t e = ent[(size_t)c], q = pairs[(size_t)c];
+        int32_t t = P.nb_off[(size_t)c];
+        for (int d : near[(size_t)c]) {
+            const int64_t bd = size_of(d), od = P.cl_off[(size_t)d];
+            P.nb_d[(size_t)t] = d;
+            P.nb_blk[(size_t)t] = e;
+            ++t;
+            if (d != c)
+                for (int64_t jj = 0; jj < bd; ++jj)
+                    for (int64_t ii = 0; ii < bc; ++ii, ++q) {
+                        P.pair_i[(size_t)q] = (int32_t)P.cl_idx[(size_t)(oc + ii)];
+                        P.pair_j[(size_t)q] = (int32_t)P.cl_idx[(size_t)(od + jj)];
+                        P.pair_dst[(size_t)q] = e + jj * bc + ii;
+                    }
+            e += bc * bd;
+        }
+    });
 }
 
 // ---------------------------------------------------------------------------
@@ -254,38 +290,35 @@ constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH * NF, OFF_W2 = OFF_B1 + NH, OFF_B
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16(x)); }
 __device__ __forceinline__ float tanh_act(float x) { return tanhf(x); }
 
-// Pair features (geometry and ka only) and the output scale.
+// Pair features (geometry and ka only) and the output scale.  The
+// coordinate differences are taken in FP64 (near pairs share their leading
+// digits), everything after in FP32: every feature is rounded to BF16 and
+// the scale multiplies an FP32 entry.  One pair per thread, its 16 features
+// written as four 16-byte stores.
 __global__ void pc_features_kernel(int64_t P, const int32_t* __restrict__ pi, const int32_t* __restrict__ pj,
                                    int64_t npad, const double* __restrict__ geo, double k, float* __restrict__ F,
                                    float* __restrict__ scale) {
     int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (p >= P) return;
     const int64_t i = pi[p], j = pj[p];
-    double dx = geo[GX * npad + j] - geo[GX * npad + i], dy = geo[GY * npad + j] - geo[GY * npad + i],
-           dz = geo[GZ * npad + j] - geo[GZ * npad + i];
-    double r = sqrt(dx * dx + dy * dy + dz * dz);
-    double ai = geo[GAREA * npad + i], aj = geo[GAREA * npad + j];
-    double h = sqrt(ai);
-    double kr = k * r;
-    float* f = F + p * NF;
-    f[0] = (float)(dx / h);
-    f[1] = (float)(dy / h);
-    f[2] = (float)(dz / h);
-    f[3] = (float)(r / h);
-    f[4] = (float)geo[GNX * npad + i];
-    f[5] = (float)geo[GNY * npad + i];
-    f[6] = (float)geo[GNZ * npad + i];
-    f[7] = (float)geo[GNX * npad + j];
-    f[8] = (float)geo[GNY * npad + j];
-    f[9] = (float)geo[GNZ * npad + j];
-    f[10] = (float)(aj / ai);
-    f[11] = (float)(k * h);
-    f[12] = (float)cos(kr);
-    f[13] = (float)sin(kr);
-    f[14] = (float)(h / r);
-    f[15] = 1.0f;
-    for (int t = 0; t < NF; ++t) f[t] = bf16r(f[t]);
-    scale[p] = (float)(geo[GWA * npad + j] / (4.0 * 3.14159265358979323846 * r));
+    const float dx = (float)(geo[GX * npad + j] - geo[GX * npad + i]);
+    const float dy = (float)(geo[GY * npad + j] - geo[GY * npad + i]);
+    const float dz = (float)(geo[GZ * npad + j] - geo[GZ * npad + i]);
+    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float ai = (float)geo[GAREA * npad + i], aj = (float)geo[GAREA * npad + j];
+    const float h = sqrtf(ai), hinv = 1.0f / h;
+    const float kf = (float)k;
+    float sn, cs;
+    sincosf(kf * r, &sn, &cs);
+    float f[NF] = {dx * hinv, dy * hinv, dz * hinv, r * hinv,
+                   (float)geo[GNX * npad + i], (float)geo[GNY * npad + i], (float)geo[GNZ * npad + i],
+                   (float)geo[GNX * npad + j], (float)geo[GNY * npad + j], (float)geo[GNZ * npad + j],
+                   aj / ai, kf * h, cs, sn, h / r, 1.0f};
+    float4* out = reinterpret_cast<float4*>(F + p * NF);
+#pragma unroll
+    for (int t = 0; t < NF / 4; ++t)
+        out[t] = make_float4(bf16r(f[4 * t]), bf16r(f[4 * t + 1]), bf16r(f[4 * t + 2]), bf16r(f[4 * t + 3]));
+    scale[p] = (float)geo[GWA * npad + j] / (4.0f * 3.14159265358979f * r);
 }
 
 // C = act(op(A) op(B) + bias) (+ C when accumulate).  Row-major storage;
@@ -666,7 +699,9 @@ struct PairBufs {
     DevBuf pi, pj, dst, F, scale, H1, H2, O;
 };
 
-static void upload_pairs(Context& c, const NearPattern& pat, PairBufs& b) {
+// The pattern's pair lists on the device, and the per-pair buffers: the
+// features and scales, plus the activations when the network is trained.
+static void upload_pairs(Context& c, const NearPattern& pat, PairBufs& b, bool training) {
     const int64_t P = std::max<int64_t>(pat.npairs, 1);
     b.pi.ensure(sizeof(int32_t) * P);
     b.pj.ensure(sizeof(int32_t) * P);
@@ -681,20 +716,24 @@ static void upload_pairs(Context& c, const NearPattern& pat, PairBufs& b) {
     }
     b.F.ensure(sizeof(float) * P * NF);
     b.scale.ensure(sizeof(float) * P);
-    b.H1.ensure(sizeof(float) * P * NH);
-    b.H2.ensure(sizeof(float) * P * NH);
-    b.O.ensure(sizeof(float) * P * NO);
+    if (training) {
+        b.H1.ensure(sizeof(float) * P * NH);
+        b.H2.ensure(sizeof(float) * P * NH);
+        b.O.ensure(sizeof(float) * P * NO);
+    }
 }
 
-static void learned_entries(Context& c, const Problem& p, const LearnedNet& net, const NearPattern& pat, PairBufs& b,
-                            double k, float2* Ms) {
-    const int64_t P = pat.npairs;
+// The learned entries of one system: features of its P pairs (pi, pj, dst
+// on the device) into F / scale (room for P pairs), then tensor-core
+// inference writing s_p (o_1 + i o_2) into the system's blocks Ms.
+static void learned_entries(Context& c, const Problem& p, const LearnedNet& net, int64_t P, const int32_t* pi,
+                            const int32_t* pj, const int64_t* dst, float* F, float* scale, double k, float2* Ms,
+                            bool check) {
     if (P == 0) return;
-    pc_features_kernel<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(
-        P, b.pi.as<int32_t>(), b.pj.as<int32_t>(), p.geo.npad, p.geo.arr(0), k, b.F.as<float>(), b.scale.as<float>());
+    pc_features_kernel<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(P, pi, pj, p.geo.npad, p.geo.arr(0), k,
+                                                                          F, scale);
     BEM_CHECK_LAUNCH(&c);
-    // inference on the tensor cores, entries written straight into the blocks
-    mlp_infer_tc(c, net, P, b.F.as<float>(), nullptr, b.dst.as<int64_t>(), b.scale.as<float>(), Ms);
+    mlp_infer_tc(c, net, P, F, nullptr, dst, scale, Ms, check);
 }
 
 struct PcHookData {
@@ -891,12 +930,14 @@ bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond k
         {
             PartTimer pt(c, "pc_learned_entries");
             PairBufs pb;
-            upload_pairs(c, h->data.pat, pb);
+            upload_pairs(c, h->data.pat, pb, false);
+            BEM_CUDA(cudaMemsetAsync(device_err(c), 0, sizeof(int), c.stream));
             for (int s = 0; s < nsys; ++s)
-                learned_entries(c, p, *c.net, h->data.pat, pb, ks[s],
-                                h->data.M.as<float2>() + (size_t)s * h->data.pat.entries);
+                learned_entries(c, p, *c.net, h->data.pat.npairs, pb.pi.as<int32_t>(), pb.pj.as<int32_t>(),
+                                pb.dst.as<int64_t>(), pb.F.as<float>(), pb.scale.as<float>(), ks[s],
+                                h->data.M.as<float2>() + (size_t)s * h->data.pat.entries, false);
             h->use_off = true;
-            c.sync();
+            check_device_err(c);
         }
         PartTimer pt(c, "pc_gate");
         learned_gate(c, h->data, ws, 17);
@@ -974,16 +1015,42 @@ bem_precond precond_setup_multi(Context& c, const std::vector<Problem*>& bodies,
     h->use_off = false;
     if (learned) {
         PartTimer pt(c, "pc_learned_entries");
-        PairBufs pb;
+        // every body's pair lists on the device at once; the systems then
+        // run back to back through one feature / scale buffer (stream
+        // order), with no host round trip between them
+        std::vector<int64_t> poff((size_t)nb + 1, 0);
+        int64_t pmax = 1;
         for (int b = 0; b < nb; ++b) {
-            if (pats[(size_t)b].npairs == 0) continue;
-            upload_pairs(c, pats[(size_t)b], pb);
-            for (int s = 0; s < nsys; ++s)
-                if (sys_body[(size_t)s] == b)
-                    learned_entries(c, *bodies[(size_t)b], *c.net, pats[(size_t)b], pb, ks[s],
-                                    d.M.as<float2>() + moff[(size_t)s]);
-            c.sync();  // the pair buffers are reused by the next body
+            poff[(size_t)b + 1] = poff[(size_t)b] + pats[(size_t)b].npairs;
+            pmax = std::max(pmax, pats[(size_t)b].npairs);
         }
+        PairBufs pb;
+        const int64_t ptot = std::max<int64_t>(poff[(size_t)nb], 1);
+        pb.pi.ensure(sizeof(int32_t) * ptot);
+        pb.pj.ensure(sizeof(int32_t) * ptot);
+        pb.dst.ensure(sizeof(int64_t) * ptot);
+        pb.F.ensure(sizeof(float) * pmax * NF);
+        pb.scale.ensure(sizeof(float) * pmax);
+        for (int b = 0; b < nb; ++b) {
+            const NearPattern& q = pats[(size_t)b];
+            if (q.npairs == 0) continue;
+            const size_t o = (size_t)poff[(size_t)b];
+            BEM_CUDA(cudaMemcpyAsync(pb.pi.as<int32_t>() + o, q.pair_i.data(), sizeof(int32_t) * q.npairs,
+                                     cudaMemcpyHostToDevice, c.stream));
+            BEM_CUDA(cudaMemcpyAsync(pb.pj.as<int32_t>() + o, q.pair_j.data(), sizeof(int32_t) * q.npairs,
+                                     cudaMemcpyHostToDevice, c.stream));
+            BEM_CUDA(cudaMemcpyAsync(pb.dst.as<int64_t>() + o, q.pair_dst.data(), sizeof(int64_t) * q.npairs,
+                                     cudaMemcpyHostToDevice, c.stream));
+        }
+        BEM_CUDA(cudaMemsetAsync(device_err(c), 0, sizeof(int), c.stream));
+        for (int s = 0; s < nsys; ++s) {
+            const int b = sys_body[(size_t)s];
+            const size_t o = (size_t)poff[(size_t)b];
+            learned_entries(c, *bodies[(size_t)b], *c.net, pats[(size_t)b].npairs, pb.pi.as<int32_t>() + o,
+                            pb.pj.as<int32_t>() + o, pb.dst.as<int64_t>() + o, pb.F.as<float>(),
+                            pb.scale.as<float>(), ks[s], d.M.as<float2>() + moff[(size_t)s], false);
+        }
+        check_device_err(c);
         h->use_off = true;
     }
     if (learned) {
@@ -1029,7 +1096,7 @@ double learned_train(Context& c, std::vector<Problem*>& probs, int steps, int np
         b->p = p;
         b->pc.pat = std::move(pats[bodies.size()]);
         upload_pattern(c, b->pc);
-        upload_pairs(c, b->pc.pat, b->pb);
+        upload_pairs(c, b->pc.pat, b->pb, true);
         b->nf = (int)p->freqs.size();
         b->lda = p->geo.npad;
         b->mstride = (size_t)b->lda * p->n;

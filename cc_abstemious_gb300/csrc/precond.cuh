@@ -39,8 +39,10 @@ struct Forest;
 // block-Jacobi pattern); pats[b] belongs to bodies[b].
 void build_patterns(Context& c, const std::vector<const Problem*>& bodies, std::vector<NearPattern>& pats,
                     bool diag_only);
-// The pattern of one body of a forest built at leaf size 64.
-void near_pattern(const Forest& F, int body, NearPattern& P, bool diag_only);
+// The pattern of one body of a forest built at leaf size 64, its leaves on
+// parallel host threads when `parallel` is set (the same result either way;
+// not from inside another host_parallel_for item).
+void near_pattern(const Forest& F, int body, NearPattern& P, bool diag_only, bool parallel);
 // Installs the preconditioner on the batch; returns the kind actually used
 // (the learned form falls back to block-Jacobi when no network is available).
 bem_precond precond_setup(Context& c, Problem& p, GmWorkspace& ws, bem_precond kind, const double* ks);
@@ -62,8 +64,10 @@ double learned_train(Context& c, std::vector<Problem*>& probs, int steps, int np
 void learned_mlp_eval(Context& c, int64_t P, const float* F, const float* dO, float* O, float* grad);
 void learned_mlp_infer(Context& c, int64_t P, const float* F, float* O);
 // Tensor-core inference (tc_mlp.cu): outputs to O (P x 2) and/or the learned
-// entries s_p (o_1 + i o_2) to M[dst[p]].
+// entries s_p (o_1 + i o_2) to M[dst[p]].  With check = false the call
+// neither clears nor reads the context's device error flag (the caller
+// clears it before a series of calls and checks it after).
 void mlp_infer_tc(Context& c, const LearnedNet& net, int64_t P, const float* F, float* O, const int64_t* dst,
-                  const float* scale, float2* M);
+                  const float* scale, float2* M, bool check = true);
 
 }  // namespace bem
