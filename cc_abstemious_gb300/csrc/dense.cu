@@ -9,29 +9,55 @@ namespace bem {
 constexpr int LU_NB = 32;
 
 // ---------------------------------------------------------------------------
-// Pivot search (nalgebra icamax): first row r >= c maximising |re| + |im|.
-__global__ void lu_pivot_kernel(int64_t n, const double2* __restrict__ A, int64_t lda, int64_t c,
-                                int32_t* __restrict__ piv, int* __restrict__ info) {
+// Partial-pivot LU in panels of LU_NB columns.  Within a panel the columns are
+// eliminated one launch each: the launch for column c scales column c below
+// the diagonal and updates the rest of the panel, and its last CTA to finish
+// picks column c + 1's pivot and swaps the two rows inside the panel.  The
+// other columns take the panel's row swaps together afterwards
+// (lu_laswp_kernel: nalgebra swaps whole rows at every step, and swaps of
+// distinct columns commute), then the row block U12 and the trailing update.
+
+// Pivot search (nalgebra icamax): first row r >= c maximising |re| + |im| of
+// column c, by the whole CTA (a multiple of 32 threads, at most 1024); records
+// piv[c] (and info on a zero column) and returns the row to every thread.
+// Loads bypass L1: in the panel kernel the column was just written by other
+// CTAs.
+__device__ __forceinline__ int64_t lu_pivot_block(int64_t n, const double2* __restrict__ A, int64_t lda, int64_t c,
+                                                  int32_t* __restrict__ piv, int* __restrict__ info) {
     __shared__ double bv[32];
     __shared__ int64_t bi[32];
+    __shared__ int64_t res;
+    const double2* col = A + c * lda;
+    // four interleaved partial maxima keep four loads in flight
     double best = -1.0;
     int64_t bidx = c;
-    const double2* col = A + c * lda;
-    for (int64_t r = c + threadIdx.x; r < n; r += blockDim.x) {
-        double v = fabs(col[r].x) + fabs(col[r].y);
-        if (v > best) { best = v; bidx = r; }
+    const int64_t stride = blockDim.x;
+    for (int64_t r0 = c + threadIdx.x; r0 < n; r0 += 4 * stride) {
+        double v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t r = r0 + u * stride;
+            const double2 e = r < n ? __ldcg(col + r) : make_double2(-1.0, 0.0);
+            v[u] = r < n ? fabs(e.x) + fabs(e.y) : -1.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (v[u] > best) {  // rows visited in increasing order per thread: first maximum kept
+                best = v[u];
+                bidx = r0 + u * stride;
+            }
     }
-    // warp reduce (ties -> smaller row index)
+    // warp and block reduction (ties -> smaller row index)
     for (int off = 16; off > 0; off >>= 1) {
         double ov = __shfl_down_sync(0xffffffffu, best, off);
         int64_t oi = __shfl_down_sync(0xffffffffu, bidx, off);
         if (ov > best || (ov == best && oi < bidx)) { best = ov; bidx = oi; }
     }
-    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     if (l == 0) { bv[w] = best; bi[w] = bidx; }
     __syncthreads();
     if (w == 0) {
-        int nw = blockDim.x >> 5;
+        const int nw = blockDim.x >> 5;
         best = l < nw ? bv[l] : -1.0;
         bidx = l < nw ? bi[l] : c;
         for (int off = 16; off > 0; off >>= 1) {
@@ -42,37 +68,82 @@ __global__ void lu_pivot_kernel(int64_t n, const double2* __restrict__ A, int64_
         if (l == 0) {
             piv[c] = (int32_t)bidx;
             if (best == 0.0 && *info == 0) *info = (int)(c + 1);
+            res = bidx;
         }
+    }
+    __syncthreads();
+    return res;
+}
+
+// Rows c and p swapped in the panel's columns [p0, pend).
+__device__ __forceinline__ void lu_swap_panel(double2* __restrict__ A, int64_t lda, int64_t c, int64_t p, int64_t p0,
+                                              int64_t pend) {
+    if (p == c) return;
+    for (int64_t j = p0 + threadIdx.x; j < pend; j += blockDim.x) {
+        const double2 t = __ldcg(A + j * lda + c);
+        A[j * lda + c] = __ldcg(A + j * lda + p);
+        A[j * lda + p] = t;
     }
 }
 
-// Swap rows c and piv[c] over all columns (nalgebra swaps the factored part
-// and the trailing part; together that is the full row).
-__global__ void lu_swap_kernel(int64_t ncols, double2* __restrict__ A, int64_t lda, int64_t c,
-                               const int32_t* __restrict__ piv) {
-    int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    int64_t p = piv[c];
-    if (j >= ncols || p == c) return;
-    double2 t = A[j * lda + c];
-    A[j * lda + c] = A[j * lda + p];
-    A[j * lda + p] = t;
+// The panel's first column: pivot and swap inside the panel.
+__global__ void lu_pivot_swap_kernel(int64_t n, double2* __restrict__ A, int64_t lda, int64_t c, int64_t p0,
+                                     int64_t pend, int32_t* __restrict__ piv, int* __restrict__ info) {
+    const int64_t p = lu_pivot_block(n, A, lda, c, piv, info);
+    lu_swap_panel(A, lda, c, p, p0, pend);
 }
 
 // gauss_step restricted to the panel: scale column c below the diagonal by
-// 1/A[c,c] and apply the rank-1 update to panel columns c+1 .. pend-1.
-__global__ void lu_panel_update_kernel(int64_t n, double2* __restrict__ A, int64_t lda, int64_t c, int64_t pend) {
-    int64_t r = c + 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (r >= n) return;
-    double2 d = A[c * lda + c];
-    if (d.x == 0.0 && d.y == 0.0) return;  // singular column: nalgebra skips the step
-    double2 inv = cdiv(make_double2(1.0, 0.0), d);
-    double2 l = cmul(A[c * lda + r], inv);
-    A[c * lda + r] = l;
-    for (int64_t j = c + 1; j < pend; ++j) {
-        double2 u = A[j * lda + c];
-        double2 a = A[j * lda + r];
-        cfma(a, cneg(l), u);
-        A[j * lda + r] = a;
+// 1/A[c,c] and apply the rank-1 update to panel columns c+1 .. pend-1 (one row
+// per thread); then the last CTA pivots column c + 1 and swaps inside the
+// panel.  `ticket` is zero on entry and left zero.
+constexpr int LU_STEP_THREADS = 1024;
+__global__ void __launch_bounds__(LU_STEP_THREADS) lu_panel_step_kernel(int64_t n, double2* __restrict__ A,
+                                                                        int64_t lda, int64_t c, int64_t p0,
+                                                                        int64_t pend, int32_t* __restrict__ piv,
+                                                                        int* __restrict__ info,
+                                                                        int* __restrict__ ticket) {
+    __shared__ int last;
+    const int64_t r = c + 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const double2 d = A[c * lda + c];
+    if (r < n && !(d.x == 0.0 && d.y == 0.0)) {  // singular column: nalgebra skips the step
+        const double2 inv = cdiv(make_double2(1.0, 0.0), d);
+        const double2 l = cmul(A[c * lda + r], inv);
+        A[c * lda + r] = l;
+        for (int64_t j = c + 1; j < pend; ++j) {
+            const double2 u = A[j * lda + c];
+            double2 a = A[j * lda + r];
+            cfma(a, cneg(l), u);
+            A[j * lda + r] = a;
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        last = atomicAdd(ticket, 1) == (int)gridDim.x - 1;
+        if (last) *ticket = 0;
+    }
+    __syncthreads();
+    if (!last || c + 1 >= pend) return;
+    __threadfence();
+    const int64_t p = lu_pivot_block(n, A, lda, c + 1, piv, info);
+    lu_swap_panel(A, lda, c + 1, p, p0, pend);
+}
+
+// The panel's row swaps piv[p0 .. pend) applied in order to every column
+// outside the panel (one thread per column).
+__global__ void lu_laswp_kernel(int64_t n, double2* __restrict__ A, int64_t lda, int64_t p0, int64_t pend,
+                                const int32_t* __restrict__ piv) {
+    int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= n - (pend - p0)) return;
+    if (j >= p0) j += pend - p0;
+    double2* col = A + j * lda;
+    for (int64_t c = p0; c < pend; ++c) {
+        const int64_t p = piv[c];
+        if (p == c) continue;
+        const double2 t = col[c];
+        col[c] = col[p];
+        col[p] = t;
     }
 }
 
@@ -159,19 +230,23 @@ __global__ void __launch_bounds__(256) lu_gemm_kernel(double2* __restrict__ M, i
 
 void lu_factor_fp64(Context& ctx, int64_t n, double2* A, int64_t lda, int32_t* d_piv, int* d_info) {
     BEM_CUDA(cudaMemsetAsync(d_info, 0, sizeof(int), ctx.stream));
+    ctx.w_flags.ensure(256);
+    int* ticket = ctx.w_flags.as<int>() + 2;  // [0] device error, [1] the caller's info
+    BEM_CUDA(cudaMemsetAsync(ticket, 0, sizeof(int), ctx.stream));
     for (int64_t p0 = 0; p0 < n; p0 += LU_NB) {
         int nb = (int)std::min<int64_t>(LU_NB, n - p0);
         int64_t pend = p0 + nb;
-        for (int64_t c = p0; c < pend; ++c) {
-            lu_pivot_kernel<<<1, 1024, 0, ctx.stream>>>(n, A, lda, c, d_piv, d_info);
+        lu_pivot_swap_kernel<<<1, 1024, 0, ctx.stream>>>(n, A, lda, p0, p0, pend, d_piv, d_info);
+        BEM_CHECK_LAUNCH(&ctx);
+        for (int64_t c = p0; c < pend && c + 1 < n; ++c) {
+            const int64_t rows = n - c - 1;
+            lu_panel_step_kernel<<<(unsigned)((rows + LU_STEP_THREADS - 1) / LU_STEP_THREADS), LU_STEP_THREADS, 0,
+                                   ctx.stream>>>(n, A, lda, c, p0, pend, d_piv, d_info, ticket);
             BEM_CHECK_LAUNCH(&ctx);
-            lu_swap_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx.stream>>>(n, A, lda, c, d_piv);
+        }
+        if (n > nb) {
+            lu_laswp_kernel<<<(unsigned)((n - nb + 255) / 256), 256, 0, ctx.stream>>>(n, A, lda, p0, pend, d_piv);
             BEM_CHECK_LAUNCH(&ctx);
-            if (c + 1 < n) {
-                lu_panel_update_kernel<<<(unsigned)((n - c - 1 + 255) / 256), 256, 0, ctx.stream>>>(n, A, lda, c,
-                                                                                                   pend);
-                BEM_CHECK_LAUNCH(&ctx);
-            }
         }
         int64_t rest = n - pend;
         if (rest <= 0) continue;
