@@ -492,7 +492,7 @@ def main():
 
 
 # ---------------------------------------------------------------------------
-# Target workloads: the configurations the benchmark spec's target is stated on
+# Target workloads: the configurations the throughput target is stated on
 # (perturbed-sphere batch, held-out learned body, ellipsoid).  At N = 1 the
 # default line carries one record per target under "targets"; --workload
 # prints one target as its own line.  Each record times every form on the

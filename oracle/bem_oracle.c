@@ -1,7 +1,7 @@
 /*
  * bem_oracle.c -- CPU FP64 restatement of the cc_abstemious BEM hot path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker).  See bem_oracle.h for the scope and
+ * TEST INFRASTRUCTURE ONLY (the oracle).  See bem_oracle.h for the scope and
  * the golden values that pin it.  Built with -ffp-contract=off and
  * -fcx-limited-range so that complex arithmetic follows num-complex 0.4.6's
  * textbook formulas and no fused multiply-adds are introduced.

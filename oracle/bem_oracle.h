@@ -1,7 +1,7 @@
 /*
  * bem_oracle.h -- CPU FP64 restatement of the cc_abstemious BEM hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: the tests, the
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle: the tests, the
  * smoke check and the CPU-baseline leg of the benchmark may call it; the
  * product path (cc_abstemious_gb300 + libbem_gb300.so) never links or calls it.
  *

@@ -1,6 +1,6 @@
 """Python front end of the CPU oracle (test infrastructure only).
 
-This module is the checker.  Only the tests, ``__graft_entry__.smoke()`` and
+This module is the oracle the GPU results are compared with.  Only the tests, ``__graft_entry__.smoke()`` and
 the CPU-baseline leg of ``bench.py`` import it; the product package
 ``cc_abstemious_gb300`` never does.
 

@@ -2,7 +2,7 @@
 
 Each case restates a test of cc_abstemious (cited) and checks the oracle with
 the reference's tolerance.  These pins are what make the oracle trustworthy
-as the checker for the GPU path."""
+as the reference the GPU path is compared with."""
 import json
 import os
 
