@@ -761,46 +761,38 @@ __device__ __forceinline__ void lu_wait_flag(const int* f, int* err) {
 constexpr int TS_THREADS = 256;  // 64 row pairs x 4 column quarters of a block
 constexpr int TS_MAXR = 4;       // right-hand sides per ticket (systems sharing one operator)
 
-// acc[r] += B v[r] for the row pair of this thread over its 32-column quarter
-// of a block, every right-hand side r < R sharing the loads of B: B's columns
-// at col (stride ld, float2 entries), v[r] in shared memory.
+// Sixteen columns c0 .. c0 + 15 of a block B (columns at col, stride ld,
+// float2 entries) for the row pair of this thread, one float4 per column
+// (zero past the block's nc columns or below its rows).
+__device__ __forceinline__ void lu_block_load(const float2* __restrict__ col, int64_t ld, int c0, int nc,
+                                              bool rows_ok, float4 (&e)[16]) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int c = c0 + i;
+        e[i] = rows_ok && c < nc ? __ldg(reinterpret_cast<const float4*>(col + (int64_t)c * ld))
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// (a0, a1)[r] += those sixteen columns times v[r][c0 ..] for every right-hand
+// side r < R (v in shared memory), in column order.
 template <int R>
-__device__ __forceinline__ void lu_block_mv(const float2* __restrict__ col, int64_t ld, const float2 (*v)[LB],
-                                            int c0, int nc, bool rows_ok, double2 (&acc)[R][2]) {
-    float2 a0[R], a1[R];
+__device__ __forceinline__ void lu_block_fma(const float4 (&e)[16], const float2 (*v)[LB], int c0, float2 (&a0)[R],
+                                             float2 (&a1)[R]) {
 #pragma unroll
-    for (int r = 0; r < R; ++r) a0[r] = a1[r] = make_float2(0.f, 0.f);
+    for (int i = 0; i < 16; ++i)
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        float4 e[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            const int c = c0 + 16 * h + i;
-            e[i] = rows_ok && c < nc ? __ldg(reinterpret_cast<const float4*>(col + (int64_t)c * ld))
-                                     : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int r = 0; r < R; ++r) {
+            const float2 x = v[r][c0 + i];
+            cfmaf_(a0[r], make_float2(e[i].x, e[i].y), x);
+            cfmaf_(a1[r], make_float2(e[i].z, e[i].w), x);
         }
-#pragma unroll
-        for (int i = 0; i < 16; ++i)
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const float2 x = v[r][c0 + 16 * h + i];
-                cfmaf_(a0[r], make_float2(e[i].x, e[i].y), x);
-                cfmaf_(a1[r], make_float2(e[i].z, e[i].w), x);
-            }
-    }
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        acc[r][0].x += a0[r].x;
-        acc[r][0].y += a0[r].y;
-        acc[r][1].x += a1[r].x;
-        acc[r][1].y += a1[r].y;
-    }
 }
 
 // R = the largest group of right-hand sides in the ticket list (1, 2 or 4):
 // smaller groups leave their unused vectors at zero.
 template <int R>
-__global__ void __launch_bounds__(TS_THREADS) lu_trsv_kernel(const LuSys* __restrict__ sys,
+__global__ void __launch_bounds__(TS_THREADS, R == TS_MAXR ? 1 : 2) lu_trsv_kernel(const LuSys* __restrict__ sys,
                                                              const LuTicket* __restrict__ tickets, int ntickets,
                                                              int* __restrict__ counter, int* __restrict__ flags,
                                                              GmBatch bt, int* __restrict__ err) {
@@ -853,6 +845,12 @@ __global__ void __launch_bounds__(TS_THREADS) lu_trsv_kernel(const LuSys* __rest
         __syncthreads();
         for (int i = 0; i < nk; ++i) {
             const int k = fwd ? i : nblk - 1 - i;
+            const int nc = (int)min((int64_t)LB, S.n - (int64_t)k * LB);
+            const float2* col = S.F + (int64_t)k * LB * S.ld + (int64_t)b * LB + 2 * rp;
+            // the factors are final: the first half of this thread's quarter of
+            // the block is requested before the wait for z_k and its staging
+            float4 e[16];
+            lu_block_load(col, S.ld, 32 * cq, nc, rows_ok, e);
             if (i >= seen) {
                 if (threadIdx.x == 0) {
                     // the row's last dependency first: once set, all are
@@ -863,7 +861,6 @@ __global__ void __launch_bounds__(TS_THREADS) lu_trsv_kernel(const LuSys* __rest
                 __syncthreads();
                 seen = all_final ? nk : i + 1;
             }
-            const int nc = (int)min((int64_t)LB, S.n - (int64_t)k * LB);
             for (int u = threadIdx.x; u < R * LB; u += TS_THREADS) {
                 const int r = u / LB, c = u % LB;
                 double2 v = make_double2(0, 0);
@@ -873,10 +870,27 @@ __global__ void __launch_bounds__(TS_THREADS) lu_trsv_kernel(const LuSys* __rest
                 xs[r][c] = make_float2((float)v.x, (float)v.y);
             }
             __syncthreads();
-            const float2* col = S.F + (int64_t)k * LB * S.ld + (int64_t)b * LB + 2 * rp;
-            lu_block_mv<R>(col, S.ld, xs, 32 * cq, nc, rows_ok, acc);
+            // acc[r] += B v[r] over this thread's 32-column quarter, summed in
+            // FP32 within the block
+            float2 a0[R], a1[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) a0[r] = a1[r] = make_float2(0.f, 0.f);
+            lu_block_fma<R>(e, xs, 32 * cq, a0, a1);
+            lu_block_load(col, S.ld, 32 * cq + 16, nc, rows_ok, e);
+            lu_block_fma<R>(e, xs, 32 * cq + 16, a0, a1);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                acc[r][0].x += a0[r].x;
+                acc[r][0].y += a0[r].y;
+                acc[r][1].x += a1[r].x;
+                acc[r][1].y += a1[r].y;
+            }
             __syncthreads();  // xs reused by the next block
         }
+        // the diagonal block's first half is requested before the reductions
+        const float2* D = S.Dm + (size_t)b * LB * LB + 2 * rp;
+        float4 e[16];
+        lu_block_load(D, LB, 32 * cq, nr, rows_ok, e);
         // y = source - sum, per right-hand side
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -904,19 +918,21 @@ __global__ void __launch_bounds__(TS_THREADS) lu_trsv_kernel(const LuSys* __rest
 #pragma unroll
         for (int r = 0; r < R; ++r) d0[r] = d1[r] = make_float2(0.f, 0.f);
         {
-            const float2* D = S.Dm + (size_t)b * LB * LB;
             const int r0 = 2 * rp;
-#pragma unroll 8
-            for (int i = 0; i < 32; ++i) {
-                const int c = 32 * cq + i;
-                if (!rows_ok || c >= nr) continue;
-                const float4 e = __ldg(reinterpret_cast<const float4*>(D + (size_t)c * LB + r0));
-                const bool u0 = fwd ? c < r0 : c >= r0, u1 = fwd ? c < r0 + 1 : c >= r0 + 1;
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const float2 x = xs[r][c];
-                    if (u0) cfmaf_(d0[r], make_float2(e.x, e.y), x);
-                    if (u1) cfmaf_(d1[r], make_float2(e.z, e.w), x);
+            for (int h = 0; h < 2; ++h) {
+                if (h == 1) lu_block_load(D, LB, 32 * cq + 16, nr, rows_ok, e);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int c = 32 * cq + 16 * h + i;
+                    if (!rows_ok || c >= nr) continue;
+                    const bool u0 = fwd ? c < r0 : c >= r0, u1 = fwd ? c < r0 + 1 : c >= r0 + 1;
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const float2 x = xs[r][c];
+                        if (u0) cfmaf_(d0[r], make_float2(e[i].x, e[i].y), x);
+                        if (u1) cfmaf_(d1[r], make_float2(e[i].z, e[i].w), x);
+                    }
                 }
             }
         }
