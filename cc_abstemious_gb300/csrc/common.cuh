@@ -40,7 +40,9 @@ inline void require(bool ok, const std::string& msg, bem_status s = BEM_ERR_BAD_
 // f(i) for every i in [0, n) on the process's host worker threads, the
 // calling thread among them, items handed out one at a time; returns when all
 // are done and rethrows the first exception an item raised.  Calls for
-// distinct i must be safe to run at the same time.
+// distinct i must be safe to run at the same time.  Calls from several host
+// threads take the workers in turn; an item must not call it again (it would
+// wait for itself).
 void host_parallel_for(int64_t n, const std::function<void(int64_t)>& f);
 
 // ---------------------------------------------------------------------------
